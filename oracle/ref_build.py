@@ -1,0 +1,124 @@
+"""Build the reference programs PAisingSSC.cu / PAisingMSC.cu as oracle binaries.
+
+TEST INFRASTRUCTURE ONLY.  Everything this script writes goes to oracle/_ref/
+(git-ignored).  The reference sources are read where they lie; the only
+changes are the ones CUDA 13 forces or the comparison needs:
+
+* legacy texture references were removed in CUDA 12, so the Boltzmann /
+  threshold table bound to ``boltzT`` (PAisingSSC.cu:59,90-94,175,187,477,797;
+  PAisingMSC.cu:63,222-223,255-256,636) becomes a ``__device__`` pointer that
+  is set with cudaMemcpyToSymbol instead of cudaBindTexture;
+* ``#define L 64`` (PAisingSSC.cu:27, PAisingMSC.cu:26) is compile-time in the
+  reference, so one binary is built per lattice size;
+* the ``inj`` variants are compiled with ``-include inj_shim.cuh``, which swaps
+  cuRAND's Philox state for the injected stream H (see inj_stream.h).  The
+  ``curand`` variants keep cuRAND and are the reference's own GPU build.
+
+Step 1 (patch) needs the reference checkout and runs in the build container;
+step 2 (nvcc) runs wherever the patched sources are, e.g. on the GPU host,
+which does not have the reference checkout.
+
+usage: python oracle/ref_build.py [--patch-only] [--sizes 16,64] [--jobs N]
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = "/root/reference"
+OUT = os.path.join(HERE, "_ref")
+SRC_OUT = os.path.join(OUT, "src")
+BIN_OUT = os.path.join(OUT, "bin")
+DEFAULT_SIZES = (16, 64)
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+# (pattern, replacement, expected count) per program
+_COMMON = [
+    (r"CUDAErrChk\( cudaUnbindTexture\(boltzT\) \);", "CUDAErrChk( cudaSuccess );", 1),
+]
+_SSC = [
+    (r"texture<int2,1,cudaReadModeElementType> boltzT;", "__device__ const double* boltzT;", 1),
+    (r"fetch_double\(texture<int2,1> t, int i\)", "fetch_double(const double* t, int i)", 1),
+    (r"int2 v = tex1Dfetch\(t,i\);", "return t[i];", 1),
+    (r"return __hiloint2double\(v\.y, v\.x\);", "", 1),
+    (r"CUDAErrChk\( cudaBindTexture\(NULL,boltzT,boltztext,boltzTableL \* sizeof\(double\)\) \);",
+     "CUDAErrChk( cudaMemcpyToSymbol(boltzT,&boltztext,sizeof(boltztext)) );", 1),
+]
+_MSC = [
+    (r"texture<unsigned int,1,cudaReadModeElementType> boltzT;",
+     "__device__ const unsigned int* boltzT;", 1),
+    (r"tex1Dfetch\(boltzT, ([01])\)", r"boltzT[\1]", 4),
+    (r"CUDAErrChk\( cudaBindTexture\(NULL,boltzT,boltztext,boltzTableL \* sizeof\(unsigned int\)\) \);",
+     "CUDAErrChk( cudaMemcpyToSymbol(boltzT,&boltztext,sizeof(boltztext)) );", 1),
+]
+
+
+def _patch(text: str, rules, L: int) -> str:
+    for pat, rep, n in rules + _COMMON:
+        text, k = re.subn(pat, rep, text)
+        if k != n:
+            raise RuntimeError(f"pattern {pat!r}: {k} matches, expected {n}")
+    text, k = re.subn(r"^#define L\s+64\b", f"#define L\t{L}", text, flags=re.M)
+    if k != 1:
+        raise RuntimeError("#define L not found")
+    return text
+
+
+def patch(sizes) -> None:
+    os.makedirs(SRC_OUT, exist_ok=True)
+    for prog, rules in (("SSC", _SSC), ("MSC", _MSC)):
+        with open(os.path.join(REF_DIR, f"PAising{prog}.cu")) as f:
+            text = f.read()
+        for L in sizes:
+            with open(os.path.join(SRC_OUT, f"PAising{prog}_L{L}.cu"), "w") as f:
+                f.write(_patch(text, rules, L))
+    shutil.copy(os.path.join(HERE, "inj_shim.cuh"), SRC_OUT)
+    shutil.copy(os.path.join(HERE, "inj_stream.h"), SRC_OUT)
+
+
+def _compile(src: str, variant: str) -> str:
+    base = os.path.splitext(os.path.basename(src))[0]
+    out = os.path.join(BIN_OUT, f"{base}_{variant}")
+    cmd = ["nvcc", "-O3", ARCH, "-w", "-o", out, src]
+    if variant == "inj":
+        cmd[1:1] = ["-include", os.path.join(SRC_OUT, "inj_shim.cuh"), "-I", SRC_OUT]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {out}:\n{r.stderr[-2000:]}")
+    return out
+
+
+def compile_all(jobs: int) -> list[str]:
+    os.makedirs(BIN_OUT, exist_ok=True)
+    srcs = sorted(f for f in os.listdir(SRC_OUT) if f.endswith(".cu") and f.startswith("PAising"))
+    tasks = [(os.path.join(SRC_OUT, s), v) for s in srcs for v in ("inj", "curand")]
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        return list(ex.map(lambda a: _compile(*a), tasks))
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--patch-only", action="store_true")
+    ap.add_argument("--sizes", default=",".join(map(str, DEFAULT_SIZES)))
+    ap.add_argument("--jobs", type=int, default=min(8, os.cpu_count() or 1))
+    a = ap.parse_args(argv)
+    sizes = [int(s) for s in a.sizes.split(",") if s]
+    if os.path.isdir(REF_DIR):
+        patch(sizes)
+    elif not os.path.isdir(SRC_OUT):
+        print("reference sources unavailable and no patched copy present", file=sys.stderr)
+        return 1
+    if not a.patch_only:
+        for b in compile_all(a.jobs):
+            print(b)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
