@@ -1,0 +1,181 @@
+/*
+ * paising.h -- C ABI of the GB300 population-annealing engine (2D +-J=1
+ * ferromagnetic Ising model, periodic L x L lattice, no field).
+ *
+ * The reference (LevBarash/PAising) is two CUDA programs without a library
+ * interface: its drop-in surface is the command line and the results file
+ * (PAisingSSC.cu:367-404 flags, 670-692 output; PAisingMSC.cu:532-569,
+ * 820-842).  The handle API below carries exactly those parameters and rows;
+ * the stage entry points replace the reference's kernels one by one and are
+ * what the parity tests call.
+ *
+ * Conventions: every function returns a pa_status (0 = success); no
+ * exception or process exit crosses the boundary (the reference aborts with
+ * exit() on any CUDA error, PAisingSSC.cu:80-88).  The library owns the
+ * device memory of a handle; the caller owns every host buffer it passes.
+ * Stage entry points take device pointers and a cudaStream_t passed as
+ * void* (NULL = the legacy default stream) and synchronise that stream
+ * before returning.  A handle is not thread-safe.
+ */
+#ifndef PAISING_H
+#define PAISING_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PA_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define PA_API __attribute__((visibility("default")))
+#else
+#define PA_API
+#endif
+
+enum pa_status {
+  PA_OK = 0,
+  PA_ERR_ARG = 1,          /* invalid argument or unsupported size */
+  PA_ERR_CUDA = 2,         /* a CUDA call failed (message in pa_last_error) */
+  PA_ERR_CAPACITY = 3,     /* the population outgrew its preallocated buffer */
+  PA_ERR_EXTINCT = 4,      /* resampling produced an empty population */
+  PA_ERR_STATE = 5,        /* call out of order (e.g. rows before a run) */
+  PA_ERR_TOO_MANY_STEPS = 6 /* schedule longer than nBmax = 10000 (PAisingSSC.cu:634-641) */
+};
+
+enum pa_coding { PA_CODING_SSC = 0, PA_CODING_MSC = 1 };
+/* PA_RNG_NATIVE: the engine's own Philox streams.  PA_RNG_REFERENCE: every
+ * random number is the Philox4x32-10 word the reference would draw at the
+ * same (subsequence, counter) coordinates -- the injected test stream that
+ * makes spins, energies and copy numbers bit-exact with the reference
+ * programs built against the same stream. */
+enum pa_rng_mode { PA_RNG_NATIVE = 0, PA_RNG_REFERENCE = 1 };
+/* resampling weights: FP32 with compensated sums (default) or FP64 in the
+ * reference's formulation (Emean shift) */
+enum pa_weights { PA_WEIGHTS_FP32 = 0, PA_WEIGHTS_FP64 = 1 };
+
+typedef struct pa_config {
+  int L;             /* lattice size; #define L (PAisingSSC.cu:27), a runtime value here */
+  int R;             /* initial population size, -R Rinit (PAisingSSC.cu:46,390) */
+  int sweeps;        /* equilibration sweeps per temperature, -t (PAisingSSC.cu:35,391) */
+  double dbeta;      /* inverse temperature step, -d (PAisingSSC.cu:39,392) */
+  double beta_final; /* final inverse temperature, -f (PAisingSSC.cu:38,393) */
+  int runs;          /* independent runs, -M (PAisingSSC.cu:48,394) */
+  uint64_t seed;     /* -s RNGseed (PAisingSSC.cu:395) */
+  int coding;        /* pa_coding: PAisingSSC or PAisingMSC */
+  int rng_mode;      /* pa_rng_mode */
+  int weights;       /* pa_weights */
+  int graph;         /* 1: each run is one CUDA graph launch; 0: host steps every temperature */
+  int device;        /* CUDA device ordinal */
+  double capacity;   /* replica buffer = ceil(capacity * R) + 256; 0 selects 1.25 */
+} pa_config;
+
+/* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */
+typedef struct pa_row {
+  double beta, e, c, m, m2, m4, bf, s, r, lnq;
+} pa_row;
+
+typedef struct pa_handle pa_handle;
+
+/* Fills cfg with the reference defaults: L=64, R=20000, 100 sweeps,
+ * dbeta=0.005, beta_final=1, 1 run, seed 1, SSC, native RNG, FP32 weights,
+ * graph mode (PAisingSSC.cu:27,35-50). */
+PA_API int pa_config_init(pa_config* cfg);
+
+/* Allocates the population buffers for cfg on cfg->device.  Replaces the
+ * set-up part of main() (PAisingSSC.cu:438-479). */
+PA_API int pa_create(const pa_config* cfg, pa_handle** out);
+
+/* Runs cfg->runs full anneals (beta from 0 while beta <= beta_final), the
+ * population-annealing loop of main() (PAisingSSC.cu:481-664,
+ * PAisingMSC.cu:640-814). */
+PA_API int pa_run(pa_handle* h);
+
+/* Number of rows per run of the last pa_run (schedule length + 1). */
+PA_API int pa_num_rows(const pa_handle* h, int* nrows);
+
+/* Copies the rows of run `run` (the contents of PA_results_run_<run>.dat,
+ * PAisingSSC.cu:670-692) into rows[0..max_rows). */
+PA_API int pa_get_rows(const pa_handle* h, int run, pa_row* rows, int max_rows, int* nrows);
+
+/* Device time of the last pa_run in milliseconds (CUDA events around all
+ * runs), and the reference's spin-flip attempt count
+ * sweeps * N * sum_{i>=1} R_i over all runs (PAisingSSC.cu:632,806). */
+PA_API int pa_get_timing(const pa_handle* h, double* ms, double* attempts);
+
+/* Writes dir/PA_results_run_<r>.dat for every run with `precision`
+ * significant digits (PAisingSSC.cu:670-692). */
+PA_API int pa_write_results(const pa_handle* h, const char* dir, int precision);
+
+PA_API int pa_destroy(pa_handle* h);
+
+PA_API const char* pa_status_string(int status);
+/* Message of the last failure on this handle (or of the last failed
+ * handle-less call when h is NULL). */
+PA_API const char* pa_last_error(const pa_handle* h);
+PA_API int pa_abi_version(void);
+
+/* The inverse-temperature schedule of a run: betas[0] = 0 and
+ * betas[i] = betas[i-1] + dbeta while betas[i] <= beta_final, accumulated in
+ * FP64 exactly like the reference (PAisingSSC.cu:508-510,661), so
+ * dbeta = 0.005 stops at 0.995 (200 rows).  Writes at most max entries;
+ * *n receives the full length. */
+PA_API int pa_schedule(double dbeta, double beta_final, double* betas, int max, int* n);
+
+/* The random word the reference would draw as number ctr of the cuRAND
+ * subsequence subseq under the injected stream (Philox4x32-10 keyed by seed,
+ * counter (ctr >> 2, subseq), word ctr & 3).  Host-side, for checks. */
+PA_API uint32_t pa_ref_word(uint64_t seed, uint64_t subseq, uint64_t ctr);
+
+/* ------------------------------------------------------------------------
+ * Stage entry points (device pointers).  Layouts:
+ *   SSC spins : int8 [R][N], +-1, sublattice A (x+y even) then B, site (x,y)
+ *               at y*L/2 + x/2 inside a sublattice (PAisingSSC.cu:70-77,169)
+ *   MSC words : uint32 [rg][N], same split; bit k = replica k of the group,
+ *               1 == +1 (PAisingMSC.cu:84-92); active: uint8 [rg*32]
+ *   energies  : int32 E, M per replica (MSC: index 32*group + bit)
+ * `iseq` is the reference's subsequence counter (initial_sequence,
+ * PAisingSSC.cu:418) at the call; `step` keys the native stream.
+ * ------------------------------------------------------------------------ */
+
+/* ReplicaInit (PAisingSSC.cu:150-157): R random +-1 lattices. */
+PA_API int pa_ssc_init(int8_t* spins, int L, int R, uint64_t seed, uint64_t iseq, void* stream);
+
+/* checkKerALL + energyKer (PAisingSSC.cu:159-215): `sweeps` checkerboard
+ * Metropolis sweeps at inverse temperature beta, then E and M per replica. */
+PA_API int pa_ssc_sweep(int8_t* spins, int L, int R, int sweeps, double beta, int rng_mode, uint64_t seed,
+                 uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream);
+
+/* ReplicaInit (PAisingMSC.cu:169-188): ceil(R/32) groups, active bits. */
+PA_API int pa_msc_init(uint32_t* words, uint8_t* active, int L, int R, uint64_t seed, uint64_t iseq, void* stream);
+
+/* checkKerALL + energyKer (PAisingMSC.cu:191-317) for rg groups. */
+PA_API int pa_msc_sweep(uint32_t* words, const uint8_t* active, int L, int rg, int sweeps, double beta, int rng_mode,
+                 uint64_t seed, uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream);
+
+/* QKer + host lnQ + CalcTauKer + CalcParSum (PAisingSSC.cu:217-270,533;
+ * PAisingMSC.cu:319-395): from the energies of the population before
+ * resampling (n = R_prev for SSC, 32 * ceil(R_prev/32) slots with `active`
+ * for MSC) computes copy numbers roff[n], their exclusive scan offs[n], the
+ * gather map src[R_new] (new replica -> old linear index) and, in the HOST
+ * array out[3], out[0] = lnQ, out[1] = q, out[2] = R_new.  e_ref is Emean for
+ * FP64 weights and Emin for FP32 weights.  Uses internal scratch memory. */
+PA_API int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding, int R_prev, int Rinit, int Rcap,
+                     double beta_prev, double beta, double e_ref, int weights, uint64_t seed, uint64_t iseq,
+                     uint32_t* roff, uint32_t* offs, uint32_t* src, double* out, void* stream);
+
+/* resampleKer (PAisingSSC.cu:272-280): new[s] = old[src[s]], s < R_new. */
+PA_API int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_new, int8_t* new_spins, void* stream);
+
+/* resampleKer (PAisingMSC.cu:397-435): new group j, bit k <- old replica
+ * src[k*rg_new + j], rg_new = ceil(R_new/32); new_active filled. */
+PA_API int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R_new, uint32_t* new_words,
+                    uint8_t* new_active, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PAISING_H */

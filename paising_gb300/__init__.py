@@ -1,0 +1,199 @@
+"""GB300-native population annealing for the 2D Ising ferromagnet.
+
+Python mirror of the C ABI in include/paising.h (loaded with ctypes from the
+in-tree build paising_gb300/_lib/libpaising.so).  There is no CPU fallback:
+if the library is missing, importing the bindings raises.
+
+The reference (LevBarash/PAising) is driven from its command line; the same
+parameters appear here as keyword arguments with the reference defaults
+(PAisingSSC.cu:27,35-50):
+
+    >>> from paising_gb300 import Engine
+    >>> with Engine(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0,
+    ...             coding="msc", seed=100) as eng:
+    ...     eng.run()
+    ...     rows = eng.rows()      # columns of PA_results_run_0.dat
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "Engine", "PaisingError", "anneal", "load_library", "lib", "COLUMNS", "SSC", "MSC",
+    "RNG_NATIVE", "RNG_REFERENCE", "schedule", "ref_word", "WEIGHTS_FP32", "WEIGHTS_FP64", "library_path",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(_HERE, "_lib", "libpaising.so")
+
+SSC, MSC = 0, 1
+RNG_NATIVE, RNG_REFERENCE = 0, 1
+WEIGHTS_FP32, WEIGHTS_FP64 = 0, 1
+# columns of PA_results_run_<r>.dat (PAisingSSC.cu:679-690)
+COLUMNS = ("beta", "E/N", "C/N", "|M|/N", "M2/N^2", "M4/N^4", "betaF/N", "S/N", "R", "lnQ")
+
+_STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity exceeded", 4: "population extinct",
+           5: "call out of order", 6: "too many temperature steps"}
+
+
+class PaisingError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        super().__init__(f"paising status {status} ({_STATUS.get(status, '?')}): {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int), ("R", ctypes.c_int), ("sweeps", ctypes.c_int), ("dbeta", ctypes.c_double),
+                ("beta_final", ctypes.c_double), ("runs", ctypes.c_int), ("seed", ctypes.c_uint64),
+                ("coding", ctypes.c_int), ("rng_mode", ctypes.c_int), ("weights", ctypes.c_int),
+                ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double)]
+
+
+class Row(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("beta", "e", "c", "m", "m2", "m4", "bf", "s", "r", "lnq")]
+
+
+_vp, _i, _u64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double
+_SIGS = {
+    "pa_abi_version": ([], _i),
+    "pa_config_init": ([ctypes.POINTER(Config)], _i),
+    "pa_create": ([ctypes.POINTER(Config), ctypes.POINTER(_vp)], _i),
+    "pa_run": ([_vp], _i),
+    "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
+    "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "pa_write_results": ([_vp, ctypes.c_char_p, _i], _i),
+    "pa_destroy": ([_vp], _i),
+    "pa_status_string": ([_i], ctypes.c_char_p),
+    "pa_last_error": ([_vp], ctypes.c_char_p),
+    "pa_schedule": ([_d, _d, _vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_ref_word": ([_u64, _u64, _u64], ctypes.c_uint32),
+    "pa_ssc_init": ([_vp, _i, _i, _u64, _u64, _vp], _i),
+    "pa_ssc_sweep": ([_vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
+    "pa_msc_init": ([_vp, _vp, _i, _i, _u64, _u64, _vp], _i),
+    "pa_msc_sweep": ([_vp, _vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
+    "pa_resample_plan": ([_vp, _vp, _i, _i, _i, _i, _d, _d, _d, _i, _u64, _u64, _vp, _vp, _vp, _vp, _vp], _i),
+    "pa_ssc_resample": ([_vp, _i, _vp, _i, _vp, _vp], _i),
+    "pa_msc_resample": ([_vp, _i, _vp, _i, _vp, _vp, _vp], _i),
+}
+
+_lib: ctypes.CDLL | None = None
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load libpaising.so and declare every C ABI signature.  Raises if the
+    library has not been built (python -m paising_gb300.build)."""
+    p = path or library_path
+    if not os.path.exists(p):
+        raise ImportError(f"paising CUDA library not built: {p} (run python -m paising_gb300.build)")
+    L = ctypes.CDLL(p)
+    for name, (args, res) in _SIGS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    return L
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load_library()
+    return _lib
+
+
+def _check(status: int, handle=None) -> None:
+    if status != 0:
+        msg = lib().pa_last_error(handle)
+        raise PaisingError(status, msg.decode() if msg else "")
+
+
+_CODING = {"ssc": SSC, "msc": MSC, SSC: SSC, MSC: MSC}
+_RNG = {"native": RNG_NATIVE, "reference": RNG_REFERENCE, RNG_NATIVE: RNG_NATIVE, RNG_REFERENCE: RNG_REFERENCE}
+_W = {"fp32": WEIGHTS_FP32, "fp64": WEIGHTS_FP64, WEIGHTS_FP32: WEIGHTS_FP32, WEIGHTS_FP64: WEIGHTS_FP64}
+
+
+def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, seed=1, coding="ssc",
+                rng="native", weights="fp32", graph=True, device=0, capacity=1.25) -> Config:
+    c = Config()
+    _check(lib().pa_config_init(ctypes.byref(c)))
+    c.L, c.R, c.sweeps, c.dbeta, c.beta_final, c.runs = int(L), int(R), int(sweeps), float(dbeta), float(beta_final), int(runs)
+    c.seed, c.coding, c.rng_mode, c.weights = int(seed), _CODING[coding], _RNG[rng], _W[weights]
+    c.graph, c.device, c.capacity = int(bool(graph)), int(device), float(capacity)
+    return c
+
+
+class Engine:
+    """One population configuration on one GPU (pa_create / pa_run / pa_get_rows)."""
+
+    def __init__(self, **kw):
+        self.config = make_config(**kw)
+        h = ctypes.c_void_p()
+        _check(lib().pa_create(ctypes.byref(self.config), ctypes.byref(h)))
+        self._h = h
+
+    def run(self) -> None:
+        _check(lib().pa_run(self._h), self._h)
+
+    def num_rows(self) -> int:
+        n = ctypes.c_int()
+        _check(lib().pa_num_rows(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+    def rows(self, run: int = 0) -> np.ndarray:
+        n = self.num_rows()
+        out = np.zeros((n, 10), dtype=np.float64)
+        got = ctypes.c_int()
+        _check(lib().pa_get_rows(self._h, run, out.ctypes.data, n, ctypes.byref(got)), self._h)
+        return out[: got.value]
+
+    def timing(self) -> tuple[float, float]:
+        """(device milliseconds of the last run() over all runs, spin-flip attempts)."""
+        ms, att = ctypes.c_double(), ctypes.c_double()
+        _check(lib().pa_get_timing(self._h, ctypes.byref(ms), ctypes.byref(att)), self._h)
+        return ms.value, att.value
+
+    def write_results(self, directory: str, precision: int = 11) -> None:
+        os.makedirs(directory, exist_ok=True)
+        _check(lib().pa_write_results(self._h, directory.encode(), int(precision)), self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pa_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def schedule(dbeta: float = 0.005, beta_final: float = 1.0) -> np.ndarray:
+    """The reference's inverse-temperature schedule (pa_schedule)."""
+    n = ctypes.c_int()
+    lib().pa_schedule(dbeta, beta_final, None, 0, ctypes.byref(n))
+    out = np.zeros(n.value)
+    _check(lib().pa_schedule(dbeta, beta_final, out.ctypes.data, n.value, ctypes.byref(n)))
+    return out
+
+
+def ref_word(seed: int, subseq: int, ctr: int) -> int:
+    return int(lib().pa_ref_word(seed, subseq, ctr))
+
+
+def anneal(**kw) -> np.ndarray:
+    """Run a full anneal and return the rows of run 0 (or all runs stacked
+    when runs > 1)."""
+    with Engine(**kw) as e:
+        e.run()
+        runs = e.config.runs
+        return e.rows(0) if runs == 1 else np.stack([e.rows(r) for r in range(runs)])

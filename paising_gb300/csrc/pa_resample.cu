@@ -1,0 +1,333 @@
+// pa_resample.cu -- resampling of the population on the device, no host
+// round trip, and the per-temperature bookkeeping.
+//
+// Replaces, from the reference (both codings):
+//   QKer        (PAisingSSC.cu:217-234, PAisingMSC.cu:319-345) + host lnQ
+//               (PAisingSSC.cu:533)                  -> q_kernel
+//   CalcTauKer  (PAisingSSC.cu:236-254, PAisingMSC.cu:347-360)
+//   + CalcParSum block totals                        -> copy_numbers_kernel
+//   CalcParSum  (PAisingSSC.cu:256-270, PAisingMSC.cu:362-395)
+//                                                    -> scatter_kernel (exclusive
+//               scan + map new replica -> old replica, consumed by the gathers)
+//   CalcAverages + host observables (PAisingSSC.cu:282-292, 614-630)
+//                                                    -> finish_step_kernel (sums
+//               are accumulated exactly in integers by the sweep kernels)
+//
+// Every multi-block reduction ends with the last-block pattern: each block
+// publishes its partial result, takes a ticket, and the block that draws the
+// last ticket combines the partials in block order.  Results therefore do not
+// depend on block scheduling, and no block ever waits for another.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+
+#include "pa_device.cuh"
+#include "pa_kernels.h"
+
+namespace pa {
+
+namespace {
+
+constexpr int kResThreads = 256;
+
+__device__ __forceinline__ int pop_units(const PopDev* st, int R) {
+  return st->coding == kMSC ? ((R + kMsb - 1) / kMsb) * kMsb : R;
+}
+
+// Neumaier's variant of Kahan compensated summation, FP32.
+struct Comp32 {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    if (fabsf(s) >= fabsf(x))
+      c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, t), x));
+    else
+      c = __fadd_rn(c, __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+  }
+};
+
+// resampling weight of one replica in FP32: exp(-dbeta (E - Emin)) <= 1
+__device__ __forceinline__ float weight32(float dBf, int E, int Emin) {
+  return expf(-dBf * (float)(E - Emin));
+}
+
+// last-block ticket: returns true in every thread of the block that finished last
+__device__ __forceinline__ bool last_block(unsigned int* ticket) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return s_last;
+}
+
+// contiguous chunk of [0, n) owned by this block, a whole number of tiles
+__device__ __forceinline__ void block_chunk(int n, int& lo, int& hi) {
+  const int per = (n + gridDim.x - 1) / gridDim.x;
+  const int c = (per + blockDim.x - 1) / blockDim.x * blockDim.x;
+  lo = min(n, (int)blockIdx.x * c);
+  hi = min(n, lo + c);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------ Q
+// q = sum_j w_j over the population before resampling, then
+//   lnQ = -dbeta E_ref + ln q - ln R_prev            (PAisingSSC.cu:533)
+// FP64 weights: w = exp(-dbeta (E - Emean)), E_ref = Emean (the reference's
+// choice, PAisingSSC.cu:222).  FP32 weights: w = exp(-dbeta (E - Emin)) <= 1,
+// compensated sums, E_ref = Emin; lnQ itself is formed in FP64.
+__global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* st) {
+  __shared__ double s_d[33];
+  __shared__ float s_f[2][kResThreads];
+  if (st->error) return;
+  const int step = st->step, Rp = st->R_prev, n = pop_units(st, Rp);
+  const double dB = st->betas[step] - st->betas[step - 1];
+  const uint8_t* act = st->coding == kMSC ? st->active[st->parity] : nullptr;
+  const int32_t* E = st->E;
+  const int tid = threadIdx.x;
+  if (st->weights == kFP64) {
+    const double Em = st->Emean;
+    double v = 0.0;
+    for (int j = blockIdx.x * blockDim.x + tid; j < n; j += gridDim.x * blockDim.x)
+      if (!act || act[j]) v += exp(-dB * (E[j] - Em));
+    v = block_sum(v, s_d);
+    if (tid == 0) st->qpart_d[blockIdx.x] = v;
+    if (last_block(&st->ticket)) {
+      double a = 0.0;
+      for (int b = tid; b < (int)gridDim.x; b += blockDim.x) a += ((volatile double*)st->qpart_d)[b];
+      a = block_sum(a, s_d);
+      if (tid == 0) {
+        const double lnQ = -(st->betas[step] - st->betas[step - 1]) * Em + log(a) - log((double)Rp);
+        st->q = a;
+        st->lnQ = lnQ;
+        st->ticket = 0;
+      }
+    }
+  } else {
+    const int Emin = st->Emin;
+    const float dBf = (float)dB;
+    Comp32 acc;
+    for (int j = blockIdx.x * blockDim.x + tid; j < n; j += gridDim.x * blockDim.x)
+      if (!act || act[j]) acc.add(weight32(dBf, E[j], Emin));
+    s_f[0][tid] = acc.s;
+    s_f[1][tid] = acc.c;
+    __syncthreads();
+    if (tid == 0) {
+      Comp32 b;
+      float c = 0.f;
+      for (int i = 0; i < (int)blockDim.x; ++i) { b.add(s_f[0][i]); c = __fadd_rn(c, s_f[1][i]); }
+      st->qpart_f[2 * blockIdx.x] = b.s;
+      st->qpart_f[2 * blockIdx.x + 1] = __fadd_rn(b.c, c);
+    }
+    if (last_block(&st->ticket) && tid == 0) {
+      Comp32 t;
+      float c = 0.f;
+      const volatile float* qp = st->qpart_f;
+      for (int b = 0; b < (int)gridDim.x; ++b) { t.add(qp[2 * b]); c = __fadd_rn(c, qp[2 * b + 1]); }
+      const float q = __fadd_rn(t.s, __fadd_rn(t.c, c));
+      st->q = (double)q;
+      st->lnQ = -dB * (double)Emin + log((double)q) - log((double)Rp);
+      st->ticket = 0;
+    }
+  }
+}
+
+// ------------------------------------------------------------ copy numbers
+// Nearest-integer resampling (PAisingSSC.cu:242-247):
+//   mu_j = R_init / R_prev * exp(-dbeta E_j - lnQ),
+//   roff_j = floor(mu_j) + [U_j < mu_j - floor(mu_j)],
+// U_j the reference's draw 0 of subsequence iseq + j (j = linear replica
+// index; for MSC j = 32 * group + bit, PAisingMSC.cu:355).  Block totals are
+// scanned by the last block, which also publishes the new population size
+// and flips the double buffer.
+__global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* st) {
+  __shared__ uint32_t s_u[33];
+  __shared__ uint32_t s_run;
+  if (st->error) return;
+  const int step = st->step, Rp = st->R_prev, n = pop_units(st, Rp), Rinit = st->Rinit;
+  const double dB = st->betas[step] - st->betas[step - 1], lnQ = st->lnQ;
+  const uint8_t* act = st->coding == kMSC ? st->active[st->parity] : nullptr;
+  const int32_t* E = st->E;
+  const unsigned long long seed = st->seed, iseq = st->iseq;
+  const bool fp64 = st->weights == kFP64;
+  const float dBf = (float)dB, qf = (float)st->q, Rf = (float)Rinit;
+  const int Emin = st->Emin;
+  int lo, hi;
+  block_chunk(n, lo, hi);
+  uint32_t tot = 0;
+  for (int base = lo; base < hi; base += blockDim.x) {
+    const int j = base + threadIdx.x;
+    uint32_t r = 0;
+    if (j < hi && (!act || act[j])) {
+      const double U = ref_uniform(ref_word(seed, iseq + (unsigned long long)j, 0));
+      if (fp64) {
+        const double mu = ((double)Rinit) / Rp * exp(-dB * (double)E[j] - lnQ);
+        const double fl = floor(mu);
+        r = (uint32_t)(U < (mu - fl) ? fl + 1 : fl);
+      } else {
+        const float mu = Rf * weight32(dBf, E[j], Emin) / qf;
+        const float fl = floorf(mu);
+        r = (uint32_t)fl + (U < (double)(mu - fl) ? 1u : 0u);
+      }
+    }
+    if (j < hi) st->roff[j] = r;
+    tot += block_sum(r, s_u);
+  }
+  if (threadIdx.x == 0) st->blk_tot[blockIdx.x] = tot;
+  if (last_block(&st->ticket)) {
+    // exclusive scan of the block totals, in block order
+    if (threadIdx.x == 0) s_run = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < (int)gridDim.x; b0 += blockDim.x) {
+      const int b = b0 + threadIdx.x;
+      const uint32_t v = b < (int)gridDim.x ? ((volatile uint32_t*)st->blk_tot)[b] : 0u;
+      uint32_t total;
+      const uint32_t ex = block_exscan(v, s_u, &total);
+      if (b < (int)gridDim.x) st->blk_off[b] = s_run + ex;
+      __syncthreads();
+      if (threadIdx.x == 0) s_run += total;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const unsigned int Rn = s_run;
+      if (Rn == 0u || Rn > (unsigned int)st->Rcap) {
+        st->error = Rn == 0u ? 2 : 1;
+        st->R_cur = 0;
+      } else {
+        st->R_cur = (int)Rn;
+      }
+      st->parity ^= 1;
+      st->ticket = 0;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ scatter
+// offs_j = exclusive prefix of roff; src[offs_j + p] = j for p < roff_j.
+__global__ void __launch_bounds__(kResThreads) scatter_kernel(PopDev* st) {
+  __shared__ uint32_t s_u[33];
+  if (st->error) return;
+  const int n = pop_units(st, st->R_prev);
+  int lo, hi;
+  block_chunk(n, lo, hi);
+  uint32_t run = st->blk_off[blockIdx.x];
+  for (int base = lo; base < hi; base += blockDim.x) {
+    const int j = base + threadIdx.x;
+    const uint32_t r = j < hi ? st->roff[j] : 0u;
+    uint32_t total;
+    const uint32_t off = run + block_exscan(r, s_u, &total);
+    if (j < hi) {
+      st->offs[j] = off;
+      for (uint32_t p = 0; p < r; ++p) st->src[off + p] = (uint32_t)j;
+    }
+    run += total;
+  }
+}
+
+// --------------------------------------------------------- run bookkeeping
+__global__ void begin_run_kernel(PopDev* st) {
+  st->step = 0;
+  st->R_prev = st->R_cur = st->Rinit;
+  st->parity = 0;
+  st->error = 0;
+  st->Emean = 0.0;  // the first resampling uses Emean = 0 (PAisingSSC.cu:483)
+  st->Emin = 0;
+  st->sumlnQ = 0.0;
+  st->lnQ = 0.0;
+  st->q = 0.0;
+  st->sE = st->sE2 = st->sM = st->sM2 = 0;
+  st->sM4lo = st->sM4hi = 0;
+  st->Emin_acc = INT_MAX;
+  st->work_next = 0;
+  st->ticket = 0;
+  double* row = st->rows;  // beta = 0 row: only betaF and R are defined (PAisingSSC.cu:435,453)
+  for (int c = 0; c < kRowCols; ++c) row[c] = 0.0;
+  row[6] = st->bf0 / st->N;
+  row[8] = (double)st->Rinit;
+}
+
+// After a sweep kernel: observables of the step (PAisingSSC.cu:620-630)
+// written to the output row, state advanced to the next temperature.  The
+// arithmetic uses explicitly rounded operations so that no multiply-add is
+// fused and the row is identical to an unfused host evaluation.
+__global__ void finish_step_kernel(PopDev* st) {
+  const int step = st->step;
+  const bool msc = st->coding == kMSC;
+  if (step == 0) {
+    const int rg = (st->R_cur + kMsb - 1) / kMsb;
+    st->iseq += (unsigned long long)(msc ? rg : st->R_cur) * kRefThreads;  // ReplicaInit draws
+    st->Emin = st->Emin_acc;
+  } else if (!st->error) {
+    const int R = st->R_cur, Rp = st->R_prev, N = st->N;
+    const double Rd = (double)R, Nd = (double)N, b = st->betas[step];
+    const double E = __ddiv_rn((double)st->sE, Rd);
+    const double C = __dmul_rn(__dmul_rn(__dsub_rn(__ddiv_rn((double)st->sE2, Rd), __dmul_rn(E, E)), b), b);
+    const double Mv = __ddiv_rn((double)st->sM, Rd);
+    const double M2 = __ddiv_rn((double)st->sM2, Rd);
+    const double M4 = __ddiv_rn(u128_to_double(st->sM4lo, st->sM4hi), Rd);
+    const double lnQ = st->lnQ;
+    const double sum = __dsub_rn(st->sumlnQ, lnQ);
+    const double BF = __dadd_rn(st->bf0, sum);
+    const double S = __dsub_rn(__dmul_rn(b, E), BF);
+    double* row = st->rows + (size_t)step * kRowCols;
+    row[0] = b;
+    row[1] = __ddiv_rn(E, Nd);
+    row[2] = __ddiv_rn(C, Nd);
+    row[3] = __ddiv_rn(Mv, Nd);
+    row[4] = __ddiv_rn(__ddiv_rn(M2, Nd), Nd);
+    row[5] = __ddiv_rn(__ddiv_rn(__ddiv_rn(__ddiv_rn(M4, Nd), Nd), Nd), Nd);
+    row[6] = __ddiv_rn(BF, Nd);
+    row[7] = __ddiv_rn(S, Nd);
+    row[8] = Rd;
+    row[9] = lnQ;
+    st->sumlnQ = sum;
+    st->Emean = E;
+    st->Emin = st->Emin_acc;
+    const int rgp = (Rp + kMsb - 1) / kMsb, rgc = (R + kMsb - 1) / kMsb;
+    st->iseq += msc ? (unsigned long long)rgp * kMsb + (unsigned long long)rgc * kRefThreads
+                    : (unsigned long long)Rp + (unsigned long long)R * kRefThreads;
+    st->R_prev = R;
+  }
+  st->step = step + 1;
+  st->sE = st->sE2 = st->sM = st->sM2 = 0;
+  st->sM4lo = st->sM4hi = 0;
+  st->Emin_acc = INT_MAX;
+  st->work_next = 0;
+}
+
+// ------------------------------------------------------------ launchers
+int res_blocks(const PopDev& h) {
+  const long long units = h.coding == kMSC ? (long long)h.rgcap * kMsb : (long long)h.Rcap;
+  long long b = (units + kResThreads - 1) / kResThreads;
+  if (b > kResBlocksMax) b = kResBlocksMax;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_q(PopDev* st, const PopDev& h, cudaStream_t s) {
+  q_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_numbers(PopDev* st, const PopDev& h, cudaStream_t s) {
+  copy_numbers_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(PopDev* st, const PopDev& h, cudaStream_t s) {
+  scatter_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_begin_run(PopDev* st, cudaStream_t s) {
+  begin_run_kernel<<<1, 1, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish_step(PopDev* st, cudaStream_t s) {
+  finish_step_kernel<<<1, 1, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

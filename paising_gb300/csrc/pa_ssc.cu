@@ -1,0 +1,284 @@
+// pa_ssc.cu -- single-spin coding (one int8 +-1 per site).
+//
+// Replaces, from the reference PAisingSSC.cu:
+//   ReplicaInit   (PAisingSSC.cu:150-157)  -> ssc_init_kernel
+//   checkKerALL   (PAisingSSC.cu:159-193)  -> ssc_sweep_kernel (all sweeps of a
+//   energyKer     (PAisingSSC.cu:195-215)     replica in shared memory, energy
+//                                             and magnetisation fused at the end)
+//   resampleKer   (PAisingSSC.cu:272-280)  -> ssc_resample_kernel (gather into
+//                                             the other half of a double buffer)
+//
+// Layout in HBM: replica r occupies N bytes at spins + r*N, sublattice A
+// (sites with x+y even) first, then B; inside a sublattice, site (x, y) is at
+// idx = y*L/2 + x/2, the reference's checkerboard index (PAisingSSC.cu:169).
+#include <climits>
+
+#include "pa_device.cuh"
+#include "pa_kernels.h"
+
+namespace pa {
+
+namespace {
+
+constexpr uint32_t kLsb = 0x01010101u;
+
+__device__ __forceinline__ uint32_t minus_bits(uint32_t w) { return (w >> 1) & kLsb; }  // 1 per byte == -1
+
+// per-replica statistics kept by thread 0 of a sweep CTA
+struct StatAcc {
+  long long sE = 0, sE2 = 0, sM = 0, sM2 = 0;
+  U128 m4{0, 0};
+  int emin = INT_MAX;
+  __device__ void add(int e, int m) {
+    const long long am = m < 0 ? -(long long)m : (long long)m;
+    sE += e;
+    sE2 += (long long)e * e;
+    sM += am;
+    sM2 += am * am;
+    unsigned long long lo, hi;
+    m4_of(m, lo, hi);
+    u128_add(m4, lo, hi);
+    emin = e < emin ? e : emin;
+  }
+  __device__ void flush(PopDev* st) const {
+    if (sE2 == 0 && emin == INT_MAX) return;
+    atomicAdd((unsigned long long*)&st->sE, (unsigned long long)sE);
+    atomicAdd((unsigned long long*)&st->sE2, (unsigned long long)sE2);
+    atomicAdd((unsigned long long*)&st->sM, (unsigned long long)sM);
+    atomicAdd((unsigned long long*)&st->sM2, (unsigned long long)sM2);
+    u128_atomic_add(&st->sM4lo, &st->sM4hi, m4.lo, m4.hi);
+    atomicMin(&st->Emin_acc, emin);
+  }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ init
+// ReplicaInit (PAisingSSC.cu:150-157): reference thread t of block B draws,
+// for its k-th site idx = t + 128k, uniform number 2k for gA[idx] and 2k+1
+// for gB[idx] from subsequence iseq + t + 128 B; spin = +1 iff U >= 0.5.
+__global__ void ssc_init_kernel(PopDev* st) {
+  const int N = st->N, h = N >> 1, R = st->R_cur;
+  const unsigned long long seed = st->seed, iseq = st->iseq;
+  int8_t* sp = (int8_t*)st->spins[st->parity];
+  const long long total = (long long)R * h;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / h), idx = (int)(e - (long long)r * h);
+    const int t = idx & (kRefThreads - 1), k = idx >> 7;
+    const unsigned long long sub = iseq + (unsigned long long)t + (unsigned long long)kRefThreads * r;
+    sp[(size_t)r * N + idx] = ref_uniform(ref_word(seed, sub, 2ull * k)) >= 0.5 ? 1 : -1;
+    sp[(size_t)r * N + h + idx] = ref_uniform(ref_word(seed, sub, 2ull * k + 1)) >= 0.5 ? 1 : -1;
+  }
+}
+
+// ----------------------------------------------------------------- sweep
+// One CTA anneals one replica at a time (dynamic work counter), the whole
+// lattice resident in shared memory as 32-bit words of 4 int8 spins.  Thread
+// (rsub, cw) owns word column cw of sublattice rows rsub, rsub+rpp, ...
+//
+// MODE kRefCoords reproduces checkKerALL's decisions exactly: site idx of
+// replica r, sweep sw, half-sweep hf uses draw
+//     ctr = sw*2K + hf*K + k   of subsequence  iseq + t + 128 r,
+// t = idx mod 128, k = idx div 128, K = draws per reference thread per half
+// sweep, and flips iff (H+1)/2^32 < boltz[idxT0 + 2 idxT1], evaluated as the
+// integer test H < thr10[...] with thr10 = ceil(2^32 p) - 1 (exact).
+// MODE kNative draws one Philox4x32-10 block per 4-site word and flips
+// iff dE <= 0 or H < ceil(2^32 exp(-beta dE)).
+template <int MODE>
+__global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g, int sweeps) {
+  extern __shared__ __align__(16) uint32_t lat[];  // N/4 words: A then B
+  __shared__ uint32_t s_thr[16];
+  __shared__ int s_unit;
+  __shared__ int s_red[2][33];
+
+  const int tid = threadIdx.x;
+  const int L = g.L, N = g.N, h = g.half, Wr = g.Wr, hw = h >> 2;  // hw: words per sublattice
+  const int R = st->R_cur, step = st->step;
+  const unsigned long long seed = st->seed;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const uint32_t tag = kTagSscSweep | (uint32_t)st->pop_id;
+  // draws consumed by the resampling of this step come before the sweep's
+  const unsigned long long iseq = st->iseq + (step > 0 ? (unsigned long long)st->R_prev : 0ull);
+  int8_t* spins = (int8_t*)st->spins[st->parity];
+  if (tid < kThrPerStep) s_thr[tid] = st->thr[(size_t)step * kThrPerStep + tid];
+
+  const bool worker = tid < g.T;
+  const int cw = worker ? tid % Wr : 0, rsub = worker ? tid / Wr : 0;
+  const int cwl = (cw == 0 ? Wr - 1 : cw - 1), cwr = (cw + 1 == Wr ? 0 : cw + 1);
+  StatAcc acc;
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_unit = (int)atomicAdd(&st->work_next, 1u);
+    __syncthreads();
+    const int r = s_unit;
+    if (r >= R) break;
+    const uint4* gsrc = (const uint4*)(spins + (size_t)r * N);
+    uint4* lat4 = (uint4*)lat;
+    for (int v = tid; v < (N >> 4); v += blockDim.x) lat4[v] = gsrc[v];
+    __syncthreads();
+
+    for (int sw = 0; sw < sweeps; ++sw) {
+#pragma unroll 1
+      for (int hf = 0; hf < 2; ++hf) {
+        uint32_t* self = lat + (hf ? hw : 0);
+        const uint32_t* oth = lat + (hf ? 0 : hw);
+        if (worker) {
+          for (int ty = rsub; ty < L; ty += g.rpp) {
+            const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
+            const int w = row + cw;
+            const uint32_t s = self[w];
+            const uint32_t o = oth[w];
+            // the horizontal neighbour that is not at the same idx: x-1 for A
+            // on even rows and B on odd rows, x+1 otherwise (PAisingSSC.cu:170,182)
+            const bool left = (hf == 0) == ((ty & 1) == 0);
+            const uint32_t oside = left ? __byte_perm(oth[row + cwl], o, 0x6543) : __byte_perm(o, oth[row + cwr], 0x4321);
+            const uint32_t ou = oth[rowu + cw], od = oth[rowd + cw];
+            uint32_t flip = 0;
+            if (MODE == kRefCoords) {
+              const uint32_t nminus = minus_bits(o) + minus_bits(oside) + minus_bits(ou) + minus_bits(od);
+              // idxT0 + 2 idxT1 = (1 - s_minus) + 2 (4 - n_minus) per byte
+              const uint32_t tix = 0x09090909u - minus_bits(s) - (nminus << 1);
+              const int idx0 = ty * (h / L) + cw * 4;
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const int idx = idx0 + j, t = idx & (kRefThreads - 1), k = idx >> 7;
+                const int K = g.kconst ? g.kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
+                const unsigned long long sub = iseq + (unsigned long long)t + (unsigned long long)kRefThreads * r;
+                const unsigned long long ctr = (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k;
+                const uint32_t u = ref_word(seed, sub, ctr);
+                if (u < s_thr[(tix >> (8 * j)) & 0xFFu]) flip |= 0xFEu << (8 * j);
+              }
+            } else {
+              const uint32_t na = ((s ^ o) >> 1 & kLsb) + ((s ^ oside) >> 1 & kLsb) + ((s ^ ou) >> 1 & kLsb) +
+                                  ((s ^ od) >> 1 & kLsb);
+              const U4 rn = philox10((uint32_t)(r * hw + w), (uint32_t)(sw * 2 + hf), (uint32_t)step, tag, k0, k1);
+              const uint32_t T4 = s_thr[10], T8 = s_thr[11];
+              const uint32_t uu[4] = {rn.x, rn.y, rn.z, rn.w};
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const uint32_t a = (na >> (8 * j)) & 0xFFu;
+                const bool acc_ = a >= 2u || uu[j] < (a ? T4 : T8);
+                if (acc_) flip |= 0xFEu << (8 * j);
+              }
+            }
+            self[w] = s ^ flip;
+          }
+        }
+        __syncthreads();
+      }
+    }
+
+    // energy: every bond joins one A and one B site, so E = -sum_A s_A sum_nn s_B
+    // = -2N + 2 * (number of anti-parallel bonds seen from A); M = N - 2 #minus.
+    int anti = 0, nminus = 0;
+    if (worker) {
+      for (int ty = rsub; ty < L; ty += g.rpp) {
+        const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
+        const int w = row + cw;
+        const uint32_t s = lat[w], o = lat[hw + w];
+        const bool left = (ty & 1) == 0;
+        const uint32_t oside = left ? __byte_perm(lat[hw + row + cwl], o, 0x6543) : __byte_perm(o, lat[hw + row + cwr], 0x4321);
+        const uint32_t na = ((s ^ o) >> 1 & kLsb) + ((s ^ oside) >> 1 & kLsb) + ((s ^ lat[hw + rowu + cw]) >> 1 & kLsb) +
+                            ((s ^ lat[hw + rowd + cw]) >> 1 & kLsb);
+        anti += (int)((na * kLsb) >> 24);
+        nminus += __popc(minus_bits(s)) + __popc(minus_bits(o));
+      }
+    }
+    anti = warp_sum(anti);
+    nminus = warp_sum(nminus);
+    if ((tid & 31) == 0) { s_red[0][tid >> 5] = anti; s_red[1][tid >> 5] = nminus; }
+    // write the lattice back while the reduction completes
+    uint4* gdst = (uint4*)(spins + (size_t)r * N);
+    __syncthreads();
+    for (int v = tid; v < (N >> 4); v += blockDim.x) gdst[v] = lat4[v];
+    if (tid == 0) {
+      int a = 0, m = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { a += s_red[0][i]; m += s_red[1][i]; }
+      const int E = -2 * N + 2 * a, Mg = N - 2 * m;
+      st->E[r] = E;
+      st->M[r] = Mg;
+      acc.add(E, Mg);
+    }
+  }
+  if (tid == 0) acc.flush(st);
+}
+
+// -------------------------------------------------------------- resample
+// Gather form of resampleKer: new replica s copies old replica src[s].
+__global__ void ssc_resample_kernel(PopDev* st) {
+  if (st->error) return;
+  const int N = st->N, Rn = st->R_cur;
+  const uint4* old = (const uint4*)st->spins[st->parity ^ 1];
+  uint4* neu = (uint4*)st->spins[st->parity];
+  const int nv = N >> 4;
+  for (int s = blockIdx.x; s < Rn; s += gridDim.x) {
+    const uint4* a = old + (size_t)st->src[s] * nv;
+    uint4* b = neu + (size_t)s * nv;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) b[v] = a[v];
+  }
+}
+
+// -------------------------------------------------------------- launchers
+static int pick_rpp(int L, int Wr, int max_threads) {
+  int best = 1;
+  for (int r = 1; r <= L; ++r)
+    if (L % r == 0 && Wr * r <= max_threads) best = r;
+  return best;
+}
+
+bool ssc_geom(int L, int max_threads, SweepGeom* g) {
+  if (L < 8 || L % 8 != 0 || L > 256) return false;
+  g->L = L;
+  g->N = L * L;
+  g->half = g->N / 2;
+  g->Wr = L / 8;
+  g->rpp = pick_rpp(L, g->Wr, max_threads);
+  g->T = g->Wr * g->rpp;
+  g->block = (g->T + 31) / 32 * 32;
+  g->npass = (L + g->rpp - 1) / g->rpp;
+  g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
+  g->smem = g->N;
+  g->grid = 0;
+  return true;
+}
+
+cudaError_t ssc_sweep_setup(SweepGeom* g, int rng_mode) {
+  const void* fn = rng_mode == kRefCoords ? (const void*)ssc_sweep_kernel<kRefCoords> : (const void*)ssc_sweep_kernel<kNative>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g->smem);
+  if (e != cudaSuccess) return e;
+  int dev, nsm, per;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, g->block, g->smem);
+  if (e != cudaSuccess) return e;
+  g->grid = nsm * (per > 0 ? per : 1);
+  return cudaSuccess;
+}
+
+cudaError_t launch_ssc_init(PopDev* st, const PopDev& h, cudaStream_t s) {
+  long long total = (long long)h.Rinit * (h.N / 2);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  ssc_init_kernel<<<blocks, 256, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssc_sweep(PopDev* st, const SweepGeom& g, int rng_mode, int sweeps, cudaStream_t s) {
+  if (rng_mode == kRefCoords)
+    ssc_sweep_kernel<kRefCoords><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+  else
+    ssc_sweep_kernel<kNative><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssc_resample(PopDev* st, const PopDev& h, cudaStream_t s) {
+  int dev, nsm;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  ssc_resample_kernel<<<nsm * 8, 128, 0, s>>>(st);
+  return cudaGetLastError();
+}
+
+}  // namespace pa

@@ -1,0 +1,64 @@
+// pa_state.h -- per-population device state of the annealing engine.
+//
+// One PopDev lives in device memory per population.  Every kernel of a
+// temperature step reads its sizes, buffer pointers and scalars from it, so a
+// whole schedule can be captured once as a CUDA graph: nothing the host knows
+// only after a step (the new population size, the parity of the double
+// buffer, lnQ, ...) is baked into launch arguments.
+#pragma once
+
+#include <cstdint>
+
+namespace pa {
+
+enum Coding : int { kSSC = 0, kMSC = 1 };
+enum RngMode : int { kNative = 0, kRefCoords = 1 };
+enum Weights : int { kFP32Kahan = 0, kFP64 = 1 };
+
+constexpr int kMsb = 32;          // replicas per MSC word (MSbits, PAisingMSC.cu:34)
+constexpr int kRefThreads = 128;  // EQthreads (PAisingSSC.cu:62): fixes the reference's draw layout
+constexpr int kThrPerStep = 12;   // [0..9] SSC table thresholds, [10] T4, [11] T8
+constexpr int kRowCols = 10;
+constexpr int kResBlocksMax = 1024;
+
+struct PopDev {
+  // ------------------------------------------------ configuration (constant)
+  int L, N, coding, Rinit, Rcap, rgcap, sweeps, rng_mode, weights, pop_id, nsteps, pad0;
+  unsigned long long seed;
+  // ------------------------------------------------ buffers
+  void* spins[2];      // SSC: int8 [Rcap][N] (+-1, sublattice A then B); MSC: uint32 [rgcap][N]
+  int32_t* E;          // SSC [Rcap], MSC [rgcap*32]: energy of the current population
+  int32_t* M;          // magnetisation, same indexing
+  uint8_t* active[2];  // MSC: [rgcap*32] replica present (isActive, PAisingMSC.cu:91)
+  uint32_t* roff;      // copy numbers of the previous population
+  uint32_t* offs;      // exclusive scan of roff
+  uint32_t* src;       // new linear replica index -> old linear replica index
+  uint32_t* blk_tot;   // [kResBlocksMax] per-block sums of roff
+  uint32_t* blk_off;   // [kResBlocksMax] exclusive scan of blk_tot
+  double* qpart_d;     // [kResBlocksMax] FP64 partial sums of the weights
+  float* qpart_f;      // [2*kResBlocksMax] FP32 (sum, compensation) partials
+  double* rows;        // [(nsteps+1) * 10] output rows (columns of PA_results_run_<r>.dat)
+  const double* betas; // [nsteps+1]
+  const uint32_t* thr; // [(nsteps+1) * kThrPerStep]
+  // ------------------------------------------------ dynamic scalars
+  int step;            // temperature index being computed (1..nsteps)
+  int R_prev;          // population size before resampling
+  int R_cur;           // population size after resampling
+  int parity;          // spins[parity] holds the current population
+  int error;           // 0 ok, 1 capacity exceeded
+  int Emin;            // minimum energy of the current population
+  unsigned int work_next;  // dynamic work counter of the sweep kernel
+  unsigned int ticket;     // last-block tickets of the resampling kernels
+  unsigned long long iseq; // reference subsequence counter (initial_sequence, PAisingSSC.cu:418)
+  double Emean;        // <E> of the current population (Emean, PAisingSSC.cu:483,620)
+  double sumlnQ;       // -sum of lnQ over the steps so far (PAisingSSC.cu:627)
+  double lnQ;          // lnQ of the step being computed
+  double q;            // sum of the resampling weights of the step being computed
+  double bf0;          // -N ln 2, betaF at beta = 0 (PAisingSSC.cu:435), computed on the host
+  // ------------------------------------------------ statistics accumulators
+  long long sE, sE2, sM, sM2;
+  unsigned long long sM4lo, sM4hi;
+  int Emin_acc, pad1;
+};
+
+}  // namespace pa

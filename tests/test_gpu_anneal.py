@@ -1,0 +1,90 @@
+"""Whole-anneal parity: the engine (through pa_create / pa_run) against the
+reference programs' own outputs under the injected stream.  With the
+reference-coordinate stream and FP64 weights every population size R_i must
+match exactly and every other column to print precision, for all 200
+temperatures.  Plus size-independent invariants and physics checks of the
+native (production) configuration."""
+import numpy as np
+import pytest
+
+import paising_gb300 as pa
+from conftest import compare_rows, load_dat
+
+pytestmark = pytest.mark.gpu
+
+
+def run(**kw):
+    with pa.Engine(**kw) as e:
+        e.run()
+        rows = [e.rows(r) for r in range(e.config.runs)]
+        return rows, e.timing()
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_reference_C1(cuda, coding, graph):
+    rows, _ = run(L=16, R=1000, sweeps=10, seed=100, coding=coding, rng="reference", weights="fp64", graph=graph)
+    compare_rows(rows[0], load_dat(f"ref/inj_{coding.upper()}_L16_R1000_t10_d0.005_s100.dat"), rtol=2e-10)
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_reference_two_runs(cuda, coding):
+    rows, _ = run(L=16, R=1000, sweeps=10, seed=7, runs=2, coding=coding, rng="reference", weights="fp64")
+    for r in range(2):
+        compare_rows(rows[r], load_dat(f"ref/inj_{coding.upper()}_L16_R1000_t10_d0.005_s7_M2_run{r}.dat"), rtol=2e-10)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("coding", ["msc", "ssc"])
+def test_reference_C2_L64(cuda, coding):
+    """The reference's sample shape: L=64, R=20000, 100 sweeps, seed 100."""
+    rows, _ = run(L=64, R=20000, sweeps=100, seed=100, coding=coding, rng="reference", weights="fp64")
+    compare_rows(rows[0], load_dat(f"ref/inj_{coding.upper()}_L64_R20000_t100_d0.005_s100.dat"), rtol=2e-10)
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_fp32_weights_track_fp64(cuda, coding):
+    """Same stream, FP32 compensated weights: lnQ per step within 1e-6 of the
+    FP64 run while the populations coincide, betaF/N within 1e-6 at the end."""
+    a, _ = run(L=16, R=1000, sweeps=10, seed=100, coding=coding, rng="reference", weights="fp64")
+    b, _ = run(L=16, R=1000, sweeps=10, seed=100, coding=coding, rng="reference", weights="fp32")
+    a, b = a[0], b[0]
+    same = np.cumprod(a[:, 8] == b[:, 8]).astype(bool)
+    k = int(same.sum())
+    assert k >= 5
+    assert np.max(np.abs(a[1:k, 9] - b[1:k, 9])) < 1e-6
+
+
+def test_invariants_native(cuda):
+    """Population size stays within the buffer, energies per site within
+    [-2, 2], |M| <= 1, and E/N is monotone-ish decreasing in beta."""
+    rows, (ms, att) = run(L=32, R=5000, sweeps=20, seed=3, coding="msc")
+    r = rows[0]
+    assert np.all(r[:, 8] > 0) and np.all(r[:, 8] <= 1.25 * 5000 + 256)
+    assert np.all(np.abs(r[1:, 1]) <= 2) and np.all((r[1:, 3] >= 0) & (r[1:, 3] <= 1))
+    assert r[-1, 1] < -1.9 and ms > 0 and att == pytest.approx(20 * 1024 * r[1:, 8].sum())
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_native_free_energy_vs_kaufman_L16(cuda, oracle, coding):
+    """Native stream, FP32 weights, L=16, R=20000, 20 sweeps: betaF/N against
+    the exact finite-lattice value within 3e-4 at every beta (the finite-R
+    bias of population annealing at this size is ~1e-4)."""
+    rows, _ = run(L=16, R=20000, sweeps=20, seed=12, coding=coding)
+    r = rows[0]
+    exact = np.array([-oracle.kaufman(16, b)[0] / 256 for b in r[:, 0]])
+    assert np.max(np.abs(r[:, 6] - exact)) < 3e-4
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("coding", ["msc", "ssc"])
+def test_native_free_energy_vs_kaufman_C2(cuda, oracle, coding):
+    """The spec bar at L=64, R=20000, 100 sweeps, dbeta=0.005:
+    |betaF/N - exact| <= 1e-4 at every beta, native stream, FP32 weights."""
+    rows, _ = run(L=64, R=20000, sweeps=100, seed=2026, coding=coding)
+    r = rows[0]
+    exact = np.array([-oracle.kaufman(64, b)[0] / 4096 for b in r[:, 0]])
+    err = np.abs(r[:, 6] - exact)
+    assert err.max() <= 1e-4, (err.max(), r[np.argmax(err), 0])
+    eE = np.array([oracle.kaufman(64, b)[1] / 4096 for b in r[1:, 0]])
+    assert np.max(np.abs(r[1:, 1] - eE)) < 5e-3
