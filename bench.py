@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Headline benchmark: spin-flip attempts per ns of a full population-annealing
+run of the 2D Ising ferromagnet at L=64, R=20000, 100 sweeps per temperature,
+dbeta=0.005, beta 0 -> 1 (199 temperatures), the reference's sample shape.
+
+One "step" is one full anneal of the batch (P independent populations run
+concurrently by one engine; P=1 is the plain single-population form).  The
+metric is the reference's own (PAisingSSC.cu:632,806):
+    attempts = sweeps * N * sum_{i>=1} R_i,   value = attempts / device ns.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference runs the reference's own CUDA program (PAisingMSC.cu built
+with cuRAND by oracle/ref_build.py) on the same GPU and reports its own
+timing.  Under torchrun with N > 1 each rank anneals its own populations
+(replicas only; the path has no data-parallel exchange) and rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PROFILES = os.path.join(ROOT, "profiles")
+METRIC = "spin-flip attempts/ns (full anneal, L=64 R=20000 100 sweeps dbeta=0.005)"
+UNIT = "attempts/ns"
+
+
+# ----------------------------------------------------------------- helpers
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--coding", choices=["msc", "ssc"], default="msc")
+    ap.add_argument("--populations", type=int, default=1, help="independent populations per engine launch")
+    ap.add_argument("--L", type=int, default=64)
+    ap.add_argument("--R", type=int, default=20000)
+    ap.add_argument("--sweeps", type=int, default=100)
+    ap.add_argument("--dbeta", type=float, default=0.005)
+    ap.add_argument("--beta-final", type=float, default=1.0)
+    ap.add_argument("--graph", type=int, default=1)
+    ap.add_argument("--cpu-sample-steps", type=int, default=4, help="temperatures in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    return ap.parse_args(argv)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.proc, self.lines = gpu, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_profile_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    p = os.path.join(PROFILES, "ncu_summary.json")
+    try:
+        d = json.load(open(p))
+        return d[kernel][workload]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws == 1:
+        return 0, 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, lrank = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(lrank)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, lrank, ws, dist
+
+
+# ------------------------------------------------------------- our engine
+def cpu_baseline(a) -> dict:
+    """The oracle (C restatement of the reference's MSC/SSC loop, OpenMP over
+    replicas) on this host's cores, over the first few temperatures of the
+    same workload."""
+    from oracle import pa_oracle
+    threads = os.cpu_count() or 1
+    pa_oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    _, att = pa_oracle.anneal(a.coding, a.L, a.R, a.sweeps, a.dbeta, a.beta_final, 1, 7,
+                              max_steps=a.cpu_sample_steps)
+    dt = time.perf_counter() - t0
+    return {"value": att / (dt * 1e9), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{a.coding.upper()} L={a.L} R={a.R} {a.sweeps} sweeps, initialisation + first "
+                      f"{a.cpu_sample_steps} temperatures ({att:.3g} attempts in {dt:.1f} s)"}
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+
+    import paising_gb300 as pa
+
+    rank, lrank, ws, dist = dist_init()
+    dev = lrank
+    torch.cuda.set_device(dev)
+    P = a.populations
+    eng = pa.Engine(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=P,
+                    seed=1000 + 97 * rank, coding=a.coding, rng="native", weights="fp32", graph=bool(a.graph),
+                    device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")  # > L2 (129 MB)
+    for _ in range(a.warmup):
+        eng.run()
+    nsteps = eng.num_rows() - 1
+    launches_per_run = 4 + 6 * nsteps
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    ms_steps, att_steps = [], []
+    with ClockSampler(dev) as clk:
+        barrier()
+        for _ in range(a.steps):
+            flush.zero_()  # evict L2 between timed steps (outside the timed region)
+            torch.cuda.synchronize(dev)
+            eng.run()
+            ms, att = eng.timing()
+            ms_steps.append(ms)
+            att_steps.append(att)
+        barrier()
+    tot_ms, tot_att = sum(ms_steps), sum(att_steps)
+    if dist:
+        t = torch.tensor([tot_ms, tot_att], dtype=torch.float64, device=f"cuda:{dev}")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        tot_ms_max, tot_att_all = mx[0].item(), t[1].item()
+    else:
+        tot_ms_max, tot_att_all = tot_ms, tot_att
+    value = tot_att_all / (tot_ms_max * 1e6)
+
+    # end to end through the C ABI with host buffers: every step uploads the
+    # initial populations from pinned host memory (pa_set_population), runs,
+    # and reads the result rows back (pa_get_rows); host wall clock.
+    N = a.L * a.L
+    pop_bytes = ((a.R + 31) // 32) * N * 4 if a.coding == "msc" else a.R * N
+    host_pop = torch.empty(pop_bytes, dtype=torch.uint8, pin_memory=True)
+    rng = np.random.default_rng(rank)
+    host_np = host_pop.numpy()
+    if a.coding == "msc":
+        host_np[:] = rng.integers(0, 256, pop_bytes, dtype=np.uint8)
+    else:
+        host_np[:] = np.where(rng.integers(0, 2, pop_bytes) > 0, 1, -1).astype(np.int8).view(np.uint8)
+    e2e_s, e2e_att = [], 0.0
+    rows_bytes = 0
+    for i in range(a.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        eng.set_population(host_pop.data_ptr())
+        eng.run()
+        rows = [eng.rows(r) for r in range(P)]
+        e2e_s.append(time.perf_counter() - t0)
+        e2e_att += eng.timing()[1]
+        rows_bytes = sum(r.nbytes for r in rows)
+    eng.set_population(None)
+    e2e_tot = sum(e2e_s)
+    if dist:
+        t = torch.tensor([e2e_tot, e2e_att], dtype=torch.float64, device=f"cuda:{dev}")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e_tot, e2e_att = mx[0].item(), t[1].item()
+    e2e_value = e2e_att / (e2e_tot * 1e9)
+
+    out = None
+    if rank == 0:
+        workload = f"PA anneal {a.coding.upper()} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} beta 0->" \
+                   f"{a.beta_final} ({nsteps} temperatures), {P} population(s) per launch"
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": tot_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32 bit-planes (int32 energies, fp32-compensated weights, fp64 lnQ)" if a.coding == "msc"
+            else "i8 spins (int32 energies, fp32-compensated weights, fp64 lnQ)",
+            "data": "synthetic (random initial spins from the seed, native Philox stream)",
+            "config": {"workload": workload, "L": a.L, "R": a.R, "sweeps": a.sweeps, "dbeta": a.dbeta,
+                       "beta_final": a.beta_final, "coding": a.coding, "populations_per_launch": P,
+                       "graph": bool(a.graph), "parallelism": f"replicas x{ws}",
+                       "l2": "flushed between timed steps (256 MB write)"},
+            "full_anneal_s": tot_ms_max / a.steps / 1e3,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": pop_bytes,
+                    "d2h_bytes_per_step": rows_bytes + 4 * P},
+            "gpu_launches": launches_per_run * P * a.steps,
+            "clocks": clk.summary(),
+        }
+        if not a.no_profile:
+            out.update(profile_leg(a, eng, pa))
+        if not a.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(a)
+    eng.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def profile_leg(a, eng, pa) -> dict:
+    """Per-kernel device times of one run (CUDA events around each launch on
+    the engine's stream) and the roofline of the dominant kernel."""
+    prof = eng.profile()
+    tot = sum(v[1] for v in prof.values())
+    rows = eng.rows(0)
+    Rs = rows[1:, 8]
+    N = a.L * a.L
+    sweep = f"{a.coding}_sweep"
+    n_launch, sweep_ms = prof[sweep]
+    avg_ms = sweep_ms / n_launch
+    attempts_per_launch = a.sweeps * N * Rs.mean()
+    ops_per_attempt = 5.0 if a.coding == "msc" else 33.0  # algorithmic INT32 ops (SURVEY 8d figures)
+    achieved = attempts_per_launch * ops_per_attempt / (avg_ms * 1e-3) / 1e12
+    peaks = pa.probe_int_issue(eng.config.device)
+    peak = max(peaks) / 1e12
+    workload = f"L{a.L}_R{a.R}_sw{a.sweeps}"
+    return {
+        "kernels": {k: {"launches": v[0], "total_ms": v[1], "share": v[1] / tot} for k, v in prof.items()},
+        "roofline": {"kernel": sweep, "bound": "int32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                     "frac": achieved / peak, "traffic": load_profile_traffic(sweep, workload),
+                     "ops_per_attempt": ops_per_attempt, "attempts_per_launch": attempts_per_launch,
+                     "avg_launch_ms": avg_ms,
+                     "peak_source": "measured in-process: integer lane-op issue rate, LOP3/IMAD chains "
+                                    f"(ALU-only {peaks[0] / 1e12:.1f}, FMA-only {peaks[1] / 1e12:.1f}, "
+                                    f"both {peaks[2] / 1e12:.1f} Tops/s)"},
+    }
+
+
+# -------------------------------------------------------- reference program
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    from oracle import ref_build
+    prog = "MSC" if a.coding == "msc" else "SSC"
+    binp = os.path.join(ROOT, "oracle", "_ref", "bin", f"PAising{prog}_L{a.L}_curand")
+    if not os.path.exists(binp):
+        try:
+            ref_build.main(["--sizes", str(a.L)])
+        except Exception as ex:  # noqa: BLE001
+            return {"impl": "reference", "unavailable": f"reference build failed: {str(ex)[:200]}"}
+    if not os.path.exists(binp):
+        return {"impl": "reference", "unavailable": f"reference sources for L={a.L} not present"}
+
+    def once(seed):
+        with tempfile.TemporaryDirectory() as d:
+            r = subprocess.run([binp, "-R", str(a.R), "-t", str(a.sweeps), "-d", str(a.dbeta), "-f",
+                                str(a.beta_final), "-s", str(seed), "-o", d], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout[-500:] + r.stderr[-500:])
+        el = float(re.search(r"Elapsed time:\s*([0-9.eE+-]+)", r.stdout).group(1))
+        tpf = float(re.search(r"Time per spin-flip:\s*([0-9.eE+-]+)", r.stdout).group(1))
+        return el, tpf
+
+    for w in range(a.warmup):
+        once(1 + w)
+    els, tpfs = [], []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for k in range(a.steps):
+            el, tpf = once(100 + k)
+            els.append(el)
+            tpfs.append(tpf)
+    # attempts/ns over all steps = total attempts / total ns
+    att = sum(el * 1e9 / tpf for el, tpf in zip(els, tpfs))
+    value = att / (sum(els) * 1e9)
+    sample = f"PAising{prog}.cu (L={a.L}, MSbits=32) built with cuRAND, full anneal per step, " \
+             "timed by the program's own CUDA events (Elapsed time / Time per spin-flip)"
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * sum(els) / len(els), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 bit-planes" if a.coding == "msc" else "i8 spins",
+        "data": "synthetic (random initial spins from the seed, cuRAND Philox)",
+        "config": {"workload": f"reference PAising{prog} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} "
+                               f"beta 0->{a.beta_final}, 1 population", "L": a.L, "R": a.R, "sweeps": a.sweeps,
+                   "dbeta": a.dbeta, "coding": a.coding, "parallelism": "single GPU"},
+        "full_anneal_s": sum(els) / len(els),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
+                         "sample": sample + " (GPU program; one host thread drives it)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "clocks": clk.summary(),
+    }
+
+
+def main(argv=None) -> int:
+    a = parse_args(argv)
+    out = run_reference(a) if a.impl == "reference" else run_ours(a)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

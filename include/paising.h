@@ -105,6 +105,36 @@ PA_API int pa_get_rows(const pa_handle* h, int run, pa_row* rows, int max_rows, 
  * sweeps * N * sum_{i>=1} R_i over all runs (PAisingSSC.cu:632,806). */
 PA_API int pa_get_timing(const pa_handle* h, double* ms, double* attempts);
 
+/* Initial population for the following pa_run calls instead of the random
+ * initialisation (ReplicaInit, PAisingSSC.cu:150-157) -- e.g. to resume from
+ * a saved population.  host points to cfg.R replicas in the stage layout of
+ * the handle's coding (SSC: int8 [R][N]; MSC: uint32 [ceil(R/32)][N], bit k of
+ * group g = replica 32g+k).  The copy is enqueued on the handle's stream and
+ * is complete when the next pa_run returns.  host = NULL restores the random
+ * initialisation. */
+PA_API int pa_set_population(pa_handle* h, const void* host);
+
+/* Final population of the last run of the last pa_run, in the same layout
+ * (MSC groups as stored: replica s of the population is at group s % rg,
+ * bit s / rg after resampling, PAisingMSC.cu:413-414).  *R receives the
+ * population size; bytes is the capacity of host. */
+PA_API int pa_get_population(const pa_handle* h, void* host, size_t bytes, int* R);
+
+/* Per-kernel device time of one run executed launch by launch with CUDA
+ * events on the handle's stream around every kernel (serialised; for
+ * profiling and rooflines, not for throughput).  Fills up to max entries. */
+typedef struct pa_kernel_time {
+  char name[24];
+  int launches;
+  double total_ms;
+} pa_kernel_time;
+PA_API int pa_profile_run(pa_handle* h, pa_kernel_time* out, int max, int* n);
+
+/* Measured 32-bit integer lane-operation throughput of `device`:
+ * [0] LOP3 only (ALU pipe), [1] IMAD only (FMA pipe), [2] both interleaved.
+ * The sweeps are integer-pipe bound; this is their roofline denominator. */
+PA_API int pa_probe_int_issue(int device, double* lane_ops_per_s);
+
 /* Writes dir/PA_results_run_<r>.dat for every run with `precision`
  * significant digits (PAisingSSC.cu:670-692). */
 PA_API int pa_write_results(const pa_handle* h, const char* dir, int precision);

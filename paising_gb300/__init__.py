@@ -56,6 +56,10 @@ class Row(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("beta", "e", "c", "m", "m2", "m4", "bf", "s", "r", "lnq")]
 
 
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 24), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
+
+
 _vp, _i, _u64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double
 _SIGS = {
     "pa_abi_version": ([], _i),
@@ -71,6 +75,10 @@ _SIGS = {
     "pa_last_error": ([_vp], ctypes.c_char_p),
     "pa_schedule": ([_d, _d, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_ref_word": ([_u64, _u64, _u64], ctypes.c_uint32),
+    "pa_set_population": ([_vp, _vp], _i),
+    "pa_get_population": ([_vp, _vp, ctypes.c_size_t, ctypes.POINTER(_i)], _i),
+    "pa_profile_run": ([_vp, _vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_probe_int_issue": ([_i, _vp], _i),
     "pa_ssc_init": ([_vp, _i, _i, _u64, _u64, _vp], _i),
     "pa_ssc_sweep": ([_vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
     "pa_msc_init": ([_vp, _vp, _i, _i, _u64, _u64, _vp], _i),
@@ -155,6 +163,32 @@ class Engine:
         _check(lib().pa_get_timing(self._h, ctypes.byref(ms), ctypes.byref(att)), self._h)
         return ms.value, att.value
 
+    def set_population(self, host_ptr) -> None:
+        """Initial population from host memory (pointer or numpy array in the
+        coding's layout); None restores the random initialisation."""
+        p = host_ptr.ctypes.data if isinstance(host_ptr, np.ndarray) else host_ptr
+        _check(lib().pa_set_population(self._h, p), self._h)
+
+    def population(self) -> np.ndarray:
+        """Final population of the last run (SSC int8 [R, N]; MSC uint32 [rg, N])."""
+        c = self.config
+        N = c.L * c.L
+        cap = int(c.R * c.capacity) + 512
+        rg = (cap + 31) // 32
+        buf = np.zeros(rg * N if c.coding == MSC else cap * N, dtype=np.uint32 if c.coding == MSC else np.int8)
+        R = ctypes.c_int()
+        _check(lib().pa_get_population(self._h, buf.ctypes.data, buf.nbytes, ctypes.byref(R)), self._h)
+        if c.coding == MSC:
+            return buf[: ((R.value + 31) // 32) * N].reshape(-1, N)
+        return buf[: R.value * N].reshape(R.value, N)
+
+    def profile(self) -> dict:
+        """{kernel: (launches, total ms)} of one run timed launch by launch."""
+        arr = (KernelTime * 32)()
+        n = ctypes.c_int()
+        _check(lib().pa_profile_run(self._h, arr, 32, ctypes.byref(n)), self._h)
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(min(n.value, 32))}
+
     def write_results(self, directory: str, precision: int = 11) -> None:
         os.makedirs(directory, exist_ok=True)
         _check(lib().pa_write_results(self._h, directory.encode(), int(precision)), self._h)
@@ -184,6 +218,13 @@ def schedule(dbeta: float = 0.005, beta_final: float = 1.0) -> np.ndarray:
     out = np.zeros(n.value)
     _check(lib().pa_schedule(dbeta, beta_final, out.ctypes.data, n.value, ctypes.byref(n)))
     return out
+
+
+def probe_int_issue(device: int = 0) -> tuple[float, float, float]:
+    """Measured integer lane-ops/s: (LOP3 only, IMAD only, interleaved)."""
+    out = (ctypes.c_double * 3)()
+    _check(lib().pa_probe_int_issue(device, out))
+    return out[0], out[1], out[2]
 
 
 def ref_word(seed: int, subseq: int, ctr: int) -> int:

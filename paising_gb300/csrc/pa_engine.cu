@@ -94,6 +94,7 @@ struct pa_handle {
   int runs_done = 0;
   double ms = 0.0, attempts = 0.0;
   std::string err;
+  void* staging = nullptr;  // device copy of a caller-supplied initial population
 
   int fail(int code, const std::string& msg) {
     err = msg;
@@ -104,31 +105,65 @@ struct pa_handle {
     return PA_ERR_CUDA;
   }
 
+  // Optional per-kernel timing (pa_profile_run): CUDA events around every
+  // launch on the handle's stream, synchronised per launch.
+  struct Prof {
+    cudaEvent_t a = nullptr, b = nullptr;
+    std::vector<std::pair<std::string, std::pair<int, double>>> acc;
+    void add(const char* name, double ms) {
+      for (auto& x : acc)
+        if (x.first == name) { x.second.first++; x.second.second += ms; return; }
+      acc.push_back({name, {1, ms}});
+    }
+  };
+  Prof* prof = nullptr;
+
+  template <class F>
+  cudaError_t launch(const char* name, F f) {
+    if (!prof) return f();
+    cudaError_t e = cudaEventRecord(prof->a, stream);
+    if (e == cudaSuccess) e = f();
+    if (e == cudaSuccess) e = cudaEventRecord(prof->b, stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(prof->b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, prof->a, prof->b);
+    if (e == cudaSuccess) prof->add(name, ms);
+    return e;
+  }
+
   cudaError_t enqueue_init() {
     cudaError_t e;
-    if ((e = launch_begin_run(d, stream)) != cudaSuccess) return e;
-    e = cfg.coding == PA_CODING_MSC ? launch_msc_init(d, h, stream) : launch_ssc_init(d, h, stream);
+    const bool msc = cfg.coding == PA_CODING_MSC;
+    if ((e = launch("begin_run", [&] { return launch_begin_run(d, stream); })) != cudaSuccess) return e;
+    e = launch(msc ? "msc_init" : "ssc_init",
+               [&] { return msc ? launch_msc_init(d, h, stream) : launch_ssc_init(d, h, stream); });
     if (e != cudaSuccess) return e;
-    e = cfg.coding == PA_CODING_MSC ? launch_msc_sweep(d, geom, cfg.rng_mode, 0, stream)
-                                    : launch_ssc_sweep(d, geom, cfg.rng_mode, 0, stream);
+    e = launch(msc ? "msc_energy" : "ssc_energy", [&] {
+      return msc ? launch_msc_sweep(d, geom, cfg.rng_mode, 0, stream) : launch_ssc_sweep(d, geom, cfg.rng_mode, 0, stream);
+    });
     if (e != cudaSuccess) return e;
-    return launch_finish_step(d, stream);
+    return launch("finish_step", [&] { return launch_finish_step(d, stream); });
   }
 
   cudaError_t enqueue_step() {
     cudaError_t e;
-    if ((e = launch_q(d, h, stream)) != cudaSuccess) return e;
-    if ((e = launch_copy_numbers(d, h, stream)) != cudaSuccess) return e;
-    if ((e = launch_scatter(d, h, stream)) != cudaSuccess) return e;
-    e = cfg.coding == PA_CODING_MSC ? launch_msc_resample(d, h, stream) : launch_ssc_resample(d, h, stream);
+    const bool msc = cfg.coding == PA_CODING_MSC;
+    if ((e = launch("q", [&] { return launch_q(d, h, stream); })) != cudaSuccess) return e;
+    if ((e = launch("copy_numbers", [&] { return launch_copy_numbers(d, h, stream); })) != cudaSuccess) return e;
+    if ((e = launch("scatter", [&] { return launch_scatter(d, h, stream); })) != cudaSuccess) return e;
+    e = launch(msc ? "msc_resample" : "ssc_resample",
+               [&] { return msc ? launch_msc_resample(d, h, stream) : launch_ssc_resample(d, h, stream); });
     if (e != cudaSuccess) return e;
-    e = cfg.coding == PA_CODING_MSC ? launch_msc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream)
-                                    : launch_ssc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream);
+    e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] {
+      return msc ? launch_msc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream)
+                 : launch_ssc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream);
+    });
     if (e != cudaSuccess) return e;
-    return launch_finish_step(d, stream);
+    return launch("finish_step", [&] { return launch_finish_step(d, stream); });
   }
 
   ~pa_handle() {
+    if (staging) cudaFree(staging);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (ev0) cudaEventDestroy(ev0);
@@ -358,6 +393,68 @@ int pa_run(pa_handle* H) {
   if (e != cudaSuccess) return H->cuda_fail(e, "timing");
   H->ms = ms;
   return status;
+}
+
+static size_t population_bytes(const pa_config& c, int R) {
+  const size_t N = (size_t)c.L * c.L;
+  return c.coding == PA_CODING_MSC ? (size_t)((R + kMsb - 1) / kMsb) * N * 4 : (size_t)R * N;
+}
+
+int pa_set_population(pa_handle* H, const void* host) {
+  if (!H) return PA_ERR_ARG;
+  cudaError_t e = cudaSuccess;
+  const void* dev = nullptr;
+  if (host) {
+    const size_t bytes = population_bytes(H->cfg, H->cfg.R);
+    if (!H->staging) e = cudaMalloc(&H->staging, bytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(H->staging, host, bytes, cudaMemcpyHostToDevice, H->stream);
+    dev = H->staging;
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&H->d->init_src, &dev, sizeof(dev), cudaMemcpyHostToDevice, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);  // `dev` lives on this stack frame
+  if (e != cudaSuccess) return H->cuda_fail(e, "set population");
+  H->h.init_src = dev;
+  return PA_OK;
+}
+
+int pa_get_population(const pa_handle* H, void* host, size_t bytes, int* R) {
+  if (!H || !host) return PA_ERR_ARG;
+  if (H->runs_done == 0) return PA_ERR_STATE;
+  PopDev st;
+  cudaError_t e = cudaMemcpy(&st, H->d, sizeof(PopDev), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return PA_ERR_CUDA;
+  const size_t need = population_bytes(H->cfg, st.R_cur);
+  if (R) *R = st.R_cur;
+  if (bytes < need) return PA_ERR_ARG;
+  e = cudaMemcpy(host, st.spins[st.parity], need, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? PA_OK : PA_ERR_CUDA;
+}
+
+int pa_profile_run(pa_handle* H, pa_kernel_time* out, int max, int* n) {
+  if (!H || (max > 0 && !out)) return PA_ERR_ARG;
+  pa_handle::Prof P;
+  cudaError_t e = cudaEventCreate(&P.a);
+  if (e == cudaSuccess) e = cudaEventCreate(&P.b);
+  H->prof = &P;
+  if (e == cudaSuccess) e = H->enqueue_init();
+  for (int i = 1; i <= H->nsteps && e == cudaSuccess; ++i) e = H->enqueue_step();
+  H->prof = nullptr;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (P.a) cudaEventDestroy(P.a);
+  if (P.b) cudaEventDestroy(P.b);
+  if (e != cudaSuccess) return H->cuda_fail(e, "profile run");
+  int k = 0;
+  for (auto& x : P.acc) {
+    if (k < max) {
+      std::snprintf(out[k].name, sizeof(out[k].name), "%s", x.first.c_str());
+      out[k].launches = x.second.first;
+      out[k].total_ms = x.second.second;
+    }
+    ++k;
+  }
+  if (n) *n = k;
+  return PA_OK;
 }
 
 int pa_num_rows(const pa_handle* H, int* n) {

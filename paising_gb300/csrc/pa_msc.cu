@@ -36,15 +36,16 @@ __device__ __forceinline__ void adder4(uint32_t I1, uint32_t I2, uint32_t I3, ui
 
 // One binary digit of the comparison U < T/2^32 done for 32 bits at once:
 // U's digit j is bit i of the random word u for replica bit i, T's digit j
-// is selected per bit from T4 (one anti-parallel neighbour, dE = 4) or T8
-// (none, dE = 8).  Bits decided so far leave `und`; those decided "less"
-// enter `lt`.
-__device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint32_t D4, uint32_t D8, uint32_t& und,
-                                           uint32_t& lt) {
-  const uint32_t p = (s0 & D4) | (~s0 & D8);
-  const uint32_t x = p ^ u;
-  lt |= und & x & p;
-  und &= ~x;
+// is selected per bit from T4 (bits in s0: one anti-parallel neighbour,
+// dE = 4) or T8 (no anti-parallel neighbour, dE = 8).  dg = (D8_j, D4_j ^ D8_j)
+// with D_j = all ones iff digit j of the threshold is 1.  Bits decided at this
+// digit leave `und` (a subtraction, since they are a subset of it); those
+// decided "less" enter `lt`.
+__device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, uint32_t& und, uint32_t& lt) {
+  const uint32_t p = (s0 & dg.y) ^ dg.x;
+  const uint32_t dec = und & (p ^ u);
+  lt |= dec & p;
+  und -= dec;
 }
 
 }  // namespace
@@ -55,6 +56,17 @@ __global__ void msc_init_kernel(PopDev* st) {
   const unsigned long long seed = st->seed, iseq = st->iseq;
   uint32_t* wd = (uint32_t*)st->spins[st->parity];
   uint8_t* act = st->active[st->parity];
+  if (st->init_src) {  // caller-supplied population (replica 32g+k at group g, bit k)
+    const uint4* src = (const uint4*)st->init_src;
+    uint4* dst = (uint4*)wd;
+    const long long nv = (long long)rg * N / 4;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x)
+      dst[v] = src[v];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)rg * kMsb;
+         i += (long long)gridDim.x * blockDim.x)
+      act[i] = i < R;
+    return;
+  }
   const long long total = (long long)rg * h;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -81,10 +93,11 @@ __global__ void msc_init_kernel(PopDev* st) {
 //   every lane is decided (on average ~11 of the 32 possible digits).  Each
 //   replica's acceptance probability is exactly T/2^32, as in the reference.
 template <int MODE>
-__global__ void __launch_bounds__(256) msc_sweep_kernel(PopDev* st, SweepGeom g, int sweeps) {
+__global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom g, int sweeps) {
   extern __shared__ __align__(16) uint32_t lat[];  // N words: A then B
   __shared__ int s_unit;
   __shared__ int s_cntE[kMsb], s_cntM[kMsb];
+  __shared__ uint2 s_dig[kMsb];  // per digit j: (D8_j, D4_j ^ D8_j)
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int L = g.L, N = g.N, h = g.half, Wr = g.Wr;
@@ -98,6 +111,10 @@ __global__ void __launch_bounds__(256) msc_sweep_kernel(PopDev* st, SweepGeom g,
   const uint32_t T4 = st->thr[(size_t)step * kThrPerStep + 10], T8 = st->thr[(size_t)step * kThrPerStep + 11];
   uint32_t* words = (uint32_t*)st->spins[st->parity];
   const uint8_t* act = st->active[st->parity];
+  if (tid < kMsb) {
+    const uint32_t d4 = 0u - ((T4 >> (31 - tid)) & 1u), d8 = 0u - ((T8 >> (31 - tid)) & 1u);
+    s_dig[tid] = make_uint2(d8, d4 ^ d8);
+  }
 
   const bool worker = tid < g.T;
   const int tx = worker ? tid % Wr : 0, rsub = worker ? tid / Wr : 0;
@@ -160,11 +177,10 @@ __global__ void __launch_bounds__(256) msc_sweep_kernel(PopDev* st, SweepGeom g,
             for (int c = 0; c < 8; ++c) {
               if (!__any_sync(0xffffffffu, und != 0u)) break;
               const U4 rn = philox10(c0, cbase | (uint32_t)c, (uint32_t)step, tag, k0, k1);
-              const uint32_t t4 = T4 << (4 * c), t8 = T8 << (4 * c);
-              digit_step(rn.x, s0, (uint32_t)((int)t4 >> 31), (uint32_t)((int)t8 >> 31), und, lt);
-              digit_step(rn.y, s0, (uint32_t)((int)(t4 << 1) >> 31), (uint32_t)((int)(t8 << 1) >> 31), und, lt);
-              digit_step(rn.z, s0, (uint32_t)((int)(t4 << 2) >> 31), (uint32_t)((int)(t8 << 2) >> 31), und, lt);
-              digit_step(rn.w, s0, (uint32_t)((int)(t4 << 3) >> 31), (uint32_t)((int)(t8 << 3) >> 31), und, lt);
+              digit_step(rn.x, s0, s_dig[4 * c + 0], und, lt);
+              digit_step(rn.y, s0, s_dig[4 * c + 1], und, lt);
+              digit_step(rn.z, s0, s_dig[4 * c + 2], und, lt);
+              digit_step(rn.w, s0, s_dig[4 * c + 3], und, lt);
             }
             acc = (s1 | s2) | lt;
           }

@@ -1,0 +1,80 @@
+// pa_probe.cu -- integer-issue throughput probe.
+//
+// The sweeps are bound by the SM's integer pipes (no memory or tensor-core
+// work in the inner loop), so their roofline denominator is the rate at
+// which the SMs can retire 32-bit integer lane operations.  This kernel
+// measures it on the device it runs on: independent chains of LOP3
+// (ALU pipe) interleaved with IMAD (FMA pipe) lane operations, the two
+// integer pipes the sweep kernels use.  Inline PTX keeps the compiler from
+// folding the chains.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/paising.h"
+#include "pa_error.h"
+
+namespace {
+
+constexpr int kProbeIters = 2048;
+
+__global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k, int mode) {
+  uint32_t a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = k * (threadIdx.x + 1) + i;
+  for (int it = 0; it < kProbeIters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (mode == 0 || (mode == 2 && (i & 1)))
+        asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[i]) : "r"(a[(i + 1) & 7]), "r"(k));
+      else
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[i]) : "r"(k), "r"(a[(i + 1) & 7]));
+    }
+  }
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s ^= a[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// lane_ops_per_s[0] = LOP3 only (ALU pipe), [1] = IMAD only (FMA pipe),
+// [2] = alternating LOP3 / IMAD (both integer pipes).
+int pa_probe_int_issue(int device, double* lane_ops_per_s) {
+  if (!lane_ops_per_s) return PA_ERR_ARG;
+  cudaError_t e = cudaSetDevice(device);
+  int nsm = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  const int blocks = nsm * 8, threads = 256;
+  uint32_t* buf = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&buf, (size_t)blocks * threads * sizeof(uint32_t));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int mode = 0; mode < 3 && e == cudaSuccess; ++mode) {
+    float best = 1e30f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+      cudaEventRecord(e0);
+      int_issue_probe<<<blocks, threads>>>(buf, 0x9E3779B9u + rep, mode);
+      cudaEventRecord(e1);
+      e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) best = ms;
+    }
+    lane_ops_per_s[mode] = (double)blocks * threads * kProbeIters * 8 / (best * 1e-3);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (buf) cudaFree(buf);
+  if (e != cudaSuccess) {
+    pa::g_last_error = std::string("int issue probe: ") + cudaGetErrorString(e);
+    return PA_ERR_CUDA;
+  }
+  return PA_OK;
+}
+
+}  // extern "C"

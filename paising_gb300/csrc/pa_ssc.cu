@@ -61,6 +61,14 @@ __global__ void ssc_init_kernel(PopDev* st) {
   const int N = st->N, h = N >> 1, R = st->R_cur;
   const unsigned long long seed = st->seed, iseq = st->iseq;
   int8_t* sp = (int8_t*)st->spins[st->parity];
+  if (st->init_src) {  // caller-supplied population: copy, 16 bytes per thread
+    const uint4* src = (const uint4*)st->init_src;
+    uint4* dst = (uint4*)sp;
+    const long long nv = (long long)R * N / 16;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x)
+      dst[v] = src[v];
+    return;
+  }
   const long long total = (long long)R * h;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {

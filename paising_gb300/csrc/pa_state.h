@@ -40,6 +40,7 @@ struct PopDev {
   double* rows;        // [(nsteps+1) * 10] output rows (columns of PA_results_run_<r>.dat)
   const double* betas; // [nsteps+1]
   const uint32_t* thr; // [(nsteps+1) * kThrPerStep]
+  const void* init_src;  // device copy of a caller-supplied initial population, or null (random init)
   // ------------------------------------------------ dynamic scalars
   int step;            // temperature index being computed (1..nsteps)
   int R_prev;          // population size before resampling

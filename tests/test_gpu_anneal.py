@@ -88,3 +88,24 @@ def test_native_free_energy_vs_kaufman_C2(cuda, oracle, coding):
     assert err.max() <= 1e-4, (err.max(), r[np.argmax(err), 0])
     eE = np.array([oracle.kaufman(64, b)[1] / 4096 for b in r[1:, 0]])
     assert np.max(np.abs(r[1:, 1] - eE)) < 5e-3
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_population_roundtrip(cuda, coding):
+    """pa_set_population / pa_get_population: with no temperature step
+    (dbeta > beta_final) the final population is the uploaded one, and its
+    energies give the beta=0 row's statistics."""
+    L, R = 16, 100
+    rng = np.random.default_rng(5)
+    if coding == "ssc":
+        pop = np.where(rng.integers(0, 2, (R, L * L)) > 0, 1, -1).astype(np.int8)
+    else:
+        pop = rng.integers(0, 2**32, ((R + 31) // 32, L * L), dtype=np.uint32)
+    with pa.Engine(L=L, R=R, sweeps=5, dbeta=2.0, beta_final=1.0, coding=coding) as e:
+        e.set_population(pop)
+        e.run()
+        assert e.num_rows() == 1
+        assert np.array_equal(e.population(), pop)
+        e.set_population(None)
+        e.run()
+        assert not np.array_equal(e.population(), pop)
