@@ -85,40 +85,57 @@ typedef struct pa_handle pa_handle;
 PA_API int pa_config_init(pa_config* cfg);
 
 /* Allocates the population buffers for cfg on cfg->device.  Replaces the
- * set-up part of main() (PAisingSSC.cu:438-479). */
+ * set-up part of main() (PAisingSSC.cu:438-479).  With the native stream,
+ * cfg->runs > 1 independent runs (-M) are annealed concurrently as a batch
+ * of populations with disjoint streams; with the reference stream they run
+ * one after the other because each run continues the previous run's
+ * subsequence counter (PAisingSSC.cu:481-486). */
 PA_API int pa_create(const pa_config* cfg, pa_handle** out);
 
-/* Runs cfg->runs full anneals (beta from 0 while beta <= beta_final), the
+/* A batch of n independent populations, each with its own L, R, sweeps,
+ * dbeta, beta_final and seed (runs must be 1; coding, rng_mode, weights,
+ * graph and device must agree), annealed together: one persistent sweep
+ * launch per temperature step serves every population, so small or uneven
+ * populations fill the GPU.  Population k's rows are result set k.  No
+ * counterpart in the reference, which runs one population per process. */
+PA_API int pa_create_batch(const pa_config* cfgs, int n, pa_handle** out);
+
+/* Runs the handle's anneals (beta from 0 while beta <= beta_final), the
  * population-annealing loop of main() (PAisingSSC.cu:481-664,
  * PAisingMSC.cu:640-814). */
 PA_API int pa_run(pa_handle* h);
 
-/* Number of rows per run of the last pa_run (schedule length + 1). */
+/* Number of result sets a pa_run produces: one per population per
+ * sequential run (PA_results_run_<set>.dat). */
+PA_API int pa_num_sets(const pa_handle* h, int* n);
+
+/* Longest number of rows of any result set (schedule length + 1). */
 PA_API int pa_num_rows(const pa_handle* h, int* nrows);
 
-/* Copies the rows of run `run` (the contents of PA_results_run_<run>.dat,
- * PAisingSSC.cu:670-692) into rows[0..max_rows). */
-PA_API int pa_get_rows(const pa_handle* h, int run, pa_row* rows, int max_rows, int* nrows);
+/* Copies the rows of result set `set` (the contents of
+ * PA_results_run_<set>.dat, PAisingSSC.cu:670-692) into rows[0..max_rows);
+ * *nrows receives the number copied. */
+PA_API int pa_get_rows(const pa_handle* h, int set, pa_row* rows, int max_rows, int* nrows);
 
 /* Device time of the last pa_run in milliseconds (CUDA events around all
  * runs), and the reference's spin-flip attempt count
  * sweeps * N * sum_{i>=1} R_i over all runs (PAisingSSC.cu:632,806). */
 PA_API int pa_get_timing(const pa_handle* h, double* ms, double* attempts);
 
-/* Initial population for the following pa_run calls instead of the random
+/* Initial populations for the following pa_run calls instead of the random
  * initialisation (ReplicaInit, PAisingSSC.cu:150-157) -- e.g. to resume from
- * a saved population.  host points to cfg.R replicas in the stage layout of
- * the handle's coding (SSC: int8 [R][N]; MSC: uint32 [ceil(R/32)][N], bit k of
- * group g = replica 32g+k).  The copy is enqueued on the handle's stream and
- * is complete when the next pa_run returns.  host = NULL restores the random
- * initialisation. */
+ * saved populations.  host holds, for every population of the handle in
+ * order, its R replicas in the stage layout of the handle's coding (SSC: int8
+ * [R][N]; MSC: uint32 [ceil(R/32)][N], bit k of group g = replica 32g+k).
+ * The copies are complete when the call returns.  host = NULL restores the
+ * random initialisation. */
 PA_API int pa_set_population(pa_handle* h, const void* host);
 
-/* Final population of the last run of the last pa_run, in the same layout
- * (MSC groups as stored: replica s of the population is at group s % rg,
- * bit s / rg after resampling, PAisingMSC.cu:413-414).  *R receives the
- * population size; bytes is the capacity of host. */
-PA_API int pa_get_population(const pa_handle* h, void* host, size_t bytes, int* R);
+/* Final population of population `pop` after the last pa_run, in the same
+ * layout (MSC groups as stored: after resampling, replica s is at group
+ * s % rg, bit s / rg, PAisingMSC.cu:413-414).  *R receives the population
+ * size; bytes is the capacity of host. */
+PA_API int pa_get_population(const pa_handle* h, int pop, void* host, size_t bytes, int* R);
 
 /* Per-kernel device time of one run executed launch by launch with CUDA
  * events on the handle's stream around every kernel (serialised; for

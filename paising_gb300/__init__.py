@@ -75,8 +75,10 @@ _SIGS = {
     "pa_last_error": ([_vp], ctypes.c_char_p),
     "pa_schedule": ([_d, _d, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_ref_word": ([_u64, _u64, _u64], ctypes.c_uint32),
+    "pa_create_batch": ([ctypes.POINTER(Config), _i, ctypes.POINTER(_vp)], _i),
+    "pa_num_sets": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_set_population": ([_vp, _vp], _i),
-    "pa_get_population": ([_vp, _vp, ctypes.c_size_t, ctypes.POINTER(_i)], _i),
+    "pa_get_population": ([_vp, _i, _vp, ctypes.c_size_t, ctypes.POINTER(_i)], _i),
     "pa_profile_run": ([_vp, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_probe_int_issue": ([_i, _vp], _i),
     "pa_ssc_init": ([_vp, _i, _i, _u64, _u64, _vp], _i),
@@ -138,9 +140,28 @@ class Engine:
 
     def __init__(self, **kw):
         self.config = make_config(**kw)
+        self.configs = [self.config]
         h = ctypes.c_void_p()
         _check(lib().pa_create(ctypes.byref(self.config), ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def batch(cls, populations: list[dict], **common) -> "Engine":
+        """Independent populations of uneven size annealed together
+        (pa_create_batch); result set k belongs to populations[k]."""
+        e = cls.__new__(cls)
+        e.configs = [make_config(**{**common, **p}) for p in populations]
+        e.config = e.configs[0]
+        arr = (Config * len(e.configs))(*e.configs)
+        h = ctypes.c_void_p()
+        _check(lib().pa_create_batch(arr, len(e.configs), ctypes.byref(h)))
+        e._h = h
+        return e
+
+    def num_sets(self) -> int:
+        n = ctypes.c_int()
+        _check(lib().pa_num_sets(self._h, ctypes.byref(n)), self._h)
+        return n.value
 
     def run(self) -> None:
         _check(lib().pa_run(self._h), self._h)
@@ -150,11 +171,12 @@ class Engine:
         _check(lib().pa_num_rows(self._h, ctypes.byref(n)), self._h)
         return n.value
 
-    def rows(self, run: int = 0) -> np.ndarray:
+    def rows(self, set: int = 0) -> np.ndarray:
+        """Rows of result set `set` (a population, or a sequential run)."""
         n = self.num_rows()
         out = np.zeros((n, 10), dtype=np.float64)
         got = ctypes.c_int()
-        _check(lib().pa_get_rows(self._h, run, out.ctypes.data, n, ctypes.byref(got)), self._h)
+        _check(lib().pa_get_rows(self._h, set, out.ctypes.data, n, ctypes.byref(got)), self._h)
         return out[: got.value]
 
     def timing(self) -> tuple[float, float]:
@@ -169,15 +191,15 @@ class Engine:
         p = host_ptr.ctypes.data if isinstance(host_ptr, np.ndarray) else host_ptr
         _check(lib().pa_set_population(self._h, p), self._h)
 
-    def population(self) -> np.ndarray:
-        """Final population of the last run (SSC int8 [R, N]; MSC uint32 [rg, N])."""
-        c = self.config
+    def population(self, pop: int = 0) -> np.ndarray:
+        """Final population of population `pop` (SSC int8 [R, N]; MSC uint32 [rg, N])."""
+        c = self.configs[pop] if len(self.configs) > 1 else self.config
         N = c.L * c.L
         cap = int(c.R * c.capacity) + 512
         rg = (cap + 31) // 32
         buf = np.zeros(rg * N if c.coding == MSC else cap * N, dtype=np.uint32 if c.coding == MSC else np.int8)
         R = ctypes.c_int()
-        _check(lib().pa_get_population(self._h, buf.ctypes.data, buf.nbytes, ctypes.byref(R)), self._h)
+        _check(lib().pa_get_population(self._h, pop, buf.ctypes.data, buf.nbytes, ctypes.byref(R)), self._h)
         if c.coding == MSC:
             return buf[: ((R.value + 31) // 32) * N].reshape(-1, N)
         return buf[: R.value * N].reshape(R.value, N)
@@ -236,5 +258,5 @@ def anneal(**kw) -> np.ndarray:
     when runs > 1)."""
     with Engine(**kw) as e:
         e.run()
-        runs = e.config.runs
-        return e.rows(0) if runs == 1 else np.stack([e.rows(r) for r in range(runs)])
+        n = e.num_sets()
+        return e.rows(0) if n == 1 else np.stack([e.rows(r) for r in range(n)])

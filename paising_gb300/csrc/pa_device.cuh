@@ -6,6 +6,9 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pa_kernels.h"
+#include "pa_state.h"
+
 namespace pa {
 
 // ----------------------------------------------------------------- Philox
@@ -41,6 +44,34 @@ __host__ __device__ __forceinline__ U4 philox10(uint32_t c0, uint32_t c1, uint32
     c3 = lo0;
     k0 += kPhiloxW0;
     k1 += kPhiloxW1;
+  }
+  return U4{c0, c1, c2, c3};
+}
+
+// Philox4x32-10 with the key schedule k + r*W precomputed once per thread
+// (kk[2r], kk[2r+1] = round-r key); same output as philox10.
+struct PhiloxKeys {
+  uint32_t k[20];
+  __device__ __forceinline__ explicit PhiloxKeys(unsigned long long seed) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+      k[2 * r] = (uint32_t)seed + (uint32_t)r * kPhiloxW0;
+      k[2 * r + 1] = (uint32_t)(seed >> 32) + (uint32_t)r * kPhiloxW1;
+    }
+  }
+};
+
+__device__ __forceinline__ U4 philox10k(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const PhiloxKeys& K) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned long long p0 = (unsigned long long)kPhiloxM0 * c0;
+    const unsigned long long p1 = (unsigned long long)kPhiloxM1 * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ K.k[2 * r];
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ K.k[2 * r + 1];
+    c3 = lo0;
   }
   return U4{c0, c1, c2, c3};
 }
@@ -159,6 +190,33 @@ __device__ __forceinline__ void m4_of(int m, unsigned long long& lo, unsigned lo
 
 __host__ __device__ __forceinline__ double u128_to_double(unsigned long long lo, unsigned long long hi) {
   return (double)hi * 18446744073709551616.0 + (double)lo;
+}
+
+// --------------------------------------------------------- batch work queue
+// Population p and its local unit for queue entry u: prefix[p] <= u < prefix[p+1].
+__device__ __forceinline__ int queue_pop(const BatchDev* b, int u, int* local) {
+  int lo = 0, hi = b->npop;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b->unit_prefix[mid] <= u) lo = mid;
+    else hi = mid;
+  }
+  *local = u - b->unit_prefix[lo];
+  return lo;
+}
+
+// Persistent grid: as many CTAs of `block` threads as can be resident.
+inline cudaError_t persistent_launch(const void* fn, int block, int smem, SweepLaunch* out) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int dev, nsm, per = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem)) != cudaSuccess) return e;
+  out->grid = nsm * (per > 0 ? per : 1);
+  out->block = block;
+  out->smem = smem;
+  return cudaSuccess;
 }
 
 }  // namespace pa

@@ -1,20 +1,24 @@
 // pa_engine.cu -- host driver of the population-annealing engine and the C
 // ABI declared in include/paising.h.
 //
-// One handle = one population configuration on one GPU.  The temperature
-// loop of the reference's main() (PAisingSSC.cu:481-664) becomes, per step,
-//   q -> copy numbers -> scatter -> resample -> sweep(+energy) -> finish
-// launched on the handle's stream with every size read from device memory.
-// In graph mode the whole run (initialisation + all temperatures) is
-// captured once and replayed as a single CUDA graph launch per run; in plain
-// mode the host launches each step and synchronises after it, reading the
-// step's output row like the reference's host loop reads its averages.
+// A handle holds a batch of populations on one GPU (one population for a
+// plain run; several identical ones for concurrent independent runs; uneven
+// ones from pa_create_batch).  The temperature loop of the reference's main()
+// (PAisingSSC.cu:481-664) becomes, per temperature step of the batch,
+//   q -> copy numbers -> scatter -> resample -> plan -> sweep(+energy) -> finish
+// with every population handled by the same launches and every size read
+// from device memory.  In graph mode a whole run of the batch is captured
+// once and replayed as one CUDA graph launch; in plain mode the host launches
+// each step and synchronises after it, reading the step's rows like the
+// reference's host loop reads its averages.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -75,31 +79,47 @@ std::vector<double> schedule(double dbeta, double bfin) {
   return b;
 }
 
-}  // namespace
+size_t population_bytes(int coding, int L, int R) {
+  const size_t N = (size_t)L * L;
+  return coding == PA_CODING_MSC ? (size_t)((R + kMsb - 1) / kMsb) * N * 4 : (size_t)R * N;
+}
 
-struct pa_handle {
+// Host view of one population of a batch.
+struct PopHost {
   pa_config cfg{};
   PopDev h{};
-  PopDev* d = nullptr;
   SweepGeom geom{};
-  DevBuf buf;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
   std::vector<double> betas;
   std::vector<uint32_t> thr;
   int nsteps = 0;
-  std::vector<double> rows;  // runs * (nsteps + 1) * 10
-  int runs_done = 0;
+  int user_index = 0;
+};
+
+}  // namespace
+
+struct pa_handle {
+  std::vector<PopHost> pops;  // device order: descending work per sweep unit
+  int npop = 0;
+  int coding = 0, rng_mode = 0, graph = 1, device = 0;
+  int seq_runs = 1;  // sequential runs of a single population (reference stream, runs > 1)
+  int max_steps = 0;
+  int rblocks = 1;
+  unsigned long long stream_seed = 0;  // key of the native sweep stream (seed of the first population)
+  SweepLaunch sweep{};
+  PopDev* d_pops = nullptr;
+  BatchDev* d_batch = nullptr;
+  DevBuf buf;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraph_t graph_t = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // rows[set] = rows of one population in one run; set = run * npop + user population index
+  std::vector<std::vector<double>> rows;
+  int sets_done = 0;
   double ms = 0.0, attempts = 0.0;
   std::string err;
-  void* staging = nullptr;  // device copy of a caller-supplied initial population
+  std::vector<void*> staging;  // per population: device copy of a caller-supplied initial population
 
-  int fail(int code, const std::string& msg) {
-    err = msg;
-    return code;
-  }
   int cuda_fail(cudaError_t e, const char* what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
     return PA_ERR_CUDA;
@@ -133,44 +153,216 @@ struct pa_handle {
 
   cudaError_t enqueue_init() {
     cudaError_t e;
-    const bool msc = cfg.coding == PA_CODING_MSC;
-    if ((e = launch("begin_run", [&] { return launch_begin_run(d, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_init" : "ssc_init",
-               [&] { return msc ? launch_msc_init(d, h, stream) : launch_ssc_init(d, h, stream); });
+    const bool msc = coding == PA_CODING_MSC;
+    if ((e = launch("begin_run", [&] { return launch_begin_run(d_pops, npop, stream); })) != cudaSuccess) return e;
+    if ((e = launch(msc ? "msc_init" : "ssc_init", [&] { return launch_init(d_pops, npop, coding, stream); })) != cudaSuccess)
+      return e;
+    if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 1, stream); })) != cudaSuccess) return e;
+    e = launch(msc ? "msc_energy" : "ssc_energy", [&] { return launch_sweep(d_batch, coding, rng_mode, 1, stream_seed, sweep, stream); });
     if (e != cudaSuccess) return e;
-    e = launch(msc ? "msc_energy" : "ssc_energy", [&] {
-      return msc ? launch_msc_sweep(d, geom, cfg.rng_mode, 0, stream) : launch_ssc_sweep(d, geom, cfg.rng_mode, 0, stream);
-    });
-    if (e != cudaSuccess) return e;
-    return launch("finish_step", [&] { return launch_finish_step(d, stream); });
+    return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
   }
 
   cudaError_t enqueue_step() {
     cudaError_t e;
-    const bool msc = cfg.coding == PA_CODING_MSC;
-    if ((e = launch("q", [&] { return launch_q(d, h, stream); })) != cudaSuccess) return e;
-    if ((e = launch("copy_numbers", [&] { return launch_copy_numbers(d, h, stream); })) != cudaSuccess) return e;
-    if ((e = launch("scatter", [&] { return launch_scatter(d, h, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_resample" : "ssc_resample",
-               [&] { return msc ? launch_msc_resample(d, h, stream) : launch_ssc_resample(d, h, stream); });
+    const bool msc = coding == PA_CODING_MSC;
+    if ((e = launch("q", [&] { return launch_q(d_pops, npop, rblocks, stream); })) != cudaSuccess) return e;
+    if ((e = launch("copy_numbers", [&] { return launch_copy_numbers(d_pops, npop, rblocks, stream); })) != cudaSuccess)
+      return e;
+    if ((e = launch("scatter", [&] { return launch_scatter(d_pops, npop, rblocks, stream); })) != cudaSuccess) return e;
+    e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_pops, npop, coding, stream); });
     if (e != cudaSuccess) return e;
-    e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] {
-      return msc ? launch_msc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream)
-                 : launch_ssc_sweep(d, geom, cfg.rng_mode, cfg.sweeps, stream);
-    });
+    if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 0, stream); })) != cudaSuccess) return e;
+    e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sweep, stream); });
     if (e != cudaSuccess) return e;
-    return launch("finish_step", [&] { return launch_finish_step(d, stream); });
+    return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+  }
+
+  cudaError_t enqueue_run() {
+    cudaError_t e = enqueue_init();
+    for (int i = 1; i <= max_steps && e == cudaSuccess; ++i) e = enqueue_step();
+    return e;
   }
 
   ~pa_handle() {
-    if (staging) cudaFree(staging);
+    for (void* p : staging)
+      if (p) cudaFree(p);
     if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
+    if (graph_t) cudaGraphDestroy(graph_t);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
   }
 };
+
+namespace {
+
+int validate(const pa_config& c) {
+  auto bad = [](const char* m) {
+    pa::g_last_error = m;
+    return PA_ERR_ARG;
+  };
+  if (c.coding != PA_CODING_SSC && c.coding != PA_CODING_MSC) return bad("coding must be SSC or MSC");
+  if (c.rng_mode != PA_RNG_NATIVE && c.rng_mode != PA_RNG_REFERENCE) return bad("bad rng_mode");
+  if (c.weights != PA_WEIGHTS_FP32 && c.weights != PA_WEIGHTS_FP64) return bad("bad weights");
+  if (c.R < 1 || c.sweeps < 0 || c.runs < 1 || !(c.dbeta > 0) || !(c.beta_final > 0))
+    return bad("R, sweeps, runs, dbeta, beta_final out of range");
+  if (c.capacity != 0 && c.capacity < 1.0) return bad("capacity must be >= 1");
+  SweepGeom g;
+  if (c.coding == PA_CODING_MSC ? !msc_geom(c.L, &g) : !ssc_geom(c.L, &g))
+    return bad(c.coding == PA_CODING_MSC ? "MSC needs even L in [8, 128]" : "SSC needs L % 8 == 0, 8 <= L <= 256");
+  if ((int)schedule(c.dbeta, c.beta_final).size() > kNBmax - 1) {
+    pa::g_last_error = "number of temperature steps exceeds nBmax=10000";
+    return PA_ERR_TOO_MANY_STEPS;
+  }
+  return PA_OK;
+}
+
+// Builds a handle from per-population configurations (already validated and
+// sharing coding, rng_mode, weights, graph, device).
+int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** out) {
+  pa_handle* H = new (std::nothrow) pa_handle();
+  if (!H) return PA_ERR_ARG;
+  auto fail = [&](int code, const std::string& m) {
+    pa::g_last_error = m;
+    delete H;
+    return code;
+  };
+  const pa_config& c0 = cfgs[0];
+  H->coding = c0.coding;
+  H->rng_mode = c0.rng_mode;
+  H->graph = c0.graph;
+  H->device = c0.device;
+  H->seq_runs = seq_runs;
+  H->npop = (int)cfgs.size();
+  H->stream_seed = c0.seed;
+  cudaError_t e = cudaSetDevice(c0.device);
+  if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+
+  H->pops.resize(cfgs.size());
+  for (size_t k = 0; k < cfgs.size(); ++k) {
+    PopHost& P = H->pops[k];
+    P.cfg = cfgs[k];
+    P.user_index = (int)k;
+    if (P.cfg.capacity <= 0) P.cfg.capacity = 1.25;
+    if (P.cfg.coding == PA_CODING_MSC) msc_geom(P.cfg.L, &P.geom);
+    else ssc_geom(P.cfg.L, &P.geom);
+    P.betas = schedule(P.cfg.dbeta, P.cfg.beta_final);
+    P.nsteps = (int)P.betas.size() - 1;
+    P.thr.assign(P.betas.size() * kThrPerStep, 0u);
+    for (size_t i = 0; i < P.betas.size(); ++i) thresholds(P.betas[i], &P.thr[i * kThrPerStep]);
+  }
+  // longest work units first: persistent CTAs then finish the batch together
+  std::stable_sort(H->pops.begin(), H->pops.end(), [](const PopHost& a, const PopHost& b) {
+    return (long long)a.cfg.L * a.cfg.L * a.cfg.sweeps > (long long)b.cfg.L * b.cfg.L * b.cfg.sweeps;
+  });
+
+  int max_smem = 0;
+  long long max_units = 1;
+  DevBuf& B = H->buf;
+  auto chk = [&](cudaError_t err) {
+    if (err != cudaSuccess && e == cudaSuccess) e = err;
+  };
+  for (int k = 0; k < H->npop; ++k) {
+    PopHost& P = H->pops[k];
+    const pa_config& c = P.cfg;
+    PopDev& h = P.h;
+    std::memset(&h, 0, sizeof(h));
+    const int L = c.L, N = L * L;
+    const long long Rcap = (long long)std::ceil(c.capacity * c.R) + 256;
+    const long long rgcap = (Rcap + kMsb - 1) / kMsb;
+    h.L = L;
+    h.N = N;
+    h.coding = c.coding;
+    h.Rinit = c.R;
+    h.Rcap = (int)Rcap;
+    h.rgcap = (int)rgcap;
+    h.sweeps = c.sweeps;
+    h.rng_mode = c.rng_mode;
+    h.weights = c.weights;
+    h.pop_id = P.user_index;
+    h.nsteps = P.nsteps;
+    h.seed = c.seed;
+    h.bf0 = -N * std::log(2.0);
+    geom_to_pop(P.geom, &h);
+    // reference stream: every population starts at initial_sequence = 0 like a
+    // separate run of the reference program; native stream: disjoint ranges
+    h.iseq = c.rng_mode == PA_RNG_REFERENCE ? 0ull : (unsigned long long)P.user_index << 40;
+    max_smem = std::max(max_smem, P.geom.smem);
+    const size_t units = c.coding == PA_CODING_MSC ? (size_t)rgcap * kMsb : (size_t)Rcap;
+    max_units = std::max(max_units, (long long)units);
+    if (c.coding == PA_CODING_MSC) {
+      uint32_t *a = nullptr, *b2 = nullptr;
+      chk(B.alloc(&a, (size_t)rgcap * N));
+      chk(B.alloc(&b2, (size_t)rgcap * N));
+      h.spins[0] = a;
+      h.spins[1] = b2;
+      chk(B.alloc(&h.active[0], units));
+      chk(B.alloc(&h.active[1], units));
+    } else {
+      int8_t *a = nullptr, *b2 = nullptr;
+      chk(B.alloc(&a, (size_t)Rcap * N));
+      chk(B.alloc(&b2, (size_t)Rcap * N));
+      h.spins[0] = a;
+      h.spins[1] = b2;
+    }
+    chk(B.alloc(&h.E, units));
+    chk(B.alloc(&h.M, units));
+    chk(B.alloc(&h.roff, units));
+    chk(B.alloc(&h.offs, units));
+    chk(B.alloc(&h.src, (size_t)Rcap));
+    chk(B.alloc(&h.blk_tot, kResBlocksMax));
+    chk(B.alloc(&h.blk_off, kResBlocksMax));
+    chk(B.alloc(&h.qpart_d, kResBlocksMax));
+    chk(B.alloc(&h.qpart_f, 2 * kResBlocksMax));
+    double* rows = nullptr;
+    chk(B.alloc(&rows, P.betas.size() * kRowCols));
+    h.rows = rows;
+    double* bet = nullptr;
+    chk(B.alloc(&bet, P.betas.size()));
+    h.betas = bet;
+    uint32_t* th = nullptr;
+    chk(B.alloc(&th, P.thr.size()));
+    h.thr = th;
+    if (e != cudaSuccess) break;
+    chk(cudaMemcpy(bet, P.betas.data(), P.betas.size() * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(th, P.thr.data(), P.thr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    H->max_steps = std::max(H->max_steps, P.nsteps);
+  }
+  if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  H->rblocks = res_blocks(max_units);
+  chk(sweep_setup(H->coding, H->rng_mode, max_smem, &H->sweep));
+  chk(B.alloc(&H->d_pops, (size_t)H->npop));
+  chk(B.alloc(&H->d_batch, 1));
+  if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
+  std::vector<PopDev> hp(H->npop);
+  for (int k = 0; k < H->npop; ++k) hp[k] = H->pops[k].h;
+  chk(cudaMemcpy(H->d_pops, hp.data(), sizeof(PopDev) * H->npop, cudaMemcpyHostToDevice));
+  BatchDev bd;
+  std::memset(&bd, 0, sizeof(bd));
+  bd.npop = H->npop;
+  bd.pops = H->d_pops;
+  chk(cudaMemcpy(H->d_batch, &bd, sizeof(bd), cudaMemcpyHostToDevice));
+  chk(cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking));
+  chk(cudaEventCreate(&H->ev0));
+  chk(cudaEventCreate(&H->ev1));
+  H->staging.assign(H->npop, nullptr);
+  if (e == cudaSuccess && H->graph) {
+    chk(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+    if (e == cudaSuccess) {
+      cudaError_t e1 = H->enqueue_run();
+      cudaError_t e2 = cudaStreamEndCapture(H->stream, &H->graph_t);
+      chk(e1);
+      chk(e2);
+      if (e == cudaSuccess) chk(cudaGraphInstantiate(&H->exec, H->graph_t, 0));
+    }
+  }
+  if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
+  *out = H;
+  return PA_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -223,168 +415,91 @@ int pa_config_init(pa_config* c) {
 int pa_create(const pa_config* cfg, pa_handle** out) {
   if (!cfg || !out) return PA_ERR_ARG;
   *out = nullptr;
-  pa_handle* H = new (std::nothrow) pa_handle();
-  if (!H) return PA_ERR_ARG;
-  H->cfg = *cfg;
-  pa_config& c = H->cfg;
-  auto bad = [&](const char* m) {
-    pa::g_last_error = m;
-    delete H;
-    return PA_ERR_ARG;
-  };
-  if (c.coding != PA_CODING_SSC && c.coding != PA_CODING_MSC) return bad("coding must be SSC or MSC");
-  if (c.rng_mode != PA_RNG_NATIVE && c.rng_mode != PA_RNG_REFERENCE) return bad("bad rng_mode");
-  if (c.weights != PA_WEIGHTS_FP32 && c.weights != PA_WEIGHTS_FP64) return bad("bad weights");
-  if (c.R < 1 || c.sweeps < 0 || c.runs < 1 || !(c.dbeta > 0) || !(c.beta_final > 0)) return bad("R, sweeps, runs, dbeta, beta_final out of range");
-  if (c.capacity <= 0) c.capacity = 1.25;
-  if (c.capacity < 1.0) return bad("capacity must be >= 1");
-  bool okg = c.coding == PA_CODING_MSC ? msc_geom(c.L, 256, &H->geom) : ssc_geom(c.L, 256, &H->geom);
-  if (!okg) return bad(c.coding == PA_CODING_MSC ? "MSC needs even L in [8, 128]" : "SSC needs L % 8 == 0, 8 <= L <= 256");
-
-  H->betas = schedule(c.dbeta, c.beta_final);
-  H->nsteps = (int)H->betas.size() - 1;
-  if ((int)H->betas.size() > kNBmax - 1) {
-    pa::g_last_error = "number of temperature steps exceeds nBmax=10000";
-    delete H;
-    return PA_ERR_TOO_MANY_STEPS;
+  int rc = validate(*cfg);
+  if (rc) return rc;
+  // independent runs: concurrent populations with disjoint native streams; with
+  // the reference stream they must run one after the other, because each run
+  // continues the subsequence counter of the previous one (PAisingSSC.cu:481-486)
+  if (cfg->rng_mode == PA_RNG_REFERENCE || cfg->runs == 1) {
+    pa_config c = *cfg;
+    return build_handle({c}, cfg->runs, out);
   }
-  H->thr.assign(H->betas.size() * kThrPerStep, 0u);
-  for (size_t i = 0; i < H->betas.size(); ++i) thresholds(H->betas[i], &H->thr[i * kThrPerStep]);
+  std::vector<pa_config> cs(cfg->runs, *cfg);
+  for (auto& c : cs) c.runs = 1;
+  return build_handle(cs, 1, out);
+}
 
-  cudaError_t e = cudaSetDevice(c.device);
-  if (e != cudaSuccess) { pa::g_last_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e); delete H; return PA_ERR_CUDA; }
-  e = c.coding == PA_CODING_MSC ? msc_sweep_setup(&H->geom, c.rng_mode) : ssc_sweep_setup(&H->geom, c.rng_mode);
-  if (e != cudaSuccess) { pa::g_last_error = std::string("sweep setup: ") + cudaGetErrorString(e); delete H; return PA_ERR_CUDA; }
-
-  PopDev& h = H->h;
-  const int L = c.L, N = L * L;
-  const long long Rcap = (long long)std::ceil(c.capacity * c.R) + 256;
-  const long long rgcap = (Rcap + kMsb - 1) / kMsb;
-  if (Rcap * (long long)(c.coding == PA_CODING_MSC ? 4 : 1) * N > (1ll << 40)) return bad("population too large");
-  h.L = L;
-  h.N = N;
-  h.coding = c.coding;
-  h.Rinit = c.R;
-  h.Rcap = (int)Rcap;
-  h.rgcap = (int)rgcap;
-  h.sweeps = c.sweeps;
-  h.rng_mode = c.rng_mode;
-  h.weights = c.weights;
-  h.pop_id = 0;
-  h.nsteps = H->nsteps;
-  h.seed = c.seed;
-  h.bf0 = -N * std::log(2.0);
-  const size_t units = c.coding == PA_CODING_MSC ? (size_t)rgcap * kMsb : (size_t)Rcap;
-  DevBuf& B = H->buf;
-  auto chk = [&](cudaError_t err, const char* what) { if (err != cudaSuccess && e == cudaSuccess) { e = err; H->err = what; } };
-  if (c.coding == PA_CODING_MSC) {
-    uint32_t *a, *b;
-    chk(B.alloc(&a, (size_t)rgcap * N), "spins");
-    chk(B.alloc(&b, (size_t)rgcap * N), "spins");
-    h.spins[0] = a;
-    h.spins[1] = b;
-    chk(B.alloc(&h.active[0], units), "active");
-    chk(B.alloc(&h.active[1], units), "active");
-  } else {
-    int8_t *a, *b;
-    chk(B.alloc(&a, (size_t)Rcap * N), "spins");
-    chk(B.alloc(&b, (size_t)Rcap * N), "spins");
-    h.spins[0] = a;
-    h.spins[1] = b;
-    h.active[0] = h.active[1] = nullptr;
-  }
-  chk(B.alloc(&h.E, units), "E");
-  chk(B.alloc(&h.M, units), "M");
-  chk(B.alloc(&h.roff, units), "roff");
-  chk(B.alloc(&h.offs, units), "offs");
-  chk(B.alloc(&h.src, (size_t)Rcap), "src");
-  chk(B.alloc(&h.blk_tot, kResBlocksMax), "scratch");
-  chk(B.alloc(&h.blk_off, kResBlocksMax), "scratch");
-  chk(B.alloc(&h.qpart_d, kResBlocksMax), "scratch");
-  chk(B.alloc(&h.qpart_f, 2 * kResBlocksMax), "scratch");
-  double* rows;
-  chk(B.alloc(&rows, H->betas.size() * kRowCols), "rows");
-  h.rows = rows;
-  double* bet;
-  chk(B.alloc(&bet, H->betas.size()), "betas");
-  h.betas = bet;
-  uint32_t* th;
-  chk(B.alloc(&th, H->thr.size()), "thresholds");
-  h.thr = th;
-  chk(B.alloc(&H->d, 1), "state");
-  if (e != cudaSuccess) {
-    pa::g_last_error = std::string("cudaMalloc (") + H->err + "): " + cudaGetErrorString(e);
-    delete H;
-    return PA_ERR_CUDA;
-  }
-  h.iseq = 0;  // initial_sequence = 0 (PAisingSSC.cu:418), continues across runs
-  chk(cudaMemcpy(bet, H->betas.data(), H->betas.size() * sizeof(double), cudaMemcpyHostToDevice), "betas");
-  chk(cudaMemcpy(th, H->thr.data(), H->thr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "thr");
-  chk(cudaMemcpy(H->d, &h, sizeof(PopDev), cudaMemcpyHostToDevice), "state");
-  chk(cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking), "stream");
-  chk(cudaEventCreate(&H->ev0), "event");
-  chk(cudaEventCreate(&H->ev1), "event");
-  if (e == cudaSuccess && c.graph) {
-    chk(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal), "capture");
-    if (e == cudaSuccess) {
-      cudaError_t e1 = H->enqueue_init();
-      for (int i = 1; i <= H->nsteps && e1 == cudaSuccess; ++i) e1 = H->enqueue_step();
-      cudaError_t e2 = cudaStreamEndCapture(H->stream, &H->graph);
-      chk(e1, "capture launches");
-      chk(e2, "end capture");
-      if (e == cudaSuccess) chk(cudaGraphInstantiate(&H->exec, H->graph, 0), "graph instantiate");
+int pa_create_batch(const pa_config* cfgs, int n, pa_handle** out) {
+  if (!cfgs || !out || n < 1 || n > kMaxPop) return PA_ERR_ARG;
+  *out = nullptr;
+  std::vector<pa_config> cs(cfgs, cfgs + n);
+  for (auto& c : cs) {
+    int rc = validate(c);
+    if (rc) return rc;
+    if (c.runs != 1 || c.coding != cs[0].coding || c.rng_mode != cs[0].rng_mode || c.weights != cs[0].weights ||
+        c.graph != cs[0].graph || c.device != cs[0].device) {
+      pa::g_last_error = "batch members need runs=1 and one coding, rng_mode, weights, graph and device";
+      return PA_ERR_ARG;
     }
   }
-  if (e != cudaSuccess) {
-    pa::g_last_error = std::string(H->err) + ": " + cudaGetErrorString(e);
-    delete H;
-    return PA_ERR_CUDA;
-  }
-  *out = H;
+  return build_handle(cs, 1, out);
+}
+
+int pa_num_sets(const pa_handle* H, int* n) {
+  if (!H || !n) return PA_ERR_ARG;
+  *n = H->npop * H->seq_runs;
   return PA_OK;
 }
 
 int pa_run(pa_handle* H) {
   if (!H) return PA_ERR_ARG;
-  const pa_config& c = H->cfg;
-  const size_t nrow = H->betas.size();
-  H->rows.assign((size_t)c.runs * nrow * kRowCols, 0.0);
-  H->runs_done = 0;
+  H->rows.assign((size_t)H->npop * H->seq_runs, {});
+  H->sets_done = 0;
   H->attempts = 0;
   cudaError_t e = cudaEventRecord(H->ev0, H->stream);
   if (e != cudaSuccess) return H->cuda_fail(e, "event");
   int status = PA_OK;
-  for (int r = 0; r < c.runs && status == PA_OK; ++r) {
-    if (c.graph) {
+  std::vector<PopDev> back(H->npop);
+  for (int r = 0; r < H->seq_runs && status == PA_OK; ++r) {
+    if (H->graph) {
       e = cudaGraphLaunch(H->exec, H->stream);
       if (e != cudaSuccess) return H->cuda_fail(e, "graph launch");
     } else {
       e = H->enqueue_init();
       if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-      for (int i = 1; i <= H->nsteps && e == cudaSuccess; ++i) {
+      for (int i = 1; i <= H->max_steps && e == cudaSuccess; ++i) {
         e = H->enqueue_step();
         if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-        double row[kRowCols];
-        if (e == cudaSuccess)
-          e = cudaMemcpy(row, H->h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
+        for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+          if (i > H->pops[k].nsteps) continue;
+          double row[kRowCols];
+          e = cudaMemcpy(row, H->pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
+        }
       }
       if (e != cudaSuccess) return H->cuda_fail(e, "plain step");
     }
-    double* dst = H->rows.data() + (size_t)r * nrow * kRowCols;
-    e = cudaMemcpyAsync(dst, H->h.rows, nrow * kRowCols * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
-    int err_flag = 0;
+    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+      const PopHost& P = H->pops[k];
+      std::vector<double>& dst = H->rows[(size_t)r * H->npop + P.user_index];
+      dst.assign(P.betas.size() * kRowCols, 0.0);
+      e = cudaMemcpyAsync(dst.data(), P.h.rows, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
+    }
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(&err_flag, &H->d->error, sizeof(int), cudaMemcpyDeviceToHost, H->stream);
+      e = cudaMemcpyAsync(back.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost, H->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     if (e != cudaSuccess) return H->cuda_fail(e, "run");
-    if (err_flag) {
-      status = err_flag == 2 ? PA_ERR_EXTINCT : PA_ERR_CAPACITY;
-      H->err = err_flag == 2 ? "resampling produced an empty population"
-                             : "population exceeded its buffer capacity (raise pa_config.capacity)";
-      break;
+    for (int k = 0; k < H->npop; ++k) {
+      if (back[k].error) {
+        status = back[k].error == 2 ? PA_ERR_EXTINCT : PA_ERR_CAPACITY;
+        H->err = back[k].error == 2 ? "resampling produced an empty population"
+                                    : "population exceeded its buffer capacity (raise pa_config.capacity)";
+      }
+      const PopHost& P = H->pops[k];
+      const std::vector<double>& rw = H->rows[(size_t)r * H->npop + P.user_index];
+      for (size_t i = 1; i < P.betas.size(); ++i)
+        H->attempts += (double)P.cfg.sweeps * (double)P.h.N * rw[i * kRowCols + 8];
     }
-    for (size_t i = 1; i < nrow; ++i) H->attempts += (double)c.sweeps * (double)H->h.N * dst[i * kRowCols + 8];
-    H->runs_done = r + 1;
+    if (status == PA_OK) H->sets_done = (r + 1) * H->npop;
   }
   e = cudaEventRecord(H->ev1, H->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(H->ev1);
@@ -395,36 +510,66 @@ int pa_run(pa_handle* H) {
   return status;
 }
 
-static size_t population_bytes(const pa_config& c, int R) {
-  const size_t N = (size_t)c.L * c.L;
-  return c.coding == PA_CODING_MSC ? (size_t)((R + kMsb - 1) / kMsb) * N * 4 : (size_t)R * N;
+int pa_num_rows(const pa_handle* H, int* n) {
+  if (!H || !n) return PA_ERR_ARG;
+  int m = 0;
+  for (const auto& P : H->pops) m = std::max(m, (int)P.betas.size());
+  *n = m;
+  return PA_OK;
+}
+
+int pa_get_rows(const pa_handle* H, int set, pa_row* rows, int max_rows, int* nrows) {
+  if (!H || !rows) return PA_ERR_ARG;
+  if (set < 0 || set >= H->sets_done) return PA_ERR_STATE;
+  const std::vector<double>& src = H->rows[set];
+  const int n = (int)(src.size() / kRowCols);
+  const int m = n < max_rows ? n : max_rows;
+  for (int i = 0; i < m; ++i) std::memcpy(&rows[i], src.data() + (size_t)i * kRowCols, sizeof(pa_row));
+  if (nrows) *nrows = m;
+  return PA_OK;
+}
+
+int pa_get_timing(const pa_handle* H, double* ms, double* attempts) {
+  if (!H) return PA_ERR_ARG;
+  if (ms) *ms = H->ms;
+  if (attempts) *attempts = H->attempts;
+  return PA_OK;
 }
 
 int pa_set_population(pa_handle* H, const void* host) {
   if (!H) return PA_ERR_ARG;
   cudaError_t e = cudaSuccess;
-  const void* dev = nullptr;
-  if (host) {
-    const size_t bytes = population_bytes(H->cfg, H->cfg.R);
-    if (!H->staging) e = cudaMalloc(&H->staging, bytes);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(H->staging, host, bytes, cudaMemcpyHostToDevice, H->stream);
-    dev = H->staging;
+  const char* src = (const char*)host;
+  for (int u = 0; u < H->npop && e == cudaSuccess; ++u) {  // populations in user order
+    int k = 0;
+    while (H->pops[k].user_index != u) ++k;
+    PopHost& P = H->pops[k];
+    const void* dev = nullptr;
+    if (host) {
+      const size_t bytes = population_bytes(H->coding, P.cfg.L, P.cfg.R);
+      if (!H->staging[k]) e = cudaMalloc(&H->staging[k], bytes);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(H->staging[k], src, bytes, cudaMemcpyHostToDevice, H->stream);
+      src += bytes;
+      dev = H->staging[k];
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&H->d_pops[k].init_src, &dev, sizeof(dev), cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);  // `dev` lives on this stack frame
+    P.h.init_src = dev;
   }
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&H->d->init_src, &dev, sizeof(dev), cudaMemcpyHostToDevice, H->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);  // `dev` lives on this stack frame
   if (e != cudaSuccess) return H->cuda_fail(e, "set population");
-  H->h.init_src = dev;
   return PA_OK;
 }
 
-int pa_get_population(const pa_handle* H, void* host, size_t bytes, int* R) {
-  if (!H || !host) return PA_ERR_ARG;
-  if (H->runs_done == 0) return PA_ERR_STATE;
+int pa_get_population(const pa_handle* H, int pop, void* host, size_t bytes, int* R) {
+  if (!H || !host || pop < 0 || pop >= H->npop) return PA_ERR_ARG;
+  if (H->sets_done == 0) return PA_ERR_STATE;
+  int k = 0;
+  while (H->pops[k].user_index != pop) ++k;
   PopDev st;
-  cudaError_t e = cudaMemcpy(&st, H->d, sizeof(PopDev), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(&st, H->d_pops + k, sizeof(PopDev), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return PA_ERR_CUDA;
-  const size_t need = population_bytes(H->cfg, st.R_cur);
+  const size_t need = population_bytes(H->coding, st.L, st.R_cur);
   if (R) *R = st.R_cur;
   if (bytes < need) return PA_ERR_ARG;
   e = cudaMemcpy(host, st.spins[st.parity], need, cudaMemcpyDeviceToHost);
@@ -437,8 +582,7 @@ int pa_profile_run(pa_handle* H, pa_kernel_time* out, int max, int* n) {
   cudaError_t e = cudaEventCreate(&P.a);
   if (e == cudaSuccess) e = cudaEventCreate(&P.b);
   H->prof = &P;
-  if (e == cudaSuccess) e = H->enqueue_init();
-  for (int i = 1; i <= H->nsteps && e == cudaSuccess; ++i) e = H->enqueue_step();
+  if (e == cudaSuccess) e = H->enqueue_run();
   H->prof = nullptr;
   if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
   if (P.a) cudaEventDestroy(P.a);
@@ -457,43 +601,19 @@ int pa_profile_run(pa_handle* H, pa_kernel_time* out, int max, int* n) {
   return PA_OK;
 }
 
-int pa_num_rows(const pa_handle* H, int* n) {
-  if (!H || !n) return PA_ERR_ARG;
-  *n = (int)H->betas.size();
-  return PA_OK;
-}
-
-int pa_get_rows(const pa_handle* H, int run, pa_row* rows, int max_rows, int* nrows) {
-  if (!H || !rows) return PA_ERR_ARG;
-  if (run < 0 || run >= H->runs_done) return PA_ERR_STATE;
-  const int n = (int)H->betas.size();
-  const int m = n < max_rows ? n : max_rows;
-  const double* src = H->rows.data() + (size_t)run * n * kRowCols;
-  for (int i = 0; i < m; ++i) std::memcpy(&rows[i], src + (size_t)i * kRowCols, sizeof(pa_row));
-  if (nrows) *nrows = m;
-  return PA_OK;
-}
-
-int pa_get_timing(const pa_handle* H, double* ms, double* attempts) {
-  if (!H) return PA_ERR_ARG;
-  if (ms) *ms = H->ms;
-  if (attempts) *attempts = H->attempts;
-  return PA_OK;
-}
-
 int pa_write_results(const pa_handle* H, const char* dir, int precision) {
   if (!H || !dir) return PA_ERR_ARG;
-  if (H->runs_done == 0) return PA_ERR_STATE;
-  const int n = (int)H->betas.size();
-  for (int r = 0; r < H->runs_done; ++r) {
+  if (H->sets_done == 0) return PA_ERR_STATE;
+  for (int r = 0; r < H->sets_done; ++r) {
     std::string path = std::string(dir);
     if (!path.empty() && path.back() != '/') path += '/';
     path += "PA_results_run_" + std::to_string(r) + ".dat";
     FILE* f = std::fopen(path.c_str(), "w");
     if (!f) return PA_ERR_ARG;
-    const double* o = H->rows.data() + (size_t)r * n * kRowCols;
+    const std::vector<double>& o = H->rows[r];
+    const int n = (int)(o.size() / kRowCols);
     for (int i = 0; i < n; ++i) {
-      const double* w = o + (size_t)i * kRowCols;
+      const double* w = o.data() + (size_t)i * kRowCols;
       for (int k = 0; k < 8; ++k) std::fprintf(f, "%.*g ", precision, w[k]);
       std::fprintf(f, "%d %.*g\n", (int)w[8], precision, w[9]);
     }

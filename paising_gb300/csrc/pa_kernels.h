@@ -1,4 +1,9 @@
 // pa_kernels.h -- host-side launchers of the engine's CUDA kernels.
+//
+// All launchers work on a batch of populations: per-population kernels take
+// the population from blockIdx.y (resampling) or blockIdx.x (bookkeeping);
+// the sweep kernels are persistent and take work units of all populations
+// from one queue (BatchDev::work_next).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -9,43 +14,59 @@
 
 namespace pa {
 
-// Thread layout of a sweep kernel for one lattice size (chosen on the host).
+// Thread layout of a sweep over one lattice size (chosen on the host and
+// stored per population in PopDev).
 struct SweepGeom {
   int L, N, half;
   int Wr;      // 32-bit words per sublattice row (SSC: 4 sites/word -> L/8; MSC: 1 site/word -> L/2)
   int rpp;     // sublattice rows handled per pass
-  int T;       // threads doing site work = Wr * rpp
-  int block;   // blockDim.x (T rounded up to a multiple of 32)
+  int T;       // threads doing site work = Wr * rpp (<= kSweepThreads)
   int npass;   // ceil(L / rpp)
   int kconst;  // (N/2)/128 when 128 divides N/2 (draws per reference thread per half sweep), else 0
-  int smem;    // dynamic shared memory bytes
-  int grid;    // persistent grid size
+  int smem;    // dynamic shared memory bytes for one work unit
 };
 
-bool ssc_geom(int L, int max_threads, SweepGeom* g);
-bool msc_geom(int L, int max_threads, SweepGeom* g);
+bool ssc_geom(int L, SweepGeom* g);
+bool msc_geom(int L, SweepGeom* g);
+void geom_to_pop(const SweepGeom& g, PopDev* h);
 
-// Occupancy-derived persistent grid for the sweep kernels.
-cudaError_t ssc_sweep_setup(SweepGeom* g, int rng_mode);
-cudaError_t msc_sweep_setup(SweepGeom* g, int rng_mode);
+struct SweepLaunch {
+  int grid, block, smem;
+};
+// Persistent grid for a sweep kernel with `smem` bytes of dynamic shared memory.
+cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out);
 
-// SSC (int8 spins)
-cudaError_t launch_ssc_init(PopDev* st, const PopDev& h, cudaStream_t s);
-cudaError_t launch_ssc_sweep(PopDev* st, const SweepGeom& g, int rng_mode, int sweeps, cudaStream_t s);
-cudaError_t launch_ssc_resample(PopDev* st, const PopDev& h, cudaStream_t s);
+// Work plan of the next sweep launch: unit counts of the populations that
+// take part (energy_only: populations at step 0), prefix sums, queue reset.
+cudaError_t launch_plan(BatchDev* b, int npop, int energy_only, cudaStream_t s);
+// `seed` keys the native sweep stream of the whole batch.
+cudaError_t launch_sweep(BatchDev* b, int coding, int rng_mode, int energy_only, unsigned long long seed,
+                         const SweepLaunch& sl, cudaStream_t s);
 
-// MSC (32 replicas per uint32 word)
-cudaError_t launch_msc_init(PopDev* st, const PopDev& h, cudaStream_t s);
-cudaError_t launch_msc_sweep(PopDev* st, const SweepGeom& g, int rng_mode, int sweeps, cudaStream_t s);
-cudaError_t launch_msc_resample(PopDev* st, const PopDev& h, cudaStream_t s);
+// Random (or caller-supplied) initial populations.
+cudaError_t launch_init(PopDev* pops, int npop, int coding, cudaStream_t s);
 
-// Resampling (both codings)
-int res_blocks(const PopDev& h);
-cudaError_t launch_q(PopDev* st, const PopDev& h, cudaStream_t s);
-cudaError_t launch_copy_numbers(PopDev* st, const PopDev& h, cudaStream_t s);
-cudaError_t launch_scatter(PopDev* st, const PopDev& h, cudaStream_t s);
-// initial statistics / per-step bookkeeping
-cudaError_t launch_begin_run(PopDev* st, cudaStream_t s);
-cudaError_t launch_finish_step(PopDev* st, cudaStream_t s);
+// Resampling (both codings); `blocks` from res_blocks().
+int res_blocks(long long max_units);
+cudaError_t launch_q(PopDev* pops, int npop, int blocks, cudaStream_t s);
+cudaError_t launch_copy_numbers(PopDev* pops, int npop, int blocks, cudaStream_t s);
+cudaError_t launch_scatter(PopDev* pops, int npop, int blocks, cudaStream_t s);
+cudaError_t launch_resample(PopDev* pops, int npop, int coding, cudaStream_t s);
+
+// Coding-specific launchers behind the generic ones above.
+cudaError_t ssc_sweep_setup(int rng_mode, int smem, SweepLaunch* out);
+cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out);
+cudaError_t launch_ssc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+                             const SweepLaunch& sl, cudaStream_t s);
+cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+                             const SweepLaunch& sl, cudaStream_t s);
+cudaError_t launch_ssc_init(PopDev* pops, int npop, cudaStream_t s);
+cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s);
+cudaError_t launch_ssc_resample(PopDev* pops, int npop, cudaStream_t s);
+cudaError_t launch_msc_resample(PopDev* pops, int npop, cudaStream_t s);
+
+// Per-run / per-step bookkeeping.
+cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s);
+cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s);
 
 }  // namespace pa

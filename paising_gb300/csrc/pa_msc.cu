@@ -23,6 +23,8 @@ namespace {
 
 constexpr uint32_t kLcgA = 1664525u;     // PAisingMSC.cu:53
 constexpr uint32_t kLcgC = 1013904223u;  // PAisingMSC.cu:54
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kKB = 4;  // word-sites per thread decided together (native stream)
 
 // Bitsliced count of anti-parallel neighbours (4 inputs -> 3 bit planes),
 // the adder of PAisingMSC.cu:212-218.
@@ -48,10 +50,140 @@ __device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, ui
   und -= dec;
 }
 
+// Remaining digits (from digit 4 on) of one 32-bit comparison word, drawing
+// fresh Philox blocks (counter (c0, c1 | sub0 + c, step, tag)) until every
+// bit of every lane is decided.  Returns the bits decided "less".
+__device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub0,
+                                                  uint32_t step, uint32_t tag, const PhiloxKeys& K,
+                                                  const uint2* dig) {
+  uint32_t lt = 0;
+#pragma unroll 1
+  for (int c = 0; c < 7; ++c) {
+    if (!__any_sync(kFull, und != 0u)) break;
+    const U4 r = philox10k(c0, c1 | (sub0 + c), step, tag, K);
+    digit_step(r.x, am, dig[4 + 4 * c], und, lt);
+    digit_step(r.y, am, dig[5 + 4 * c], und, lt);
+    digit_step(r.z, am, dig[6 + 4 * c], und, lt);
+    digit_step(r.w, am, dig[7 + 4 * c], und, lt);
+  }
+  return lt;
+}
+
+// Exact Metropolis decisions U < T/2^32 for kKB word-sites of one thread.
+// Head: digits 0..3 of every site come from the site's own Philox block;
+// after them only ~1/16 of the bits are undecided.  Tail: those sparse bits
+// of the kKB sites are merged into one word, site k's masks rotated by rot_k
+// so that every (site, replica) pair gets its own bit position -- hence its
+// own fresh digits -- and the remaining digits are drawn once for all sites.
+// A site whose bits find no free rotation is finished on its own.
+//   a[k]   : bits with one anti-parallel neighbour (threshold T4), else T8
+//   und[k] : bits needing a random decision (consumed)
+//   acc[k] : accepted bits (in: outright accepts; out: all accepts)
+__device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t (&und)[kKB], uint32_t (&acc)[kKB],
+                                              const uint32_t (&site)[kKB], uint32_t chain_c0, uint32_t c1,
+                                              uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig) {
+  // independent Philox chains of the kKB sites, interleaved by the compiler
+  const uint2 d0 = dig[0], d1 = dig[1], d2 = dig[2], d3 = dig[3];
+#pragma unroll
+  for (int k = 0; k < kKB; ++k) {
+    const U4 r = philox10k(site[k], c1, step, tag, K);
+    digit_step(r.x, a[k], d0, und[k], acc[k]);
+    digit_step(r.y, a[k], d1, und[k], acc[k]);
+    digit_step(r.z, a[k], d2, und[k], acc[k]);
+    digit_step(r.w, a[k], d3, und[k], acc[k]);
+  }
+  uint32_t m = und[0], am = a[0] & und[0];
+  uint32_t rot[kKB];
+  rot[0] = 0;
+  uint32_t ovf = 0;
+#pragma unroll
+  for (int k = 1; k < kKB; ++k) {
+    uint32_t r = 0;
+    while (r < 32u && (m & __funnelshift_l(und[k], und[k], r))) ++r;
+    rot[k] = r;
+    if (r < 32u) {
+      m |= __funnelshift_l(und[k], und[k], r);
+      am |= __funnelshift_l(a[k] & und[k], a[k] & und[k], r);
+    } else {
+      ovf |= 1u << k;
+    }
+  }
+  const uint32_t lt = finish_digits(m, am, chain_c0, c1, 1u, step, tag, K, dig);
+  acc[0] |= lt & und[0];
+#pragma unroll
+  for (int k = 1; k < kKB; ++k) {
+    if (!(ovf >> k & 1u)) acc[k] |= __funnelshift_r(lt, lt, rot[k]) & und[k];
+    if (__any_sync(kFull, ovf >> k & 1u))
+      acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, step, tag, K, dig);
+  }
+}
+
+// Per-population parameters of the group a CTA is annealing.  They live in
+// shared memory and are read where used, which keeps the hot loops' register
+// footprint independent of how many populations the batch holds.
+struct UnitParams {
+  int L, N, h, Wr, rpp, npass, kconst, step, sweeps, nbatch;
+  uint32_t tag, T4, T8;
+  unsigned long long seed, iseq;
+  uint32_t* words;
+  const uint8_t* act;
+  int32_t* E;
+  int32_t* M;
+};
+
+// Statistics of the groups a CTA annealed for one population, accumulated in
+// shared memory by lane k of warp 0 for replica bit k (registers stay free
+// for the sweep); flushed to the population when the CTA moves on.
+struct BitStats {
+  long long sE[kMsb], sE2[kMsb], sM[kMsb], sM2[kMsb];
+  unsigned long long m4lo[kMsb], m4hi[kMsb];
+  int emin[kMsb];
+  __device__ void reset(int k) {
+    sE[k] = sE2[k] = sM[k] = sM2[k] = 0;
+    m4lo[k] = m4hi[k] = 0;
+    emin[k] = INT_MAX;
+  }
+  __device__ void add(int k, int E, int Mg) {
+    const long long am = Mg < 0 ? -(long long)Mg : (long long)Mg;
+    sE[k] += E;
+    sE2[k] += (long long)E * E;
+    sM[k] += am;
+    sM2[k] += am * am;
+    unsigned long long lo, hi;
+    m4_of(Mg, lo, hi);
+    U128 m{m4lo[k], m4hi[k]};
+    u128_add(m, lo, hi);
+    m4lo[k] = m.lo;
+    m4hi[k] = m.hi;
+    emin[k] = E < emin[k] ? E : emin[k];
+  }
+  // warp 0 only, lane k = bit k
+  __device__ void flush(PopDev* st, int k) {
+    const long long e = warp_sum(sE[k]), e2 = warp_sum(sE2[k]), m = warp_sum(sM[k]), m2 = warp_sum(sM2[k]);
+    const int mn = warp_min(emin[k]);
+    U128 q{m4lo[k], m4hi[k]};
+    for (int o = 16; o > 0; o >>= 1) {  // 128-bit sum across the warp, carries into hi
+      const unsigned long long lo = __shfl_xor_sync(kFull, q.lo, o);
+      const unsigned long long hi = __shfl_xor_sync(kFull, q.hi, o);
+      u128_add(q, lo, hi);
+    }
+    if (k == 0 && mn != INT_MAX) {
+      atomicAdd((unsigned long long*)&st->sE, (unsigned long long)e);
+      atomicAdd((unsigned long long*)&st->sE2, (unsigned long long)e2);
+      atomicAdd((unsigned long long*)&st->sM, (unsigned long long)m);
+      atomicAdd((unsigned long long*)&st->sM2, (unsigned long long)m2);
+      u128_atomic_add(&st->sM4lo, &st->sM4hi, q.lo, q.hi);
+      atomicMin(&st->Emin_acc, mn);
+    }
+    reset(k);
+  }
+};
+
 }  // namespace
 
 // ------------------------------------------------------------------ init
-__global__ void msc_init_kernel(PopDev* st) {
+__global__ void msc_init_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
   const int N = st->N, h = N >> 1, R = st->R_cur, rg = (R + kMsb - 1) / kMsb;
   const unsigned long long seed = st->seed, iseq = st->iseq;
   uint32_t* wd = (uint32_t*)st->spins[st->parity];
@@ -67,6 +199,8 @@ __global__ void msc_init_kernel(PopDev* st) {
       act[i] = i < R;
     return;
   }
+  // ReplicaInit (PAisingMSC.cu:169-188): reference thread t of block B draws
+  // words 2k (gA) and 2k+1 (gB) of subsequence iseq + t + 128 B for idx = t + 128 k
   const long long total = (long long)rg * h;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -80,86 +214,115 @@ __global__ void msc_init_kernel(PopDev* st) {
 }
 
 // ----------------------------------------------------------------- sweep
-// One CTA anneals one group of 32 replicas at a time (dynamic work counter),
-// both sublattices resident in shared memory.  Thread (rsub, tx) owns site
-// column tx of sublattice rows rsub, rsub+rpp, ...
+// Persistent: every CTA takes groups of 32 replicas of any population from
+// the batch's work queue and anneals one group at a time, both sublattices
+// resident in shared memory.  Thread (rsub, tx) owns site column tx of
+// sublattice rows rsub, rsub+rpp, ...
 //
 // MODE kRefCoords: decisions of checkKerALL exactly -- one draw per word-site
 //   (ctr = sw*2K + hf*K + k of subsequence iseq + t + 128 g) expanded to 32
 //   numbers by the LCG and compared with T4 = ceil(2^32 e^-4b), T8.
 // MODE kNative: U_i < T/2^32 for the 32 replica bits is decided digit by
-//   digit, most significant first; digit j of every U_i comes from one fresh
-//   Philox4x32-10 output word, and the warp stops drawing once every bit of
-//   every lane is decided (on average ~11 of the 32 possible digits).  Each
-//   replica's acceptance probability is exactly T/2^32, as in the reference.
+//   digit, most significant first, each digit a fresh Philox4x32-10 bit
+//   (accept_native); each replica's acceptance probability is exactly
+//   T/2^32, as in the reference.  The stream is keyed by stream_seed (one
+//   per batch; populations differ in counter word 3).
 template <int MODE>
-__global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom g, int sweeps) {
+__global__ void __launch_bounds__(kSweepThreads, 5)
+    msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
   extern __shared__ __align__(16) uint32_t lat[];  // N words: A then B
-  __shared__ int s_unit;
+  __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMsb], s_cntM[kMsb];
   __shared__ uint2 s_dig[kMsb];  // per digit j: (D8_j, D4_j ^ D8_j)
+  __shared__ UnitParams P;
+  __shared__ BitStats stats;
 
   const int tid = threadIdx.x, lane = tid & 31;
-  const int L = g.L, N = g.N, h = g.half, Wr = g.Wr;
-  const int R = st->R_cur, step = st->step;
-  const int rg = (R + kMsb - 1) / kMsb;
-  const unsigned long long seed = st->seed;
-  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  const uint32_t tag = kTagMscSweep | (uint32_t)st->pop_id;
-  const int rg_prev = (st->R_prev + kMsb - 1) / kMsb;
-  const unsigned long long iseq = st->iseq + (step > 0 ? (unsigned long long)rg_prev * kMsb : 0ull);
-  const uint32_t T4 = st->thr[(size_t)step * kThrPerStep + 10], T8 = st->thr[(size_t)step * kThrPerStep + 11];
-  uint32_t* words = (uint32_t*)st->spins[st->parity];
-  const uint8_t* act = st->active[st->parity];
-  if (tid < kMsb) {
-    const uint32_t d4 = 0u - ((T4 >> (31 - tid)) & 1u), d8 = 0u - ((T8 >> (31 - tid)) & 1u);
-    s_dig[tid] = make_uint2(d8, d4 ^ d8);
-  }
-
-  const bool worker = tid < g.T;
-  const int tx = worker ? tid % Wr : 0, rsub = worker ? tid / Wr : 0;
-  const int txl = (tx == 0 ? Wr - 1 : tx - 1), txr = (tx + 1 == Wr ? 0 : tx + 1);
-
-  long long sE = 0, sE2 = 0, sM = 0, sM2 = 0;
-  U128 m4{0, 0};
-  int emin = INT_MAX;
+  const int total = b->unit_prefix[b->npop];
+  const PhiloxKeys keys(stream_seed);
+  int cur = -1;
+  int tx = 0, rsub = 0, txl = 0, txr = 0;
+  bool worker = false;
+  if (tid < kMsb) stats.reset(tid);
 
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_unit = (int)atomicAdd(&st->work_next, 1u);
+    if (tid == 0) {
+      const int u = (int)atomicAdd(&b->work_next, 1u);
+      int loc = 0;
+      const int p = u < total ? queue_pop(b, u, &loc) : -1;
+      s_pop = p;
+      s_unit = loc;
+      if (p >= 0 && p != cur) {  // parameters of a new population
+        const PopDev* st = b->pops + p;
+        P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.Wr = st->Wr; P.rpp = st->rpp; P.npass = st->npass;
+        P.kconst = st->kconst;
+        P.step = st->step;
+        P.sweeps = energy_only ? 0 : st->sweeps;
+        P.nbatch = (st->npass + kKB - 1) / kKB;
+        P.tag = kTagMscSweep | (uint32_t)st->pop_id;
+        P.T4 = st->thr[(size_t)st->step * kThrPerStep + 10];
+        P.T8 = st->thr[(size_t)st->step * kThrPerStep + 11];
+        P.seed = st->seed;
+        const int rg_prev = (st->R_prev + kMsb - 1) / kMsb;
+        P.iseq = st->iseq + (st->step > 0 ? (unsigned long long)rg_prev * kMsb : 0ull);
+        P.words = (uint32_t*)st->spins[st->parity];
+        P.act = st->active[st->parity];
+        P.E = st->E;
+        P.M = st->M;
+      }
+    }
     if (tid < kMsb) { s_cntE[tid] = 0; s_cntM[tid] = 0; }
     __syncthreads();
-    const int gi = s_unit;
-    if (gi >= rg) break;
+    const int p = s_pop, gi = s_unit;
+    if (p < 0) break;
+    if (p != cur) {  // block-uniform
+      if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
+      cur = p;
+      const int Wr = P.Wr;
+      worker = tid < Wr * P.rpp;
+      tx = worker ? tid % Wr : 0;
+      rsub = worker ? tid / Wr : 0;
+      txl = (tx == 0 ? Wr - 1 : tx - 1);
+      txr = (tx + 1 == Wr ? 0 : tx + 1);
+      if (tid < kMsb) {
+        const uint32_t d4 = 0u - ((P.T4 >> (31 - tid)) & 1u), d8 = 0u - ((P.T8 >> (31 - tid)) & 1u);
+        s_dig[tid] = make_uint2(d8, d4 ^ d8);
+      }
+    }
+    const int N = P.N, h = P.h;
+    uint32_t* words = P.words;
     const uint4* gsrc = (const uint4*)(words + (size_t)gi * N);
     uint4* lat4 = (uint4*)lat;
     for (int v = tid; v < (N >> 2); v += blockDim.x) lat4[v] = gsrc[v];
     __syncthreads();
 
+    const int sweeps = P.sweeps;
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
       for (int hf = 0; hf < 2; ++hf) {
         uint32_t* self = lat + (hf ? h : 0);
         const uint32_t* oth = lat + (hf ? 0 : h);
+        const int L = P.L, Wr = P.Wr, rpp = P.rpp, npass = P.npass;
+        if (MODE == kRefCoords) {
 #pragma unroll 1
-        for (int pass = 0; pass < g.npass; ++pass) {
-          const int ty = rsub + pass * g.rpp;
-          const bool valid = worker && ty < L;
-          const int tyc = valid ? ty : 0;
-          const int row = tyc * Wr, rowu = (tyc == 0 ? L - 1 : tyc - 1) * Wr, rowd = (tyc + 1 == L ? 0 : tyc + 1) * Wr;
-          const int idx = row + tx;
-          // horizontal neighbour not at the same idx (PAisingMSC.cu:203, 238)
-          const bool left = (hf == 0) == ((tyc & 1) == 0);
-          const uint32_t s = self[idx];
-          const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[idx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
-          uint32_t s0, s1, s2;
-          adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
-          uint32_t acc;
-          if (MODE == kRefCoords) {
+          for (int pass = 0; pass < npass; ++pass) {
+            const int ty = rsub + pass * rpp;
+            const bool valid = worker && ty < L;
+            const int tyc = valid ? ty : 0;
+            const int row = tyc * Wr, rowu = (tyc == 0 ? L - 1 : tyc - 1) * Wr, rowd = (tyc + 1 == L ? 0 : tyc + 1) * Wr;
+            const int idx = row + tx;
+            // horizontal neighbour not at the same idx (PAisingMSC.cu:203, 238)
+            const bool left = (hf == 0) == ((tyc & 1) == 0);
+            const uint32_t s = self[idx];
+            const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[idx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
+            uint32_t s0, s1, s2;
+            adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
             const int t = idx & (kRefThreads - 1), k = idx >> 7;
-            const int K = g.kconst ? g.kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
-            const unsigned long long sub = iseq + (unsigned long long)t + (unsigned long long)kRefThreads * gi;
-            uint32_t ran = ref_word(seed, sub, (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k);
+            const int K = P.kconst ? P.kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
+            const unsigned long long sub = P.iseq + (unsigned long long)t + (unsigned long long)kRefThreads * gi;
+            uint32_t ran = ref_word(P.seed, sub, (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k);
+            const uint32_t T4 = P.T4, T8 = P.T8;
             uint32_t c4 = 0, c8 = 0;
 #pragma unroll 8
             for (int i = 0; i < kMsb; ++i) {
@@ -168,23 +331,40 @@ __global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom
               ran = kLcgA * ran + kLcgC;
             }
             const uint32_t hi = s1 | s2;
-            acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
-          } else {
-            uint32_t und = valid ? ~(s1 | s2) : 0u, lt = 0;
-            const uint32_t c0 = (uint32_t)gi * (uint32_t)h + (uint32_t)idx;
-            const uint32_t cbase = (uint32_t)((sw * 2 + hf) << 3);
-#pragma unroll 1
-            for (int c = 0; c < 8; ++c) {
-              if (!__any_sync(0xffffffffu, und != 0u)) break;
-              const U4 rn = philox10(c0, cbase | (uint32_t)c, (uint32_t)step, tag, k0, k1);
-              digit_step(rn.x, s0, s_dig[4 * c + 0], und, lt);
-              digit_step(rn.y, s0, s_dig[4 * c + 1], und, lt);
-              digit_step(rn.z, s0, s_dig[4 * c + 2], und, lt);
-              digit_step(rn.w, s0, s_dig[4 * c + 3], und, lt);
-            }
-            acc = (s1 | s2) | lt;
+            const uint32_t acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
+            if (valid) self[idx] = s ^ acc;
           }
-          if (valid) self[idx] = s ^ acc;
+        } else {
+          const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+#pragma unroll 1
+          for (int p0 = 0; p0 < npass; p0 += kKB) {
+            uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+            int ix[kKB];
+#pragma unroll
+            for (int k = 0; k < kKB; ++k) {
+              const int pass = p0 + k;
+              const int ty = rsub + pass * rpp;
+              const bool valid = worker && pass < npass && ty < L;
+              const int tyc = valid ? ty : 0;
+              const int row = tyc * Wr, rowu = (tyc == 0 ? L - 1 : tyc - 1) * Wr, rowd = (tyc + 1 == L ? 0 : tyc + 1) * Wr;
+              const int idx = row + tx;
+              const bool left = (hf == 0) == ((tyc & 1) == 0);
+              const uint32_t s = self[idx];
+              const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[idx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
+              uint32_t s0, s1, s2;
+              adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
+              av[k] = s0;
+              ac[k] = s1 | s2;
+              un[k] = valid ? ~(s1 | s2) : 0u;
+              ix[k] = valid ? idx : -1;
+              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)idx;
+            }
+            const uint32_t chain = ((uint32_t)gi * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
+            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig);
+#pragma unroll
+            for (int k = 0; k < kKB; ++k)
+              if (ix[k] >= 0) self[ix[k]] ^= ac[k];
+          }
         }
         __syncthreads();
       }
@@ -193,26 +373,28 @@ __global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom
     // energy and magnetisation per replica bit: the left and up bond of every
     // A and B site (PAisingMSC.cu:272-294), counted per bit with warp ballots.
     int cE = 0, cM = 0;  // lane k accumulates bit k
-    for (int pass = 0; pass < g.npass; ++pass) {
-      const int ty = rsub + pass * g.rpp;
-      const bool valid = worker && ty < L;
-      uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
-      if (valid) {
-        const int row = ty * Wr, idx = row + tx, iL = row + txl, iU = (ty + 1 == L ? 0 : ty + 1) * Wr + tx;
-        sA = lat[idx];
-        sB = lat[h + idx];
-        uint32_t Ai2, Bi2;
-        if (ty & 1) { Ai2 = sB; Bi2 = lat[iL]; }
-        else { Ai2 = lat[h + iL]; Bi2 = sA; }
-        adder4(sA ^ Ai2, sA ^ lat[h + iU], sB ^ Bi2, sB ^ lat[iU], s0, s1, s2);
-      }
+    {
+      const int L = P.L, Wr = P.Wr, rpp = P.rpp, npass = P.npass;
+      for (int pass = 0; pass < npass; ++pass) {
+        const int ty = rsub + pass * rpp;
+        const bool valid = worker && ty < L;
+        uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
+        if (valid) {
+          const int row = ty * Wr, idx = row + tx, iL = row + txl, iU = (ty + 1 == L ? 0 : ty + 1) * Wr + tx;
+          sA = lat[idx];
+          sB = lat[h + idx];
+          uint32_t Ai2, Bi2;
+          if (ty & 1) { Ai2 = sB; Bi2 = lat[iL]; }
+          else { Ai2 = lat[h + iL]; Bi2 = sA; }
+          adder4(sA ^ Ai2, sA ^ lat[h + iU], sB ^ Bi2, sB ^ lat[iU], s0, s1, s2);
+        }
 #pragma unroll 4
-      for (int k = 0; k < kMsb; ++k) {
-        const int e = __popc(__ballot_sync(0xffffffffu, (s0 >> k) & 1u)) +
-                      2 * __popc(__ballot_sync(0xffffffffu, (s1 >> k) & 1u)) +
-                      4 * __popc(__ballot_sync(0xffffffffu, (s2 >> k) & 1u));
-        const int m = __popc(__ballot_sync(0xffffffffu, (sA >> k) & 1u)) + __popc(__ballot_sync(0xffffffffu, (sB >> k) & 1u));
-        if (lane == k) { cE += e; cM += m; }
+        for (int k = 0; k < kMsb; ++k) {
+          const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
+                        4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
+          const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
+          if (lane == k) { cE += e; cM += m; }
+        }
       }
     }
     atomicAdd(&s_cntE[lane], cE);
@@ -222,43 +404,12 @@ __global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom
     __syncthreads();
     if (tid < kMsb) {
       const int E = 2 * s_cntE[tid] - 2 * N, Mg = 2 * s_cntM[tid] - N;
-      st->E[gi * kMsb + tid] = E;
-      st->M[gi * kMsb + tid] = Mg;
-      if (act[gi * kMsb + tid]) {
-        const long long am = Mg < 0 ? -(long long)Mg : (long long)Mg;
-        sE += E;
-        sE2 += (long long)E * E;
-        sM += am;
-        sM2 += am * am;
-        unsigned long long lo, hi;
-        m4_of(Mg, lo, hi);
-        u128_add(m4, lo, hi);
-        emin = E < emin ? E : emin;
-      }
+      P.E[gi * kMsb + tid] = E;
+      P.M[gi * kMsb + tid] = Mg;
+      if (P.act[gi * kMsb + tid]) stats.add(tid, E, Mg);
     }
   }
-  // flush the statistics of this CTA (warp 0 holds them, one lane per bit)
-  if (tid < kMsb) {
-    sE = warp_sum(sE);
-    sE2 = warp_sum(sE2);
-    sM = warp_sum(sM);
-    sM2 = warp_sum(sM2);
-    emin = warp_min(emin);
-    // 128-bit sum across the warp: reduce lo with carries into hi
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long lo = __shfl_xor_sync(0xffffffffu, m4.lo, o);
-      const unsigned long long hi = __shfl_xor_sync(0xffffffffu, m4.hi, o);
-      u128_add(m4, lo, hi);
-    }
-    if (tid == 0 && emin != INT_MAX) {
-      atomicAdd((unsigned long long*)&st->sE, (unsigned long long)sE);
-      atomicAdd((unsigned long long*)&st->sE2, (unsigned long long)sE2);
-      atomicAdd((unsigned long long*)&st->sM, (unsigned long long)sM);
-      atomicAdd((unsigned long long*)&st->sM2, (unsigned long long)sM2);
-      u128_atomic_add(&st->sM4lo, &st->sM4hi, m4.lo, m4.hi);
-      atomicMin(&st->Emin_acc, emin);
-    }
-  }
+  if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
 }
 
 // -------------------------------------------------------------- resample
@@ -266,8 +417,9 @@ __global__ void __launch_bounds__(256, 5) msc_sweep_kernel(PopDev* st, SweepGeom
 // (old group, bit)) at new group s % rg_new, bit s / rg_new
 // (PAisingMSC.cu:413-414).  Here every new word gathers its 32 bits:
 // bit k of new group j comes from old replica src[k*rg_new + j].
-__global__ void msc_resample_kernel(PopDev* st) {
-  if (st->error) return;
+__global__ void msc_resample_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  if (!pop_stepping(st)) return;
   const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb;
   const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1];
   uint32_t* neu = (uint32_t*)st->spins[st->parity];
@@ -291,65 +443,57 @@ __global__ void msc_resample_kernel(PopDev* st) {
   }
 }
 
-// -------------------------------------------------------------- launchers
-static int pick_rpp(int L, int Wr, int max_threads) {
+// -------------------------------------------------------------- geometry
+static int pick_rpp(int L, int Wr) {
   int best = 1;
   for (int r = 1; r <= L; ++r)
-    if (L % r == 0 && Wr * r <= max_threads) best = r;
+    if (L % r == 0 && Wr * r <= kSweepThreads) best = r;
   return best;
 }
 
-bool msc_geom(int L, int max_threads, SweepGeom* g) {
+bool msc_geom(int L, SweepGeom* g) {
   if (L < 8 || L % 2 != 0 || L > 128) return false;
   g->L = L;
   g->N = L * L;
   g->half = g->N / 2;
   g->Wr = L / 2;
-  g->rpp = pick_rpp(L, g->Wr, max_threads);
+  g->rpp = pick_rpp(L, g->Wr);
   g->T = g->Wr * g->rpp;
-  g->block = (g->T + 31) / 32 * 32;
   g->npass = (L + g->rpp - 1) / g->rpp;
   g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
   g->smem = g->N * 4;
-  g->grid = 0;
   return true;
 }
 
-cudaError_t msc_sweep_setup(SweepGeom* g, int rng_mode) {
-  const void* fn = rng_mode == kRefCoords ? (const void*)msc_sweep_kernel<kRefCoords> : (const void*)msc_sweep_kernel<kNative>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g->smem);
-  if (e != cudaSuccess) return e;
-  int dev, nsm, per;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, g->block, g->smem);
-  if (e != cudaSuccess) return e;
-  g->grid = nsm * (per > 0 ? per : 1);
-  return cudaSuccess;
+// -------------------------------------------------------------- launchers
+static const void* msc_sweep_fn(int rng_mode) {
+  return rng_mode == kRefCoords ? (const void*)msc_sweep_kernel<kRefCoords> : (const void*)msc_sweep_kernel<kNative>;
 }
 
-cudaError_t launch_msc_init(PopDev* st, const PopDev& h, cudaStream_t s) {
-  const int rg = (h.Rinit + kMsb - 1) / kMsb;
-  long long total = (long long)rg * (h.N / 2);
-  int blocks = (int)((total + 255) / 256);
-  if (blocks > 4096) blocks = 4096;
-  msc_init_kernel<<<blocks, 256, 0, s>>>(st);
-  return cudaGetLastError();
+cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out) {
+  return persistent_launch(msc_sweep_fn(rng_mode), kSweepThreads, smem, out);
 }
 
-cudaError_t launch_msc_sweep(PopDev* st, const SweepGeom& g, int rng_mode, int sweeps, cudaStream_t s) {
+cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+                             const SweepLaunch& sl, cudaStream_t s) {
   if (rng_mode == kRefCoords)
-    msc_sweep_kernel<kRefCoords><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+    msc_sweep_kernel<kRefCoords><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   else
-    msc_sweep_kernel<kNative><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+    msc_sweep_kernel<kNative><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   return cudaGetLastError();
 }
 
-cudaError_t launch_msc_resample(PopDev* st, const PopDev& h, cudaStream_t s) {
+cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s) {
+  msc_init_kernel<<<dim3(256, npop), 256, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_msc_resample(PopDev* pops, int npop, cudaStream_t s) {
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  msc_resample_kernel<<<nsm * 8, 256, 0, s>>>(st);
+  const int x = (nsm * 8 + npop - 1) / npop;
+  msc_resample_kernel<<<dim3(x < 16 ? 16 : x, npop), 256, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

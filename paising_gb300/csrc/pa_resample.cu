@@ -1,5 +1,5 @@
-// pa_resample.cu -- resampling of the population on the device, no host
-// round trip, and the per-temperature bookkeeping.
+// pa_resample.cu -- resampling of the populations on the device, no host
+// round trip, the per-temperature bookkeeping, and the batch launchers.
 //
 // Replaces, from the reference (both codings):
 //   QKer        (PAisingSSC.cu:217-234, PAisingMSC.cu:319-345) + host lnQ
@@ -13,6 +13,7 @@
 //                                                    -> finish_step_kernel (sums
 //               are accumulated exactly in integers by the sweep kernels)
 //
+// Population p of a batch is handled by the blocks with blockIdx.y == p.
 // Every multi-block reduction ends with the last-block pattern: each block
 // publishes its partial result, takes a ticket, and the block that draws the
 // last ticket combines the partials in block order.  Results therefore do not
@@ -52,7 +53,8 @@ __device__ __forceinline__ float weight32(float dBf, int E, int Emin) {
   return expf(-dBf * (float)(E - Emin));
 }
 
-// last-block ticket: returns true in every thread of the block that finished last
+// last-block ticket: returns true in every thread of the block that finished
+// last among the gridDim.x blocks of its population
 __device__ __forceinline__ bool last_block(unsigned int* ticket) {
   __shared__ bool s_last;
   __threadfence();
@@ -78,10 +80,11 @@ __device__ __forceinline__ void block_chunk(int n, int& lo, int& hi) {
 // FP64 weights: w = exp(-dbeta (E - Emean)), E_ref = Emean (the reference's
 // choice, PAisingSSC.cu:222).  FP32 weights: w = exp(-dbeta (E - Emin)) <= 1,
 // compensated sums, E_ref = Emin; lnQ itself is formed in FP64.
-__global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* st) {
+__global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* pops) {
   __shared__ double s_d[33];
   __shared__ float s_f[2][kResThreads];
-  if (st->error) return;
+  PopDev* st = pops + blockIdx.y;
+  if (!pop_stepping(st)) return;
   const int step = st->step, Rp = st->R_prev, n = pop_units(st, Rp);
   const double dB = st->betas[step] - st->betas[step - 1];
   const uint8_t* act = st->coding == kMSC ? st->active[st->parity] : nullptr;
@@ -96,12 +99,11 @@ __global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* st) {
     if (tid == 0) st->qpart_d[blockIdx.x] = v;
     if (last_block(&st->ticket)) {
       double a = 0.0;
-      for (int b = tid; b < (int)gridDim.x; b += blockDim.x) a += ((volatile double*)st->qpart_d)[b];
+      for (int bb = tid; bb < (int)gridDim.x; bb += blockDim.x) a += ((volatile double*)st->qpart_d)[bb];
       a = block_sum(a, s_d);
       if (tid == 0) {
-        const double lnQ = -(st->betas[step] - st->betas[step - 1]) * Em + log(a) - log((double)Rp);
         st->q = a;
-        st->lnQ = lnQ;
+        st->lnQ = -(st->betas[step] - st->betas[step - 1]) * Em + log(a) - log((double)Rp);
         st->ticket = 0;
       }
     }
@@ -115,17 +117,17 @@ __global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* st) {
     s_f[1][tid] = acc.c;
     __syncthreads();
     if (tid == 0) {
-      Comp32 b;
+      Comp32 bsum;
       float c = 0.f;
-      for (int i = 0; i < (int)blockDim.x; ++i) { b.add(s_f[0][i]); c = __fadd_rn(c, s_f[1][i]); }
-      st->qpart_f[2 * blockIdx.x] = b.s;
-      st->qpart_f[2 * blockIdx.x + 1] = __fadd_rn(b.c, c);
+      for (int i = 0; i < (int)blockDim.x; ++i) { bsum.add(s_f[0][i]); c = __fadd_rn(c, s_f[1][i]); }
+      st->qpart_f[2 * blockIdx.x] = bsum.s;
+      st->qpart_f[2 * blockIdx.x + 1] = __fadd_rn(bsum.c, c);
     }
     if (last_block(&st->ticket) && tid == 0) {
       Comp32 t;
       float c = 0.f;
       const volatile float* qp = st->qpart_f;
-      for (int b = 0; b < (int)gridDim.x; ++b) { t.add(qp[2 * b]); c = __fadd_rn(c, qp[2 * b + 1]); }
+      for (int bb = 0; bb < (int)gridDim.x; ++bb) { t.add(qp[2 * bb]); c = __fadd_rn(c, qp[2 * bb + 1]); }
       const float q = __fadd_rn(t.s, __fadd_rn(t.c, c));
       st->q = (double)q;
       st->lnQ = -dB * (double)Emin + log((double)q) - log((double)Rp);
@@ -142,10 +144,11 @@ __global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* st) {
 // index; for MSC j = 32 * group + bit, PAisingMSC.cu:355).  Block totals are
 // scanned by the last block, which also publishes the new population size
 // and flips the double buffer.
-__global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* st) {
+__global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* pops) {
   __shared__ uint32_t s_u[33];
   __shared__ uint32_t s_run;
-  if (st->error) return;
+  PopDev* st = pops + blockIdx.y;
+  if (!pop_stepping(st)) return;
   const int step = st->step, Rp = st->R_prev, n = pop_units(st, Rp), Rinit = st->Rinit;
   const double dB = st->betas[step] - st->betas[step - 1], lnQ = st->lnQ;
   const uint8_t* act = st->coding == kMSC ? st->active[st->parity] : nullptr;
@@ -181,11 +184,11 @@ __global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* st) {
     if (threadIdx.x == 0) s_run = 0;
     __syncthreads();
     for (int b0 = 0; b0 < (int)gridDim.x; b0 += blockDim.x) {
-      const int b = b0 + threadIdx.x;
-      const uint32_t v = b < (int)gridDim.x ? ((volatile uint32_t*)st->blk_tot)[b] : 0u;
+      const int bb = b0 + threadIdx.x;
+      const uint32_t v = bb < (int)gridDim.x ? ((volatile uint32_t*)st->blk_tot)[bb] : 0u;
       uint32_t total;
       const uint32_t ex = block_exscan(v, s_u, &total);
-      if (b < (int)gridDim.x) st->blk_off[b] = s_run + ex;
+      if (bb < (int)gridDim.x) st->blk_off[bb] = s_run + ex;
       __syncthreads();
       if (threadIdx.x == 0) s_run += total;
       __syncthreads();
@@ -206,9 +209,10 @@ __global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* st) {
 
 // ------------------------------------------------------------------ scatter
 // offs_j = exclusive prefix of roff; src[offs_j + p] = j for p < roff_j.
-__global__ void __launch_bounds__(kResThreads) scatter_kernel(PopDev* st) {
+__global__ void __launch_bounds__(kResThreads) scatter_kernel(PopDev* pops) {
   __shared__ uint32_t s_u[33];
-  if (st->error) return;
+  PopDev* st = pops + blockIdx.y;
+  if (!pop_stepping(st)) return;
   const int n = pop_units(st, st->R_prev);
   int lo, hi;
   block_chunk(n, lo, hi);
@@ -226,8 +230,30 @@ __global__ void __launch_bounds__(kResThreads) scatter_kernel(PopDev* st) {
   }
 }
 
+// ------------------------------------------------------------- sweep plan
+// Unit counts of the populations that take part in the next sweep launch,
+// their exclusive prefix sums, and a fresh work queue.
+__global__ void __launch_bounds__(1024) plan_kernel(BatchDev* b, int energy_only) {
+  __shared__ uint32_t s_u[33];
+  const int p = threadIdx.x, np = b->npop;
+  uint32_t units = 0;
+  if (p < np) {
+    const PopDev* st = b->pops + p;
+    const bool part = energy_only ? (st->step == 0) : pop_stepping(st);
+    if (part) units = st->coding == kMSC ? (uint32_t)((st->R_cur + kMsb - 1) / kMsb) : (uint32_t)st->R_cur;
+  }
+  uint32_t total;
+  const uint32_t ex = block_exscan(units, s_u, &total);
+  if (p < np) b->unit_prefix[p] = (int)ex;
+  if (p == 0) {
+    b->unit_prefix[np] = (int)total;
+    b->work_next = 0;
+  }
+}
+
 // --------------------------------------------------------- run bookkeeping
-__global__ void begin_run_kernel(PopDev* st) {
+__global__ void begin_run_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.x;
   st->step = 0;
   st->R_prev = st->R_cur = st->Rinit;
   st->parity = 0;
@@ -240,7 +266,6 @@ __global__ void begin_run_kernel(PopDev* st) {
   st->sE = st->sE2 = st->sM = st->sM2 = 0;
   st->sM4lo = st->sM4hi = 0;
   st->Emin_acc = INT_MAX;
-  st->work_next = 0;
   st->ticket = 0;
   double* row = st->rows;  // beta = 0 row: only betaF and R are defined (PAisingSSC.cu:435,453)
   for (int c = 0; c < kRowCols; ++c) row[c] = 0.0;
@@ -252,8 +277,10 @@ __global__ void begin_run_kernel(PopDev* st) {
 // written to the output row, state advanced to the next temperature.  The
 // arithmetic uses explicitly rounded operations so that no multiply-add is
 // fused and the row is identical to an unfused host evaluation.
-__global__ void finish_step_kernel(PopDev* st) {
+__global__ void finish_step_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.x;
   const int step = st->step;
+  if (step > st->nsteps) return;  // this population's schedule is complete
   const bool msc = st->coding == kMSC;
   if (step == 0) {
     const int rg = (st->R_cur + kMsb - 1) / kMsb;
@@ -294,39 +321,69 @@ __global__ void finish_step_kernel(PopDev* st) {
   st->sE = st->sE2 = st->sM = st->sM2 = 0;
   st->sM4lo = st->sM4hi = 0;
   st->Emin_acc = INT_MAX;
-  st->work_next = 0;
 }
 
 // ------------------------------------------------------------ launchers
-int res_blocks(const PopDev& h) {
-  const long long units = h.coding == kMSC ? (long long)h.rgcap * kMsb : (long long)h.Rcap;
+int res_blocks(long long units) {
   long long b = (units + kResThreads - 1) / kResThreads;
   if (b > kResBlocksMax) b = kResBlocksMax;
   return (int)(b < 1 ? 1 : b);
 }
 
-cudaError_t launch_q(PopDev* st, const PopDev& h, cudaStream_t s) {
-  q_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+void geom_to_pop(const SweepGeom& g, PopDev* h) {
+  h->Wr = g.Wr;
+  h->rpp = g.rpp;
+  h->T = g.T;
+  h->npass = g.npass;
+  h->kconst = g.kconst;
+}
+
+cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out) {
+  return coding == kMSC ? msc_sweep_setup(rng_mode, smem, out) : ssc_sweep_setup(rng_mode, smem, out);
+}
+
+cudaError_t launch_plan(BatchDev* b, int npop, int energy_only, cudaStream_t s) {
+  (void)npop;
+  plan_kernel<<<1, 1024, 0, s>>>(b, energy_only);
   return cudaGetLastError();
 }
 
-cudaError_t launch_copy_numbers(PopDev* st, const PopDev& h, cudaStream_t s) {
-  copy_numbers_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+cudaError_t launch_sweep(BatchDev* b, int coding, int rng_mode, int energy_only, unsigned long long seed,
+                         const SweepLaunch& sl, cudaStream_t s) {
+  return coding == kMSC ? launch_msc_sweep(b, rng_mode, energy_only, seed, sl, s)
+                        : launch_ssc_sweep(b, rng_mode, energy_only, seed, sl, s);
+}
+
+cudaError_t launch_init(PopDev* pops, int npop, int coding, cudaStream_t s) {
+  return coding == kMSC ? launch_msc_init(pops, npop, s) : launch_ssc_init(pops, npop, s);
+}
+
+cudaError_t launch_resample(PopDev* pops, int npop, int coding, cudaStream_t s) {
+  return coding == kMSC ? launch_msc_resample(pops, npop, s) : launch_ssc_resample(pops, npop, s);
+}
+
+cudaError_t launch_q(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  q_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 
-cudaError_t launch_scatter(PopDev* st, const PopDev& h, cudaStream_t s) {
-  scatter_kernel<<<res_blocks(h), kResThreads, 0, s>>>(st);
+cudaError_t launch_copy_numbers(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  copy_numbers_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 
-cudaError_t launch_begin_run(PopDev* st, cudaStream_t s) {
-  begin_run_kernel<<<1, 1, 0, s>>>(st);
+cudaError_t launch_scatter(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  scatter_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 
-cudaError_t launch_finish_step(PopDev* st, cudaStream_t s) {
-  finish_step_kernel<<<1, 1, 0, s>>>(st);
+cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s) {
+  begin_run_kernel<<<npop, 1, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s) {
+  finish_step_kernel<<<npop, 1, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

@@ -24,11 +24,17 @@ constexpr uint32_t kLsb = 0x01010101u;
 
 __device__ __forceinline__ uint32_t minus_bits(uint32_t w) { return (w >> 1) & kLsb; }  // 1 per byte == -1
 
-// per-replica statistics kept by thread 0 of a sweep CTA
+// per-replica statistics kept by thread 0 of a sweep CTA until the CTA moves
+// to another population or finishes
 struct StatAcc {
-  long long sE = 0, sE2 = 0, sM = 0, sM2 = 0;
-  U128 m4{0, 0};
-  int emin = INT_MAX;
+  long long sE, sE2, sM, sM2;
+  U128 m4;
+  int emin;
+  __device__ void reset() {
+    sE = sE2 = sM = sM2 = 0;
+    m4 = U128{0, 0};
+    emin = INT_MAX;
+  }
   __device__ void add(int e, int m) {
     const long long am = m < 0 ? -(long long)m : (long long)m;
     sE += e;
@@ -41,7 +47,7 @@ struct StatAcc {
     emin = e < emin ? e : emin;
   }
   __device__ void flush(PopDev* st) const {
-    if (sE2 == 0 && emin == INT_MAX) return;
+    if (emin == INT_MAX) return;
     atomicAdd((unsigned long long*)&st->sE, (unsigned long long)sE);
     atomicAdd((unsigned long long*)&st->sE2, (unsigned long long)sE2);
     atomicAdd((unsigned long long*)&st->sM, (unsigned long long)sM);
@@ -57,7 +63,8 @@ struct StatAcc {
 // ReplicaInit (PAisingSSC.cu:150-157): reference thread t of block B draws,
 // for its k-th site idx = t + 128k, uniform number 2k for gA[idx] and 2k+1
 // for gB[idx] from subsequence iseq + t + 128 B; spin = +1 iff U >= 0.5.
-__global__ void ssc_init_kernel(PopDev* st) {
+__global__ void ssc_init_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
   const int N = st->N, h = N >> 1, R = st->R_cur;
   const unsigned long long seed = st->seed, iseq = st->iseq;
   int8_t* sp = (int8_t*)st->spins[st->parity];
@@ -81,9 +88,10 @@ __global__ void ssc_init_kernel(PopDev* st) {
 }
 
 // ----------------------------------------------------------------- sweep
-// One CTA anneals one replica at a time (dynamic work counter), the whole
-// lattice resident in shared memory as 32-bit words of 4 int8 spins.  Thread
-// (rsub, cw) owns word column cw of sublattice rows rsub, rsub+rpp, ...
+// Persistent: every CTA takes replicas of any population from the batch's
+// work queue and anneals one replica at a time, the whole lattice resident in
+// shared memory as 32-bit words of 4 int8 spins.  Thread (rsub, cw) owns word
+// column cw of sublattice rows rsub, rsub+rpp, ...
 //
 // MODE kRefCoords reproduces checkKerALL's decisions exactly: site idx of
 // replica r, sweep sw, half-sweep hf uses draw
@@ -94,34 +102,61 @@ __global__ void ssc_init_kernel(PopDev* st) {
 // MODE kNative draws one Philox4x32-10 block per 4-site word and flips
 // iff dE <= 0 or H < ceil(2^32 exp(-beta dE)).
 template <int MODE>
-__global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g, int sweeps) {
+__global__ void __launch_bounds__(kSweepThreads)
+    ssc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
   extern __shared__ __align__(16) uint32_t lat[];  // N/4 words: A then B
   __shared__ uint32_t s_thr[16];
-  __shared__ int s_unit;
+  __shared__ int s_unit, s_pop;
   __shared__ int s_red[2][33];
 
   const int tid = threadIdx.x;
-  const int L = g.L, N = g.N, h = g.half, Wr = g.Wr, hw = h >> 2;  // hw: words per sublattice
-  const int R = st->R_cur, step = st->step;
-  const unsigned long long seed = st->seed;
-  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  const uint32_t tag = kTagSscSweep | (uint32_t)st->pop_id;
-  // draws consumed by the resampling of this step come before the sweep's
-  const unsigned long long iseq = st->iseq + (step > 0 ? (unsigned long long)st->R_prev : 0ull);
-  int8_t* spins = (int8_t*)st->spins[st->parity];
-  if (tid < kThrPerStep) s_thr[tid] = st->thr[(size_t)step * kThrPerStep + tid];
-
-  const bool worker = tid < g.T;
-  const int cw = worker ? tid % Wr : 0, rsub = worker ? tid / Wr : 0;
-  const int cwl = (cw == 0 ? Wr - 1 : cw - 1), cwr = (cw + 1 == Wr ? 0 : cw + 1);
+  const int total = b->unit_prefix[b->npop];
+  int cur = -1;
+  PopDev* st = nullptr;
+  int L = 0, N = 0, h = 0, Wr = 1, hw = 0, rpp = 1, kconst = 0, step = 0, sweeps = 0;
+  unsigned long long seed = 0, iseq = 0;
+  // native stream key: one seed for the whole batch; populations differ in counter word 3
+  const uint32_t k0 = (uint32_t)stream_seed, k1 = (uint32_t)(stream_seed >> 32);
+  uint32_t tag = 0;
+  int8_t* spins = nullptr;
+  bool worker = false;
+  int cw = 0, rsub = 0, cwl = 0, cwr = 0;
   StatAcc acc;
+  acc.reset();
 
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_unit = (int)atomicAdd(&st->work_next, 1u);
+    if (tid == 0) {
+      const int u = (int)atomicAdd(&b->work_next, 1u);
+      int loc = 0;
+      s_pop = u < total ? queue_pop(b, u, &loc) : -1;
+      s_unit = loc;
+    }
     __syncthreads();
-    const int r = s_unit;
-    if (r >= R) break;
+    const int p = s_pop, r = s_unit;
+    if (p < 0) break;
+    if (p != cur) {  // block-uniform: load the population's parameters
+      if (tid == 0 && st) {
+        acc.flush(st);
+        acc.reset();
+      }
+      cur = p;
+      st = b->pops + p;
+      L = st->L; N = st->N; h = N >> 1; hw = h >> 2; Wr = st->Wr; rpp = st->rpp; kconst = st->kconst;
+      step = st->step;
+      sweeps = energy_only ? 0 : st->sweeps;
+      seed = st->seed;
+      tag = kTagSscSweep | (uint32_t)st->pop_id;
+      // draws consumed by the resampling of this step come before the sweep's
+      iseq = st->iseq + (step > 0 ? (unsigned long long)st->R_prev : 0ull);
+      spins = (int8_t*)st->spins[st->parity];
+      worker = tid < st->T;
+      cw = worker ? tid % Wr : 0;
+      rsub = worker ? tid / Wr : 0;
+      cwl = (cw == 0 ? Wr - 1 : cw - 1);
+      cwr = (cw + 1 == Wr ? 0 : cw + 1);
+      if (tid < kThrPerStep) s_thr[tid] = st->thr[(size_t)step * kThrPerStep + tid];
+    }
     const uint4* gsrc = (const uint4*)(spins + (size_t)r * N);
     uint4* lat4 = (uint4*)lat;
     for (int v = tid; v < (N >> 4); v += blockDim.x) lat4[v] = gsrc[v];
@@ -133,7 +168,7 @@ __global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g,
         uint32_t* self = lat + (hf ? hw : 0);
         const uint32_t* oth = lat + (hf ? 0 : hw);
         if (worker) {
-          for (int ty = rsub; ty < L; ty += g.rpp) {
+          for (int ty = rsub; ty < L; ty += rpp) {
             const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
             const int w = row + cw;
             const uint32_t s = self[w];
@@ -152,7 +187,7 @@ __global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g,
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
                 const int idx = idx0 + j, t = idx & (kRefThreads - 1), k = idx >> 7;
-                const int K = g.kconst ? g.kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
+                const int K = kconst ? kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
                 const unsigned long long sub = iseq + (unsigned long long)t + (unsigned long long)kRefThreads * r;
                 const unsigned long long ctr = (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k;
                 const uint32_t u = ref_word(seed, sub, ctr);
@@ -182,7 +217,7 @@ __global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g,
     // = -2N + 2 * (number of anti-parallel bonds seen from A); M = N - 2 #minus.
     int anti = 0, nminus = 0;
     if (worker) {
-      for (int ty = rsub; ty < L; ty += g.rpp) {
+      for (int ty = rsub; ty < L; ty += rpp) {
         const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
         const int w = row + cw;
         const uint32_t s = lat[w], o = lat[hw + w];
@@ -210,82 +245,76 @@ __global__ void __launch_bounds__(256) ssc_sweep_kernel(PopDev* st, SweepGeom g,
       acc.add(E, Mg);
     }
   }
-  if (tid == 0) acc.flush(st);
+  if (tid == 0 && st) acc.flush(st);
 }
 
 // -------------------------------------------------------------- resample
 // Gather form of resampleKer: new replica s copies old replica src[s].
-__global__ void ssc_resample_kernel(PopDev* st) {
-  if (st->error) return;
+__global__ void ssc_resample_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  if (!pop_stepping(st)) return;
   const int N = st->N, Rn = st->R_cur;
   const uint4* old = (const uint4*)st->spins[st->parity ^ 1];
   uint4* neu = (uint4*)st->spins[st->parity];
   const int nv = N >> 4;
   for (int s = blockIdx.x; s < Rn; s += gridDim.x) {
     const uint4* a = old + (size_t)st->src[s] * nv;
-    uint4* b = neu + (size_t)s * nv;
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) b[v] = a[v];
+    uint4* c = neu + (size_t)s * nv;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) c[v] = a[v];
   }
 }
 
-// -------------------------------------------------------------- launchers
-static int pick_rpp(int L, int Wr, int max_threads) {
+// -------------------------------------------------------------- geometry
+static int pick_rpp(int L, int Wr) {
   int best = 1;
   for (int r = 1; r <= L; ++r)
-    if (L % r == 0 && Wr * r <= max_threads) best = r;
+    if (L % r == 0 && Wr * r <= kSweepThreads) best = r;
   return best;
 }
 
-bool ssc_geom(int L, int max_threads, SweepGeom* g) {
+bool ssc_geom(int L, SweepGeom* g) {
   if (L < 8 || L % 8 != 0 || L > 256) return false;
   g->L = L;
   g->N = L * L;
   g->half = g->N / 2;
   g->Wr = L / 8;
-  g->rpp = pick_rpp(L, g->Wr, max_threads);
+  g->rpp = pick_rpp(L, g->Wr);
   g->T = g->Wr * g->rpp;
-  g->block = (g->T + 31) / 32 * 32;
   g->npass = (L + g->rpp - 1) / g->rpp;
   g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
   g->smem = g->N;
-  g->grid = 0;
   return true;
 }
 
-cudaError_t ssc_sweep_setup(SweepGeom* g, int rng_mode) {
-  const void* fn = rng_mode == kRefCoords ? (const void*)ssc_sweep_kernel<kRefCoords> : (const void*)ssc_sweep_kernel<kNative>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g->smem);
-  if (e != cudaSuccess) return e;
-  int dev, nsm, per;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, g->block, g->smem);
-  if (e != cudaSuccess) return e;
-  g->grid = nsm * (per > 0 ? per : 1);
-  return cudaSuccess;
+// -------------------------------------------------------------- launchers
+static const void* ssc_sweep_fn(int rng_mode) {
+  return rng_mode == kRefCoords ? (const void*)ssc_sweep_kernel<kRefCoords> : (const void*)ssc_sweep_kernel<kNative>;
 }
 
-cudaError_t launch_ssc_init(PopDev* st, const PopDev& h, cudaStream_t s) {
-  long long total = (long long)h.Rinit * (h.N / 2);
-  int blocks = (int)((total + 255) / 256);
-  if (blocks > 4096) blocks = 4096;
-  ssc_init_kernel<<<blocks, 256, 0, s>>>(st);
-  return cudaGetLastError();
+cudaError_t ssc_sweep_setup(int rng_mode, int smem, SweepLaunch* out) {
+  return persistent_launch(ssc_sweep_fn(rng_mode), kSweepThreads, smem, out);
 }
 
-cudaError_t launch_ssc_sweep(PopDev* st, const SweepGeom& g, int rng_mode, int sweeps, cudaStream_t s) {
+cudaError_t launch_ssc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+                             const SweepLaunch& sl, cudaStream_t s) {
   if (rng_mode == kRefCoords)
-    ssc_sweep_kernel<kRefCoords><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+    ssc_sweep_kernel<kRefCoords><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   else
-    ssc_sweep_kernel<kNative><<<g.grid, g.block, g.smem, s>>>(st, g, sweeps);
+    ssc_sweep_kernel<kNative><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ssc_resample(PopDev* st, const PopDev& h, cudaStream_t s) {
+cudaError_t launch_ssc_init(PopDev* pops, int npop, cudaStream_t s) {
+  ssc_init_kernel<<<dim3(512, npop), 256, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssc_resample(PopDev* pops, int npop, cudaStream_t s) {
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  ssc_resample_kernel<<<nsm * 8, 128, 0, s>>>(st);
+  const int x = (nsm * 8 + npop - 1) / npop;
+  ssc_resample_kernel<<<dim3(x < 16 ? 16 : x, npop), 128, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

@@ -1,7 +1,8 @@
 // pa_stages.cu -- stage entry points of the C ABI: one reference kernel (or
 // kernel group) each, on caller-owned device buffers.  They run the same
-// kernels as the engine; a small PopDev describing the caller's buffers is
-// placed in scratch device memory for the duration of the call.
+// kernels as the engine on a batch of one population whose PopDev describes
+// the caller's buffers; that descriptor and the reductions' partial sums live
+// in scratch device memory allocated for the duration of the call.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -9,6 +10,7 @@
 #include <string>
 
 #include "../../include/paising.h"
+#include "pa_device.cuh"
 #include "pa_error.h"
 #include "pa_kernels.h"
 
@@ -21,33 +23,31 @@ int stage_fail(cudaError_t e, const char* what) {
   return PA_ERR_CUDA;
 }
 
-// Scratch of one stage call: the PopDev plus betas/thresholds and the
-// resampling partial-sum buffers.
+// Device scratch of one stage call.
 struct Scratch {
+  BatchDev* b = nullptr;
   PopDev* st = nullptr;
   double* betas = nullptr;
   uint32_t* thr = nullptr;
-  uint32_t* blk = nullptr;   // blk_tot | blk_off
+  uint32_t* blk = nullptr;  // blk_tot | blk_off
   double* qd = nullptr;
   float* qf = nullptr;
   void* base = nullptr;
   cudaError_t alloc() {
-    const size_t sz = 4096 + 2 * sizeof(double) + 2 * kThrPerStep * 4 + 2 * kResBlocksMax * 4 +
-                      kResBlocksMax * 8 + 2 * kResBlocksMax * 4 + 256;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_st = up(sizeof(BatchDev)), o_b = o_st + up(sizeof(PopDev)), o_t = o_b + 256,
+                 o_k = o_t + up(2 * kThrPerStep * 4), o_qd = o_k + up(2 * kResBlocksMax * 4),
+                 o_qf = o_qd + up(kResBlocksMax * 8), sz = o_qf + up(2 * kResBlocksMax * 4);
     cudaError_t e = cudaMalloc(&base, sz);
     if (e != cudaSuccess) return e;
     char* p = (char*)base;
-    st = (PopDev*)p;
-    p += 4096;
-    betas = (double*)p;
-    p += 2 * sizeof(double);
-    thr = (uint32_t*)p;
-    p += 2 * kThrPerStep * 4;
-    blk = (uint32_t*)p;
-    p += 2 * kResBlocksMax * 4;
-    qd = (double*)(((uintptr_t)p + 7) & ~(uintptr_t)7);
-    p = (char*)(qd + kResBlocksMax);
-    qf = (float*)p;
+    b = (BatchDev*)p;
+    st = (PopDev*)(p + o_st);
+    betas = (double*)(p + o_b);
+    thr = (uint32_t*)(p + o_t);
+    blk = (uint32_t*)(p + o_k);
+    qd = (double*)(p + o_qd);
+    qf = (float*)(p + o_qf);
     return cudaSuccess;
   }
   ~Scratch() {
@@ -67,21 +67,70 @@ void fill_thr(double beta, uint32_t* t) {
   t[11] = t8 >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t8;
 }
 
+// A one-population state at temperature step 1 of a one-step schedule.
 PopDev base_state(int coding, int L) {
   PopDev h;
   std::memset(&h, 0, sizeof(h));
   h.coding = coding;
   h.L = L;
   h.N = L * L;
+  h.step = 1;
+  h.nsteps = 1;
   h.Emin_acc = 0x7fffffff;
+  SweepGeom g;
+  if (coding == kMSC ? msc_geom(L, &g) : ssc_geom(L, &g)) geom_to_pop(g, &h);
   return h;
 }
 
-int upload_and_sync(Scratch& S, const PopDev& h, const double* betas, const uint32_t* thr, cudaStream_t s) {
+int upload(Scratch& S, const PopDev& h, const double* betas, const uint32_t* thr, cudaStream_t s) {
+  BatchDev bd;
+  std::memset(&bd, 0, sizeof(bd));
+  bd.npop = 1;
+  bd.pops = S.st;
   cudaError_t e = cudaMemcpyAsync(S.st, &h, sizeof(PopDev), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(S.b, &bd, sizeof(bd), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && betas) e = cudaMemcpyAsync(S.betas, betas, 2 * sizeof(double), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && thr) e = cudaMemcpyAsync(S.thr, thr, 2 * kThrPerStep * 4, cudaMemcpyHostToDevice, s);
   return e == cudaSuccess ? PA_OK : stage_fail(e, "upload");
+}
+
+int finish(cudaError_t e, cudaStream_t s, const char* what) {
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? PA_OK : stage_fail(e, what);
+}
+
+int sweep_stage(int coding, void* spins, uint8_t* active, int L, int units, int sweeps, double beta, int rng_mode,
+                uint64_t seed, uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  SweepGeom g;
+  if (coding == kMSC ? !msc_geom(L, &g) : !ssc_geom(L, &g)) return PA_ERR_ARG;
+  SweepLaunch sl;
+  cudaError_t e = sweep_setup(coding, rng_mode, g.smem, &sl);
+  if (e != cudaSuccess) return stage_fail(e, "sweep setup");
+  Scratch S;
+  if ((e = S.alloc()) != cudaSuccess) return stage_fail(e, "scratch");
+  PopDev h = base_state(coding, L);
+  h.spins[0] = spins;
+  h.active[0] = active;
+  h.R_cur = h.Rinit = coding == kMSC ? units * kMsb : units;
+  h.sweeps = sweeps;
+  h.rng_mode = rng_mode;
+  h.seed = seed;
+  h.iseq = iseq;
+  h.pop_id = step;  // native stream key: the stage call folds (step, population) into pop_id
+  h.E = E;
+  h.M = M;
+  h.betas = S.betas;
+  h.thr = S.thr;
+  double b[2] = {0.0, beta};
+  uint32_t t[2 * kThrPerStep];
+  fill_thr(0.0, t);
+  fill_thr(beta, t + kThrPerStep);
+  int rc = upload(S, h, b, t, s);
+  if (rc) return rc;
+  e = launch_plan(S.b, 1, 0, s);
+  if (e == cudaSuccess) e = launch_sweep(S.b, coding, rng_mode, 0, seed, sl, s);
+  return finish(e, s, "sweep");
 }
 
 }  // namespace
@@ -90,7 +139,7 @@ extern "C" {
 
 int pa_ssc_init(int8_t* spins, int L, int R, uint64_t seed, uint64_t iseq, void* stream) {
   SweepGeom g;
-  if (!spins || R < 1 || !ssc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!spins || R < 1 || !ssc_geom(L, &g)) return PA_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Scratch S;
   cudaError_t e = S.alloc();
@@ -100,49 +149,22 @@ int pa_ssc_init(int8_t* spins, int L, int R, uint64_t seed, uint64_t iseq, void*
   h.R_cur = h.Rinit = R;
   h.seed = seed;
   h.iseq = iseq;
-  int rc = upload_and_sync(S, h, nullptr, nullptr, s);
+  int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  if ((e = launch_ssc_init(S.st, h, s)) != cudaSuccess) return stage_fail(e, "ssc_init");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "ssc_init");
-  return PA_OK;
+  return finish(launch_init(S.st, 1, kSSC, s), s, "ssc_init");
 }
 
 int pa_ssc_sweep(int8_t* spins, int L, int R, int sweeps, double beta, int rng_mode, uint64_t seed,
                  uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream) {
   SweepGeom g;
-  if (!spins || !E || !M || R < 1 || sweeps < 0 || step < 0 || !ssc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!spins || !E || !M || R < 1 || sweeps < 0 || step < 0 || !ssc_geom(L, &g)) return PA_ERR_ARG;
   if (rng_mode != PA_RNG_NATIVE && rng_mode != PA_RNG_REFERENCE) return PA_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = ssc_sweep_setup(&g, rng_mode);
-  if (e != cudaSuccess) return stage_fail(e, "ssc setup");
-  Scratch S;
-  if ((e = S.alloc()) != cudaSuccess) return stage_fail(e, "scratch");
-  PopDev h = base_state(kSSC, L);
-  h.spins[0] = spins;
-  h.R_cur = h.Rinit = R;
-  h.R_prev = 0;
-  h.seed = seed;
-  h.iseq = iseq;
-  h.step = 1;
-  h.pop_id = step;  // native stream key: (step, pop) -- the stage call folds both into pop_id
-  h.E = E;
-  h.M = M;
-  h.betas = S.betas;
-  h.thr = S.thr;
-  double b[2] = {0.0, beta};
-  uint32_t t[2 * kThrPerStep];
-  fill_thr(0.0, t);
-  fill_thr(beta, t + kThrPerStep);
-  int rc = upload_and_sync(S, h, b, t, s);
-  if (rc) return rc;
-  if ((e = launch_ssc_sweep(S.st, g, rng_mode, sweeps, s)) != cudaSuccess) return stage_fail(e, "ssc_sweep");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "ssc_sweep");
-  return PA_OK;
+  return sweep_stage(kSSC, spins, nullptr, L, R, sweeps, beta, rng_mode, seed, iseq, step, E, M, stream);
 }
 
 int pa_msc_init(uint32_t* words, uint8_t* active, int L, int R, uint64_t seed, uint64_t iseq, void* stream) {
   SweepGeom g;
-  if (!words || !active || R < 1 || !msc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!words || !active || R < 1 || !msc_geom(L, &g)) return PA_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Scratch S;
   cudaError_t e = S.alloc();
@@ -153,45 +175,18 @@ int pa_msc_init(uint32_t* words, uint8_t* active, int L, int R, uint64_t seed, u
   h.R_cur = h.Rinit = R;
   h.seed = seed;
   h.iseq = iseq;
-  int rc = upload_and_sync(S, h, nullptr, nullptr, s);
+  int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  if ((e = launch_msc_init(S.st, h, s)) != cudaSuccess) return stage_fail(e, "msc_init");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "msc_init");
-  return PA_OK;
+  return finish(launch_init(S.st, 1, kMSC, s), s, "msc_init");
 }
 
 int pa_msc_sweep(uint32_t* words, const uint8_t* active, int L, int rg, int sweeps, double beta, int rng_mode,
                  uint64_t seed, uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream) {
   SweepGeom g;
-  if (!words || !active || !E || !M || rg < 1 || sweeps < 0 || step < 0 || !msc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!words || !active || !E || !M || rg < 1 || sweeps < 0 || step < 0 || !msc_geom(L, &g)) return PA_ERR_ARG;
   if (rng_mode != PA_RNG_NATIVE && rng_mode != PA_RNG_REFERENCE) return PA_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = msc_sweep_setup(&g, rng_mode);
-  if (e != cudaSuccess) return stage_fail(e, "msc setup");
-  Scratch S;
-  if ((e = S.alloc()) != cudaSuccess) return stage_fail(e, "scratch");
-  PopDev h = base_state(kMSC, L);
-  h.spins[0] = words;
-  h.active[0] = const_cast<uint8_t*>(active);
-  h.R_cur = h.Rinit = rg * kMsb;
-  h.R_prev = 0;
-  h.seed = seed;
-  h.iseq = iseq;
-  h.step = 1;
-  h.pop_id = step;
-  h.E = E;
-  h.M = M;
-  h.betas = S.betas;
-  h.thr = S.thr;
-  double b[2] = {0.0, beta};
-  uint32_t t[2 * kThrPerStep];
-  fill_thr(0.0, t);
-  fill_thr(beta, t + kThrPerStep);
-  int rc = upload_and_sync(S, h, b, t, s);
-  if (rc) return rc;
-  if ((e = launch_msc_sweep(S.st, g, rng_mode, sweeps, s)) != cudaSuccess) return stage_fail(e, "msc_sweep");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "msc_sweep");
-  return PA_OK;
+  return sweep_stage(kMSC, words, const_cast<uint8_t*>(active), L, rg, sweeps, beta, rng_mode, seed, iseq, step, E,
+                     M, stream);
 }
 
 int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding, int R_prev, int Rinit, int Rcap,
@@ -211,7 +206,6 @@ int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding, int R_
   h.rgcap = (Rcap + kMsb - 1) / kMsb;
   h.R_prev = R_prev;
   h.R_cur = R_prev;
-  h.step = 1;
   h.weights = weights;
   h.seed = seed;
   h.iseq = iseq;
@@ -228,16 +222,13 @@ int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding, int R_
   h.qpart_f = S.qf;
   h.betas = S.betas;
   const long long units = coding == PA_CODING_MSC ? (long long)((R_prev + kMsb - 1) / kMsb) * kMsb : R_prev;
-  // launch geometry follows the population that is resampled
-  PopDev g = h;
-  g.Rcap = (int)units;
-  g.rgcap = (int)(units / kMsb + 1);
+  const int blocks = res_blocks(units);
   double b[2] = {beta_prev, beta};
-  int rc = upload_and_sync(S, h, b, nullptr, s);
+  int rc = upload(S, h, b, nullptr, s);
   if (rc) return rc;
-  if ((e = launch_q(S.st, g, s)) != cudaSuccess) return stage_fail(e, "q");
-  if ((e = launch_copy_numbers(S.st, g, s)) != cudaSuccess) return stage_fail(e, "copy numbers");
-  if ((e = launch_scatter(S.st, g, s)) != cudaSuccess) return stage_fail(e, "scatter");
+  if ((e = launch_q(S.st, 1, blocks, s)) != cudaSuccess) return stage_fail(e, "q");
+  if ((e = launch_copy_numbers(S.st, 1, blocks, s)) != cudaSuccess) return stage_fail(e, "copy numbers");
+  if ((e = launch_scatter(S.st, 1, blocks, s)) != cudaSuccess) return stage_fail(e, "scatter");
   PopDev back;
   if ((e = cudaMemcpyAsync(&back, S.st, sizeof(PopDev), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
     return stage_fail(e, "readback");
@@ -252,7 +243,7 @@ int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding, int R_
 
 int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_new, int8_t* new_spins, void* stream) {
   SweepGeom g;
-  if (!old_spins || !src || !new_spins || R_new < 1 || !ssc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!old_spins || !src || !new_spins || R_new < 1 || !ssc_geom(L, &g)) return PA_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Scratch S;
   cudaError_t e = S.alloc();
@@ -262,17 +253,15 @@ int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_n
   h.spins[1] = const_cast<int8_t*>(old_spins);
   h.R_cur = R_new;
   h.src = const_cast<uint32_t*>(src);
-  int rc = upload_and_sync(S, h, nullptr, nullptr, s);
+  int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  if ((e = launch_ssc_resample(S.st, h, s)) != cudaSuccess) return stage_fail(e, "ssc_resample");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "ssc_resample");
-  return PA_OK;
+  return finish(launch_resample(S.st, 1, kSSC, s), s, "ssc_resample");
 }
 
 int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R_new, uint32_t* new_words,
                     uint8_t* new_active, void* stream) {
   SweepGeom g;
-  if (!old_words || !src || !new_words || !new_active || R_new < 1 || !msc_geom(L, 256, &g)) return PA_ERR_ARG;
+  if (!old_words || !src || !new_words || !new_active || R_new < 1 || !msc_geom(L, &g)) return PA_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Scratch S;
   cudaError_t e = S.alloc();
@@ -283,11 +272,9 @@ int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R
   h.active[0] = new_active;
   h.R_cur = R_new;
   h.src = const_cast<uint32_t*>(src);
-  int rc = upload_and_sync(S, h, nullptr, nullptr, s);
+  int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  if ((e = launch_msc_resample(S.st, h, s)) != cudaSuccess) return stage_fail(e, "msc_resample");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return stage_fail(e, "msc_resample");
-  return PA_OK;
+  return finish(launch_resample(S.st, 1, kMSC, s), s, "msc_resample");
 }
 
 }  // extern "C"

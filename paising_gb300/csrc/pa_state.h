@@ -1,10 +1,11 @@
-// pa_state.h -- per-population device state of the annealing engine.
+// pa_state.h -- device state of the annealing engine.
 //
-// One PopDev lives in device memory per population.  Every kernel of a
-// temperature step reads its sizes, buffer pointers and scalars from it, so a
-// whole schedule can be captured once as a CUDA graph: nothing the host knows
-// only after a step (the new population size, the parity of the double
-// buffer, lnQ, ...) is baked into launch arguments.
+// One PopDev lives in device memory per population; a BatchDev lists the
+// populations that advance together.  Every kernel of a temperature step
+// reads its sizes, buffer pointers and scalars from there, so a whole
+// schedule is captured once as a CUDA graph: nothing the host learns only
+// after a step (population sizes, the parity of the double buffer, lnQ, ...)
+// is baked into launch arguments.
 #pragma once
 
 #include <cstdint>
@@ -20,10 +21,15 @@ constexpr int kRefThreads = 128;  // EQthreads (PAisingSSC.cu:62): fixes the ref
 constexpr int kThrPerStep = 12;   // [0..9] SSC table thresholds, [10] T4, [11] T8
 constexpr int kRowCols = 10;
 constexpr int kResBlocksMax = 1024;
+constexpr int kMaxPop = 1024;     // populations per batch
+constexpr int kSweepThreads = 256;
 
 struct PopDev {
   // ------------------------------------------------ configuration (constant)
   int L, N, coding, Rinit, Rcap, rgcap, sweeps, rng_mode, weights, pop_id, nsteps, pad0;
+  // sweep thread layout (see SweepGeom): words per row, rows per pass,
+  // worker threads, passes, reference draws per thread per half sweep
+  int Wr, rpp, T, npass, kconst, pad1;
   unsigned long long seed;
   // ------------------------------------------------ buffers
   void* spins[2];      // SSC: int8 [Rcap][N] (+-1, sublattice A then B); MSC: uint32 [rgcap][N]
@@ -42,15 +48,15 @@ struct PopDev {
   const uint32_t* thr; // [(nsteps+1) * kThrPerStep]
   const void* init_src;  // device copy of a caller-supplied initial population, or null (random init)
   // ------------------------------------------------ dynamic scalars
-  int step;            // temperature index being computed (1..nsteps)
+  int step;            // temperature index being computed (1..nsteps); nsteps+1 when done
   int R_prev;          // population size before resampling
   int R_cur;           // population size after resampling
   int parity;          // spins[parity] holds the current population
-  int error;           // 0 ok, 1 capacity exceeded
+  int error;           // 0 ok, 1 capacity exceeded, 2 population extinct
   int Emin;            // minimum energy of the current population
-  unsigned int work_next;  // dynamic work counter of the sweep kernel
   unsigned int ticket;     // last-block tickets of the resampling kernels
-  unsigned long long iseq; // reference subsequence counter (initial_sequence, PAisingSSC.cu:418)
+  unsigned int pad2;
+  unsigned long long iseq;  // reference subsequence counter (initial_sequence, PAisingSSC.cu:418)
   double Emean;        // <E> of the current population (Emean, PAisingSSC.cu:483,620)
   double sumlnQ;       // -sum of lnQ over the steps so far (PAisingSSC.cu:627)
   double lnQ;          // lnQ of the step being computed
@@ -59,7 +65,22 @@ struct PopDev {
   // ------------------------------------------------ statistics accumulators
   long long sE, sE2, sM, sM2;
   unsigned long long sM4lo, sM4hi;
-  int Emin_acc, pad1;
+  int Emin_acc, pad3;
 };
+
+// Populations advancing together.  unit_prefix[p] .. unit_prefix[p+1]-1 are
+// the sweep work units (SSC replicas, MSC groups) of population p in the
+// current sweep launch; work_next hands them out to persistent CTAs.
+struct BatchDev {
+  int npop;
+  unsigned int work_next;
+  PopDev* pops;
+  int unit_prefix[kMaxPop + 1];
+};
+
+// A population takes part in the current temperature step.
+__host__ __device__ inline bool pop_stepping(const PopDev* st) {
+  return st->step >= 1 && st->step <= st->nsteps && !st->error;
+}
 
 }  // namespace pa
