@@ -43,7 +43,9 @@ def parse_args(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc")
-    ap.add_argument("--populations", type=int, default=1, help="independent populations per engine launch")
+    ap.add_argument("--populations", type=int, default=8,
+                    help="independent populations per engine launch (the batched form; 1 = plain)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain single-population comparison")
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--R", type=int, default=20000)
     ap.add_argument("--sweeps", type=int, default=100)
@@ -246,6 +248,7 @@ def run_ours(a):
                        "graph": bool(a.graph), "parallelism": f"replicas x{ws}",
                        "l2": "flushed between timed steps (256 MB write)"},
             "full_anneal_s": tot_ms_max / a.steps / 1e3,
+            "full_anneal_s_per_population": tot_ms_max / a.steps / 1e3 / P,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": pop_bytes,
                     "d2h_bytes_per_step": rows_bytes + 4 * P},
             "gpu_launches": launches_per_run * a.steps,
@@ -253,6 +256,8 @@ def run_ours(a):
         }
         if not a.no_profile:
             out.update(profile_leg(a, eng, pa))
+        if not a.no_plain and P > 1:
+            out["plain"] = plain_leg(a, dev, flush)
         if not a.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(a)
     eng.close()
@@ -262,14 +267,38 @@ def run_ours(a):
     return out
 
 
+def plain_leg(a, dev, flush) -> dict:
+    """The plain form on the same GPU: one population per launch sequence,
+    the host stepping every temperature and synchronising after it."""
+    import torch
+
+    import paising_gb300 as pa
+    out = {}
+    for graph in (False, True):
+        with pa.Engine(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=1, seed=4242,
+                       coding=a.coding, rng="native", weights="fp32", graph=graph, device=dev) as e:
+            e.run()
+            ms, att = [], []
+            for _ in range(a.steps):
+                flush.zero_()
+                torch.cuda.synchronize(dev)
+                e.run()
+                t, n = e.timing()
+                ms.append(t)
+                att.append(n)
+        key = "graph" if graph else "host_stepped"
+        out[key] = {"value": sum(att) / (sum(ms) * 1e6), "unit": UNIT, "ms_per_anneal": sum(ms) / len(ms)}
+    return out
+
+
 def profile_leg(a, eng, pa) -> dict:
     """Per-kernel device times of one run (CUDA events around each launch on
     the engine's stream) and the roofline of the dominant kernel."""
     prof = eng.profile()
     tot = sum(v[1] for v in prof.values())
-    rows = eng.rows(0)
-    Rs = rows[1:, 8]
     N = a.L * a.L
+    # replicas swept per launch: all populations of the batch at one temperature
+    Rs = sum(eng.rows(k)[1:, 8] for k in range(eng.num_sets()))
     sweep = f"{a.coding}_sweep"
     n_launch, sweep_ms = prof[sweep]
     avg_ms = sweep_ms / n_launch
