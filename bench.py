@@ -303,7 +303,10 @@ def profile_leg(a, eng, pa) -> dict:
     n_launch, sweep_ms = prof[sweep]
     avg_ms = sweep_ms / n_launch
     attempts_per_launch = a.sweeps * N * Rs.mean()
-    ops_per_attempt = 5.0 if a.coding == "msc" else 33.0  # algorithmic INT32 ops (SURVEY 8d figures)
+    # algorithmic INT32 operations per spin-flip attempt: MSC ~5 (bitsliced
+    # neighbour count and acceptance mask shared by 32 replicas), SSC ~33 (a
+    # 32-bit Philox word, ~25 operations, plus the update of one site)
+    ops_per_attempt = 5.0 if a.coding == "msc" else 33.0
     achieved = attempts_per_launch * ops_per_attempt / (avg_ms * 1e-3) / 1e12
     peaks = pa.probe_int_issue(eng.config.device)
     peak = max(peaks) / 1e12
@@ -311,7 +314,9 @@ def profile_leg(a, eng, pa) -> dict:
     return {
         "kernels": {k: {"launches": v[0], "total_ms": v[1], "share": v[1] / tot} for k, v in prof.items()},
         "roofline": {"kernel": sweep, "bound": "int32", "achieved": achieved, "peak": peak, "unit": "Tops/s",
-                     "frac": achieved / peak, "traffic": load_profile_traffic(sweep, workload),
+                     "frac": achieved / peak,
+                     # ncu DRAM bytes of one single-population launch, scaled by the populations per launch
+                     "traffic": (lambda t: None if t is None else t * eng.num_sets())(load_profile_traffic(sweep, workload)),
                      "ops_per_attempt": ops_per_attempt, "attempts_per_launch": attempts_per_launch,
                      "avg_launch_ms": avg_ms,
                      "peak_source": "measured in-process: integer lane-op issue rate, LOP3/IMAD chains "

@@ -70,6 +70,11 @@ def _patch(text: str, rules, L: int) -> str:
     return text
 
 
+def reference_available() -> bool:
+    """The reference checkout is present (true in the build container only)."""
+    return os.path.isdir(REF_DIR)
+
+
 def patch(sizes) -> None:
     os.makedirs(SRC_OUT, exist_ok=True)
     for prog, rules in (("SSC", _SSC), ("MSC", _MSC)):

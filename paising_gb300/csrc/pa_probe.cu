@@ -20,15 +20,18 @@ constexpr int kProbeIters = 2048;
 
 __global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k, int mode) {
   uint32_t a[8];
+  const uint32_t k2 = k * 3u + 1u;
 #pragma unroll
   for (int i = 0; i < 8; ++i) a[i] = k * (threadIdx.x + 1) + i;
+  // eight independent chains per thread: each instruction depends only on
+  // its own chain's previous result
   for (int it = 0; it < kProbeIters; ++it) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      if (mode == 0 || (mode == 2 && (i & 1)))
-        asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[i]) : "r"(a[(i + 1) & 7]), "r"(k));
+      if (mode == 0 || (mode == 2 && i < 4))
+        asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[i]) : "r"(k), "r"(k2));
       else
-        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[i]) : "r"(k), "r"(a[(i + 1) & 7]));
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[i]) : "r"(k), "r"(k2));
     }
   }
   uint32_t s = 0;

@@ -68,3 +68,18 @@ def test_stage_argument_checks(engine_lib):
     assert engine_lib.pa_ssc_sweep(None, 64, 10, 1, 0.4, 0, 1, 0, 1, None, None, None) == 1
     assert engine_lib.pa_msc_sweep(None, None, 64, 1, 1, 0.4, 0, 1, 0, 1, None, None, None) == 1
     assert engine_lib.pa_resample_plan(None, None, 0, 10, 10, 10, 0, 0.1, 0, 0, 1, 0, None, None, None, None, None) == 1
+
+
+def test_cli_argument_errors():
+    """The command-line driver rejects unknown options (usage, exit 1) and
+    non-option arguments (exit 1) like PAisingSSC.cu:399-404."""
+    import subprocess
+    exe = os.path.join(ROOT, "paising_gb300", "_lib", "paising")
+    if not os.path.exists(exe):
+        pytest.skip("CLI not built")
+    r = subprocess.run([exe, "-x"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage" in r.stdout
+    r = subprocess.run([exe, "extra"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Non-option argument extra" in r.stderr
+    r = subprocess.run([exe, "-c", "ssc", "-L", "12", "-o", "/tmp/pa_cli_bad_L"], capture_output=True, text=True)
+    assert r.returncode == 1 and "L % 8" in r.stderr

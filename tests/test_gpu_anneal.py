@@ -140,3 +140,26 @@ def test_native_runs_are_independent(cuda):
     bf = np.array([r[-1, 6] for r in rows])
     assert bf.std() < 2e-3
     assert att == pytest.approx(10 * 256 * sum(r[1:, 8].sum() for r in rows))
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_cli_reference_C1(cuda, tmp_path, coding):
+    """The command-line driver with the reference's flags writes the
+    reference's results file (same directory layout, 11 digits)."""
+    import os
+    import subprocess
+    from conftest import ROOT
+    exe = os.path.join(ROOT, "paising_gb300", "_lib", "paising")
+    r = subprocess.run([exe, "-R", "1000", "-t", "10", "-L", "16", "-s", "100", "-c", coding, "-m", "reference",
+                        "-w", "fp64", "-o", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Time per spin-flip" in r.stdout and "RNG initial seed: 100" in r.stdout
+    got = np.loadtxt(tmp_path / "PA_results_run_0.dat")
+    ref_name = f"ref/inj_{coding.upper()}_L16_R1000_t10_d0.005_s100.dat"
+    compare_rows(got, load_dat(ref_name), rtol=2e-10)
+    from conftest import GOLDEN
+    mine = open(tmp_path / "PA_results_run_0.dat").read().split("\n")
+    theirs = open(os.path.join(GOLDEN, ref_name)).read().split("\n")
+    for a, b in zip(mine[:50], theirs[:50]):  # beta, E/N and R print identically
+        fa, fb = a.split(), b.split()
+        assert fa[0] == fb[0] and fa[1] == fb[1] and fa[8] == fb[8]
