@@ -213,6 +213,24 @@ PA_API int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding,
                      double beta_prev, double beta, double e_ref, int weights, uint64_t seed, uint64_t iseq,
                      uint32_t* roff, uint32_t* offs, uint32_t* src, double* out, void* stream);
 
+/* No counterpart in the reference.  pa_resample_plan for callers that cannot
+ * allocate device memory -- e.g. a host framework that has reserved the
+ * device's memory for its own allocator, or a latency-critical loop that
+ * cannot afford the device-wide synchronisation cudaFree implies.  Same
+ * arguments, kernels and results as pa_resample_plan, but it calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch is a
+ * 32 KB array in the library's device memory, held by every GPU that loads
+ * the library until the process exits.  Limit: at most 262144 replica slots
+ * (SSC: R_prev; MSC: 32 * ceil(R_prev/32)); larger inputs return PA_ERR_ARG.
+ * All calls share that one array, so calls whose GPU work overlaps (other
+ * streams or host threads) race.  The first call on a device looks up the
+ * array's device address with that device current; make it before any
+ * stream capture. */
+PA_API int pa_resample_plan_noalloc(const int32_t* E, const uint8_t* active, int coding, int R_prev, int Rinit,
+                                    int Rcap, double beta_prev, double beta, double e_ref, int weights, uint64_t seed,
+                                    uint64_t iseq, uint32_t* roff, uint32_t* offs, uint32_t* src, double* out,
+                                    void* stream);
+
 /* resampleKer (PAisingSSC.cu:272-280): new[s] = old[src[s]], s < R_new. */
 PA_API int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_new, int8_t* new_spins, void* stream);
 
