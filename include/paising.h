@@ -70,6 +70,8 @@ typedef struct pa_config {
   int graph;         /* 1: each run is one CUDA graph launch; 0: host steps every temperature */
   int device;        /* CUDA device ordinal */
   double capacity;   /* replica buffer = ceil(capacity * R) + 256; 0 selects 1.25 */
+  int sweep_variant; /* MSC sweep kernel: 0 automatic, 1 one CTA per group, 2 or 4: a thread-block
+                        cluster of that many CTAs per group (needed for L > 128) */
 } pa_config;
 
 /* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */

@@ -49,7 +49,8 @@ class Config(ctypes.Structure):
     _fields_ = [("L", ctypes.c_int), ("R", ctypes.c_int), ("sweeps", ctypes.c_int), ("dbeta", ctypes.c_double),
                 ("beta_final", ctypes.c_double), ("runs", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("coding", ctypes.c_int), ("rng_mode", ctypes.c_int), ("weights", ctypes.c_int),
-                ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double)]
+                ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double),
+                ("sweep_variant", ctypes.c_int)]
 
 
 class Row(ctypes.Structure):
@@ -127,12 +128,15 @@ _W = {"fp32": WEIGHTS_FP32, "fp64": WEIGHTS_FP64, WEIGHTS_FP32: WEIGHTS_FP32, WE
 
 
 def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, seed=1, coding="ssc",
-                rng="native", weights="fp32", graph=True, device=0, capacity=1.25) -> Config:
+                rng="native", weights="fp32", graph=True, device=0, capacity=1.25, sweep_variant=0) -> Config:
+    """sweep_variant: CTAs per MSC group in the sweep kernel (0 automatic,
+    1 one CTA, 2 or 4 a thread-block cluster)."""
     c = Config()
     _check(lib().pa_config_init(ctypes.byref(c)))
     c.L, c.R, c.sweeps, c.dbeta, c.beta_final, c.runs = int(L), int(R), int(sweeps), float(dbeta), float(beta_final), int(runs)
     c.seed, c.coding, c.rng_mode, c.weights = int(seed), _CODING[coding], _RNG[rng], _W[weights]
     c.graph, c.device, c.capacity = int(bool(graph)), int(device), float(capacity)
+    c.sweep_variant = int(sweep_variant)
     return c
 
 

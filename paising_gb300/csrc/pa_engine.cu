@@ -104,6 +104,7 @@ struct pa_handle {
   int seq_runs = 1;  // sequential runs of a single population (reference stream, runs > 1)
   int max_steps = 0;
   int rblocks = 1;
+  int cs = 1;  // CTAs per MSC group in the sweep (1, or a cluster of 2 / 4)
   unsigned long long stream_seed = 0;  // key of the native sweep stream (seed of the first population)
   SweepLaunch sweep{};
   PopDev* d_pops = nullptr;
@@ -151,6 +152,11 @@ struct pa_handle {
     return e;
   }
 
+  cudaError_t sweep_launch(int energy_only) {
+    return cs > 1 ? launch_msc_cluster_sweep(cs, d_batch, rng_mode, energy_only, stream_seed, sweep, stream)
+                  : launch_sweep(d_batch, coding, rng_mode, energy_only, stream_seed, sweep, stream);
+  }
+
   cudaError_t enqueue_init() {
     cudaError_t e;
     const bool msc = coding == PA_CODING_MSC;
@@ -158,7 +164,7 @@ struct pa_handle {
     if ((e = launch(msc ? "msc_init" : "ssc_init", [&] { return launch_init(d_pops, npop, coding, stream); })) != cudaSuccess)
       return e;
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 1, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_energy" : "ssc_energy", [&] { return launch_sweep(d_batch, coding, rng_mode, 1, stream_seed, sweep, stream); });
+    e = launch(msc ? "msc_energy" : "ssc_energy", [&] { return sweep_launch(1); });
     if (e != cudaSuccess) return e;
     return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
   }
@@ -173,7 +179,7 @@ struct pa_handle {
     e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_pops, npop, coding, stream); });
     if (e != cudaSuccess) return e;
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 0, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sweep, stream); });
+    e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return sweep_launch(0); });
     if (e != cudaSuccess) return e;
     return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
   }
@@ -197,6 +203,10 @@ struct pa_handle {
 
 namespace {
 
+// CTAs per MSC group: the requested variant, or automatically one CTA when
+// the group (4 N bytes) fits its shared memory and a cluster of 2 otherwise.
+int msc_variant(int requested, int L) { return requested ? requested : (L > 128 ? 2 : 1); }
+
 int validate(const pa_config& c) {
   auto bad = [](const char* m) {
     pa::g_last_error = m;
@@ -208,9 +218,17 @@ int validate(const pa_config& c) {
   if (c.R < 1 || c.sweeps < 0 || c.runs < 1 || !(c.dbeta > 0) || !(c.beta_final > 0))
     return bad("R, sweeps, runs, dbeta, beta_final out of range");
   if (c.capacity != 0 && c.capacity < 1.0) return bad("capacity must be >= 1");
+  if (c.sweep_variant != 0 && c.sweep_variant != 1 && c.sweep_variant != 2 && c.sweep_variant != 4)
+    return bad("sweep_variant must be 0, 1, 2 or 4");
+  if (c.coding == PA_CODING_SSC && c.sweep_variant > 1) return bad("cluster sweeps exist for MSC only");
   SweepGeom g;
-  if (c.coding == PA_CODING_MSC ? !msc_geom(c.L, &g) : !ssc_geom(c.L, &g))
-    return bad(c.coding == PA_CODING_MSC ? "MSC needs even L in [8, 128]" : "SSC needs L % 8 == 0, 8 <= L <= 256");
+  if (c.coding == PA_CODING_MSC) {
+    const int cs = msc_variant(c.sweep_variant, c.L);
+    const bool ok = cs == 1 ? msc_geom(c.L, &g) : msc_cluster_geom(c.L, cs, msc_cluster_threads(cs), &g);
+    if (!ok) return bad("MSC needs even L in [8, 128] (one CTA per group) or L % 4 == 0 up to 256 (clusters)");
+  } else if (!ssc_geom(c.L, &g)) {
+    return bad("SSC needs L % 8 == 0, 8 <= L <= 256");
+  }
   if ((int)schedule(c.dbeta, c.beta_final).size() > kNBmax - 1) {
     pa::g_last_error = "number of temperature steps exceeds nBmax=10000";
     return PA_ERR_TOO_MANY_STEPS;
@@ -239,14 +257,22 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   cudaError_t e = cudaSetDevice(c0.device);
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
 
+  // one sweep kernel serves the whole batch: clusters if any population needs them
+  H->cs = 1;
+  if (H->coding == PA_CODING_MSC)
+    for (const auto& c : cfgs) H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
   H->pops.resize(cfgs.size());
   for (size_t k = 0; k < cfgs.size(); ++k) {
     PopHost& P = H->pops[k];
     P.cfg = cfgs[k];
     P.user_index = (int)k;
     if (P.cfg.capacity <= 0) P.cfg.capacity = 1.25;
-    if (P.cfg.coding == PA_CODING_MSC) msc_geom(P.cfg.L, &P.geom);
-    else ssc_geom(P.cfg.L, &P.geom);
+    bool okg;
+    if (P.cfg.coding == PA_CODING_SSC) okg = ssc_geom(P.cfg.L, &P.geom);
+    else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom);
+    else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
+    if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +
+                                          std::to_string(H->cs) + " CTAs");
     P.betas = schedule(P.cfg.dbeta, P.cfg.beta_final);
     P.nsteps = (int)P.betas.size() - 1;
     P.thr.assign(P.betas.size() * kThrPerStep, 0u);
@@ -331,7 +357,8 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   }
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   H->rblocks = res_blocks(max_units);
-  chk(sweep_setup(H->coding, H->rng_mode, max_smem, &H->sweep));
+  chk(H->cs > 1 ? msc_cluster_setup(H->cs, H->rng_mode, max_smem, &H->sweep)
+                : sweep_setup(H->coding, H->rng_mode, max_smem, &H->sweep));
   chk(B.alloc(&H->d_pops, (size_t)H->npop));
   chk(B.alloc(&H->d_batch, 1));
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e));

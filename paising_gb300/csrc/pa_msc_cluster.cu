@@ -1,0 +1,338 @@
+// pa_msc_cluster.cu -- multi-spin-coded sweep of one group by a thread-block
+// cluster, for lattices whose two sublattices (4 N bytes per group) do not
+// fit one CTA's shared memory (L = 256: 256 KB > 227 KB).
+//
+// CTA r of a cluster of CS holds rows [r L/CS, (r+1) L/CS) of both
+// sublattices in its shared memory, each stripe framed by two halo rows.
+// During a half-sweep only one sublattice changes, so after the cluster
+// barrier that ends the previous half-sweep every CTA copies the rows of the
+// other sublattice just above and below its stripe out of the neighbouring
+// CTAs' shared memory (distributed shared memory) into its halo rows; the
+// update itself then reads local shared memory only.  Random draws,
+// decisions, energies and statistics are the ones of msc_sweep_kernel
+// (pa_msc.cu): with the reference stream both give identical lattices
+// (every draw is keyed by global site coordinates).
+#include <cooperative_groups.h>
+
+#include <climits>
+
+#include "pa_kernels.h"
+#include "pa_msc_core.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pa {
+
+using namespace msc;
+
+template <int MODE, int CS, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS)
+    msc_sweep_cluster_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
+  extern __shared__ __align__(16) uint32_t lat[];  // stripe of A (LR*Wr words), then stripe of B
+  __shared__ int s_unit, s_pop;
+  __shared__ int s_cntE[kMsb], s_cntM[kMsb];
+  __shared__ uint2 s_dig[kMsb];
+  __shared__ UnitParams P;
+  __shared__ BitStats stats;  // used by rank 0
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int prev = (rank + CS - 1) % CS, next = (rank + 1) % CS;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int total = b->unit_prefix[b->npop];
+  const PhiloxKeys keys(stream_seed);
+  int cur = -1;
+  int tx = 0, rsub = 0, txl = 0, txr = 0;
+  bool worker = false;
+  if (tid < kMsb) stats.reset(tid);
+
+  for (;;) {
+    cluster.sync();  // the previous group is finished everywhere (including remote reads)
+    if (rank == 0 && tid == 0) {
+      const int u = (int)atomicAdd(&b->work_next, 1u);
+      int loc = 0;
+      const int p = u < total ? queue_pop(b, u, &loc) : -1;
+      for (int r = 0; r < CS; ++r) {
+        *cluster.map_shared_rank(&s_pop, r) = p;
+        *cluster.map_shared_rank(&s_unit, r) = loc;
+      }
+    }
+    cluster.sync();
+    const int p = s_pop, gi = s_unit;
+    if (p < 0) break;  // every CTA of the cluster leaves after the same barrier
+    if (tid < kMsb) { s_cntE[tid] = 0; s_cntM[tid] = 0; }
+    if (p != cur) {  // cluster-uniform
+      if (rank == 0 && tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
+      if (tid == 0) {
+        const PopDev* st = b->pops + p;
+        P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.Wr = st->Wr; P.rpp = st->rpp; P.npass = st->npass;
+        P.kconst = st->kconst;
+        P.step = st->step;
+        P.sweeps = energy_only ? 0 : st->sweeps;
+        P.nbatch = (st->npass + kKB - 1) / kKB;
+        P.tag = kTagMscSweep | (uint32_t)st->pop_id;
+        P.T4 = st->thr[(size_t)st->step * kThrPerStep + 10];
+        P.T8 = st->thr[(size_t)st->step * kThrPerStep + 11];
+        P.seed = st->seed;
+        const int rg_prev = (st->R_prev + kMsb - 1) / kMsb;
+        P.iseq = st->iseq + (st->step > 0 ? (unsigned long long)rg_prev * kMsb : 0ull);
+        P.words = (uint32_t*)st->spins[st->parity];
+        P.act = st->active[st->parity];
+        P.E = st->E;
+        P.M = st->M;
+      }
+      __syncthreads();
+      cur = p;
+      const int Wr = P.Wr;
+      worker = tid < Wr * P.rpp;
+      tx = worker ? tid % Wr : 0;
+      rsub = worker ? tid / Wr : 0;
+      txl = (tx == 0 ? Wr - 1 : tx - 1);
+      txr = (tx + 1 == Wr ? 0 : tx + 1);
+      if (tid < kMsb) {
+        const uint32_t d4 = 0u - ((P.T4 >> (31 - tid)) & 1u), d8 = 0u - ((P.T8 >> (31 - tid)) & 1u);
+        s_dig[tid] = make_uint2(d8, d4 ^ d8);
+      }
+    }
+    // stripe of a sublattice in shared memory: halo row, LR rows, halo row
+    const int h = P.h, Wr = P.Wr, L = P.L, LR = L / CS, SW = LR * Wr, SH = SW + 2 * Wr;
+    const int row0 = rank * LR;
+    uint32_t* words = P.words;
+    {  // load this CTA's stripe of both sublattices
+      const uint4* ga = (const uint4*)(words + (size_t)gi * P.N + (size_t)row0 * Wr);
+      const uint4* gb = (const uint4*)(words + (size_t)gi * P.N + h + (size_t)row0 * Wr);
+      uint4* la = (uint4*)(lat + Wr);
+      uint4* lb = (uint4*)(lat + SH + Wr);
+      for (int v = tid; v < (SW >> 2); v += blockDim.x) {
+        la[v] = ga[v];
+        lb[v] = gb[v];
+      }
+    }
+    cluster.sync();
+    // halo rows of sublattice X (0: A, 1: B): the last row of the previous
+    // stripe and the first row of the next one
+    auto fetch_halo = [&](int X) {
+      uint32_t* own = lat + X * SH;
+      const uint32_t* up = cluster.map_shared_rank(own, prev);
+      const uint32_t* dn = cluster.map_shared_rank(own, next);
+      for (int v = tid; v < 2 * Wr; v += blockDim.x)
+        own[v < Wr ? v : SW + v] = v < Wr ? up[SW + v] : dn[v];
+    };
+
+    const int sweeps = P.sweeps;
+    for (int sw = 0; sw < sweeps; ++sw) {
+#pragma unroll 1
+      for (int hf = 0; hf < 2; ++hf) {
+        fetch_halo(hf ? 0 : 1);
+        __syncthreads();
+        uint32_t* self = lat + (hf ? SH : 0) + Wr;
+        const uint32_t* oth = lat + (hf ? 0 : SH) + Wr;
+        const int rpp = P.rpp, npass = P.npass;
+        if (MODE == kRefCoords) {
+#pragma unroll 1
+          for (int pass = 0; pass < npass; ++pass) {
+            const int lr = rsub + pass * rpp;
+            const bool valid = worker && lr < LR;
+            const int lrc = valid ? lr : 0, ty = row0 + lrc;
+            const int row = lrc * Wr, idx = ty * Wr + tx;
+            const bool left = (hf == 0) == ((ty & 1) == 0);
+            const uint32_t s = self[row + tx];
+            const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[row + tx];
+            const uint32_t n3 = oth[row - Wr + tx], n4 = oth[row + Wr + tx];
+            uint32_t s0, s1, s2;
+            adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
+            const int t = idx & (kRefThreads - 1), k = idx >> 7;
+            const int K = P.kconst ? P.kconst : (t < h ? (h - t + kRefThreads - 1) / kRefThreads : 0);
+            const unsigned long long sub = P.iseq + (unsigned long long)t + (unsigned long long)kRefThreads * gi;
+            uint32_t ran = ref_word(P.seed, sub, (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k);
+            const uint32_t T4 = P.T4, T8 = P.T8;
+            uint32_t c4 = 0, c8 = 0;
+#pragma unroll 8
+            for (int i = 0; i < kMsb; ++i) {
+              c4 |= (ran < T4 ? 1u : 0u) << i;
+              c8 |= (ran < T8 ? 1u : 0u) << i;
+              ran = kLcgA * ran + kLcgC;
+            }
+            const uint32_t hi = s1 | s2;
+            const uint32_t acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
+            if (valid) self[row + tx] = s ^ acc;
+          }
+        } else {
+          const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+#pragma unroll 1
+          for (int p0 = 0; p0 < npass; p0 += kKB) {
+            uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+            int ix[kKB];
+#pragma unroll
+            for (int k = 0; k < kKB; ++k) {
+              const int pass = p0 + k;
+              const int lr = rsub + pass * rpp;
+              const bool valid = worker && pass < npass && lr < LR;
+              const int lrc = valid ? lr : 0, ty = row0 + lrc;
+              const int row = lrc * Wr;
+              const bool left = (hf == 0) == ((ty & 1) == 0);
+              const uint32_t s = self[row + tx];
+              const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[row + tx];
+              const uint32_t n3 = oth[row - Wr + tx], n4 = oth[row + Wr + tx];
+              uint32_t s0, s1, s2;
+              adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
+              av[k] = s0;
+              ac[k] = s1 | s2;
+              un[k] = valid ? ~(s1 | s2) : 0u;
+              ix[k] = valid ? row + tx : -1;
+              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)(ty * Wr + tx);
+            }
+            const uint32_t chain =
+                (((uint32_t)gi * CS + (uint32_t)rank) * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
+            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig);
+#pragma unroll
+            for (int k = 0; k < kKB; ++k)
+              if (ix[k] >= 0) self[ix[k]] ^= ac[k];
+          }
+        }
+        cluster.sync();
+      }
+    }
+
+    // energy and magnetisation of this stripe: left and up bond of every A
+    // and B site (PAisingMSC.cu:272-294); the up neighbours of the last row
+    // are the first row of the next stripe, fetched into the lower halos.
+    fetch_halo(0);
+    fetch_halo(1);
+    __syncthreads();
+    int cE = 0, cM = 0;
+    {
+      const uint32_t* A = lat + Wr;
+      const uint32_t* Bs = lat + SH + Wr;
+      const int rpp = P.rpp, npass = P.npass;
+      for (int pass = 0; pass < npass; ++pass) {
+        const int lr = rsub + pass * rpp;
+        const bool valid = worker && lr < LR;
+        uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
+        if (valid) {
+          const int ty = row0 + lr, row = lr * Wr;
+          sA = A[row + tx];
+          sB = Bs[row + tx];
+          uint32_t Ai2, Bi2;
+          if (ty & 1) { Ai2 = sB; Bi2 = A[row + txl]; }
+          else { Ai2 = Bs[row + txl]; Bi2 = sA; }
+          const uint32_t Ai4 = Bs[row + Wr + tx], Bi4 = A[row + Wr + tx];
+          adder4(sA ^ Ai2, sA ^ Ai4, sB ^ Bi2, sB ^ Bi4, s0, s1, s2);
+        }
+#pragma unroll 4
+        for (int k = 0; k < kMsb; ++k) {
+          const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
+                        4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
+          const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
+          if (lane == k) { cE += e; cM += m; }
+        }
+      }
+    }
+    atomicAdd(&s_cntE[lane], cE);
+    atomicAdd(&s_cntM[lane], cM);
+    {  // write the stripe back
+      uint4* ga = (uint4*)(words + (size_t)gi * P.N + (size_t)row0 * Wr);
+      uint4* gb = (uint4*)(words + (size_t)gi * P.N + h + (size_t)row0 * Wr);
+      const uint4* la = (const uint4*)(lat + Wr);
+      const uint4* lb = (const uint4*)(lat + SH + Wr);
+      for (int v = tid; v < (SW >> 2); v += blockDim.x) {
+        ga[v] = la[v];
+        gb[v] = lb[v];
+      }
+    }
+    cluster.sync();  // all stripes' counts are complete
+    if (rank == 0 && tid < kMsb) {
+      int ce = 0, cm = 0;
+      for (int r = 0; r < CS; ++r) {
+        ce += *cluster.map_shared_rank(&s_cntE[tid], r);
+        cm += *cluster.map_shared_rank(&s_cntM[tid], r);
+      }
+      const int N = P.N;
+      const int E = 2 * ce - 2 * N, Mg = 2 * cm - N;
+      P.E[gi * kMsb + tid] = E;
+      P.M[gi * kMsb + tid] = Mg;
+      if (P.act[gi * kMsb + tid]) stats.add(tid, E, Mg);
+    }
+  }
+  if (rank == 0 && tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
+}
+
+// -------------------------------------------------------------- geometry
+bool msc_cluster_geom(int L, int cs, int threads, SweepGeom* g) {
+  if (L < 8 || L % 2 != 0 || L > 256 || (cs != 2 && cs != 4) || L % cs != 0) return false;
+  const int LR = L / cs;
+  if (LR < 2) return false;
+  g->L = L;
+  g->N = L * L;
+  g->half = g->N / 2;
+  g->Wr = L / 2;
+  if (g->Wr > threads) return false;
+  int best = 1;
+  for (int r = 1; r <= LR; ++r)
+    if (LR % r == 0 && g->Wr * r <= threads) best = r;
+  g->rpp = best;
+  g->T = g->Wr * g->rpp;
+  g->npass = LR / g->rpp;
+  g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
+  g->smem = 2 * (LR + 2) * g->Wr * 4;  // both sublattice stripes with their halo rows
+  // stripes are moved with 16-byte vectors: rows start on a 4-word boundary
+  return g->Wr % 4 == 0;
+}
+
+// -------------------------------------------------------------- launchers
+template <int MODE, int CS, int THREADS>
+static cudaError_t cluster_launch(BatchDev* b, int energy_only, unsigned long long seed, const SweepLaunch* sl,
+                                  SweepLaunch* setup, cudaStream_t s) {
+  auto fn = msc_sweep_cluster_kernel<MODE, CS, THREADS>;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.blockDim = dim3(THREADS);
+  cfg.stream = s;
+  if (setup) {  // persistent grid: as many clusters as can be resident
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, setup->smem);
+    if (e != cudaSuccess) return e;
+    cfg.gridDim = dim3(CS);
+    cfg.dynamicSmemBytes = setup->smem;
+    int nclusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg);
+    if (e != cudaSuccess) return e;
+    if (nclusters < 1) return cudaErrorInvalidConfiguration;
+    setup->grid = nclusters * CS;
+    setup->block = THREADS;
+    return cudaSuccess;
+  }
+  cfg.gridDim = dim3(sl->grid);
+  cfg.dynamicSmemBytes = sl->smem;
+  return cudaLaunchKernelEx(&cfg, fn, b, energy_only, seed);
+}
+
+template <int CS, int THREADS>
+static cudaError_t cluster_dispatch(int rng_mode, BatchDev* b, int energy_only, unsigned long long seed,
+                                    const SweepLaunch* sl, SweepLaunch* setup, cudaStream_t s) {
+  return rng_mode == kRefCoords ? cluster_launch<kRefCoords, CS, THREADS>(b, energy_only, seed, sl, setup, s)
+                                : cluster_launch<kNative, CS, THREADS>(b, energy_only, seed, sl, setup, s);
+}
+
+int msc_cluster_threads(int cs) { return cs == 2 ? 1024 : 512; }
+
+cudaError_t msc_cluster_setup(int cs, int rng_mode, int smem, SweepLaunch* out) {
+  out->smem = smem;
+  if (cs == 2) return cluster_dispatch<2, 1024>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  if (cs == 4) return cluster_dispatch<4, 512>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_msc_cluster_sweep(int cs, BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+                                     const SweepLaunch& sl, cudaStream_t s) {
+  if (cs == 2) return cluster_dispatch<2, 1024>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+  if (cs == 4) return cluster_dispatch<4, 512>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace pa

@@ -1,0 +1,173 @@
+// pa_msc_core.cuh -- device building blocks of the multi-spin-coded sweeps
+// (single-CTA and cluster variants): the bitsliced neighbour adder, the
+// digit-serial acceptance for 32 replicas per word, per-population parameters
+// and per-bit statistics.
+#pragma once
+
+#include <climits>
+
+#include "pa_device.cuh"
+
+namespace pa {
+namespace msc {
+
+constexpr uint32_t kLcgA = 1664525u;     // PAisingMSC.cu:53
+constexpr uint32_t kLcgC = 1013904223u;  // PAisingMSC.cu:54
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kKB = 4;  // word-sites per thread decided together (native stream)
+
+// Bitsliced count of anti-parallel neighbours (4 inputs -> 3 bit planes),
+// the adder of PAisingMSC.cu:212-218.
+__device__ __forceinline__ void adder4(uint32_t I1, uint32_t I2, uint32_t I3, uint32_t I4, uint32_t& s0,
+                                       uint32_t& s1, uint32_t& s2) {
+  const uint32_t x12 = I1 ^ I2, x34 = I3 ^ I4, a12 = I1 & I2, a34 = I3 & I4;
+  s0 = x12 ^ x34;
+  s1 = (x12 & x34) ^ a12 ^ a34;
+  s2 = a12 & a34;
+}
+
+// One binary digit of the comparison U < T/2^32 done for 32 bits at once:
+// U's digit j is bit i of the random word u for replica bit i, T's digit j
+// is selected per bit from T4 (bits in s0: one anti-parallel neighbour,
+// dE = 4) or T8 (no anti-parallel neighbour, dE = 8).  dg = (D8_j, D4_j ^ D8_j)
+// with D_j = all ones iff digit j of the threshold is 1.  Bits decided at this
+// digit leave `und` (a subtraction, since they are a subset of it); those
+// decided "less" enter `lt`.
+__device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, uint32_t& und, uint32_t& lt) {
+  const uint32_t p = (s0 & dg.y) ^ dg.x;
+  const uint32_t dec = und & (p ^ u);
+  lt |= dec & p;
+  und -= dec;
+}
+
+// Remaining digits (from digit 4 on) of one 32-bit comparison word, drawing
+// fresh Philox blocks (counter (c0, c1 | sub0 + c, step, tag)) until every
+// bit of every lane is decided.  Returns the bits decided "less".
+__device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub0,
+                                                  uint32_t step, uint32_t tag, const PhiloxKeys& K,
+                                                  const uint2* dig) {
+  uint32_t lt = 0;
+#pragma unroll 1
+  for (int c = 0; c < 7; ++c) {
+    if (!__any_sync(kFull, und != 0u)) break;
+    const U4 r = philox10k(c0, c1 | (sub0 + c), step, tag, K);
+    digit_step(r.x, am, dig[4 + 4 * c], und, lt);
+    digit_step(r.y, am, dig[5 + 4 * c], und, lt);
+    digit_step(r.z, am, dig[6 + 4 * c], und, lt);
+    digit_step(r.w, am, dig[7 + 4 * c], und, lt);
+  }
+  return lt;
+}
+
+// Exact Metropolis decisions U < T/2^32 for kKB word-sites of one thread.
+// Head: digits 0..3 of every site come from the site's own Philox block;
+// after them only ~1/16 of the bits are undecided.  Tail: those sparse bits
+// of the kKB sites are merged into one word, site k's masks rotated by rot_k
+// so that every (site, replica) pair gets its own bit position -- hence its
+// own fresh digits -- and the remaining digits are drawn once for all sites.
+// A site whose bits find no free rotation is finished on its own.
+//   a[k]   : bits with one anti-parallel neighbour (threshold T4), else T8
+//   und[k] : bits needing a random decision (consumed)
+//   acc[k] : accepted bits (in: outright accepts; out: all accepts)
+__device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t (&und)[kKB], uint32_t (&acc)[kKB],
+                                              const uint32_t (&site)[kKB], uint32_t chain_c0, uint32_t c1,
+                                              uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig) {
+  // independent Philox chains of the kKB sites, interleaved by the compiler
+  const uint2 d0 = dig[0], d1 = dig[1], d2 = dig[2], d3 = dig[3];
+#pragma unroll
+  for (int k = 0; k < kKB; ++k) {
+    const U4 r = philox10k(site[k], c1, step, tag, K);
+    digit_step(r.x, a[k], d0, und[k], acc[k]);
+    digit_step(r.y, a[k], d1, und[k], acc[k]);
+    digit_step(r.z, a[k], d2, und[k], acc[k]);
+    digit_step(r.w, a[k], d3, und[k], acc[k]);
+  }
+  uint32_t m = und[0], am = a[0] & und[0];
+  uint32_t rot[kKB];
+  rot[0] = 0;
+  uint32_t ovf = 0;
+#pragma unroll
+  for (int k = 1; k < kKB; ++k) {
+    uint32_t r = 0;
+    while (r < 32u && (m & __funnelshift_l(und[k], und[k], r))) ++r;
+    rot[k] = r;
+    if (r < 32u) {
+      m |= __funnelshift_l(und[k], und[k], r);
+      am |= __funnelshift_l(a[k] & und[k], a[k] & und[k], r);
+    } else {
+      ovf |= 1u << k;
+    }
+  }
+  const uint32_t lt = finish_digits(m, am, chain_c0, c1, 1u, step, tag, K, dig);
+  acc[0] |= lt & und[0];
+#pragma unroll
+  for (int k = 1; k < kKB; ++k) {
+    if (!(ovf >> k & 1u)) acc[k] |= __funnelshift_r(lt, lt, rot[k]) & und[k];
+    if (__any_sync(kFull, ovf >> k & 1u))
+      acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, step, tag, K, dig);
+  }
+}
+
+// Per-population parameters of the group a CTA is annealing.  They live in
+// shared memory and are read where used, which keeps the hot loops' register
+// footprint independent of how many populations the batch holds.
+struct UnitParams {
+  int L, N, h, Wr, rpp, npass, kconst, step, sweeps, nbatch;
+  uint32_t tag, T4, T8;
+  unsigned long long seed, iseq;
+  uint32_t* words;
+  const uint8_t* act;
+  int32_t* E;
+  int32_t* M;
+};
+
+// Statistics of the groups a CTA annealed for one population, accumulated in
+// shared memory by lane k of warp 0 for replica bit k (registers stay free
+// for the sweep); flushed to the population when the CTA moves on.
+struct BitStats {
+  long long sE[kMsb], sE2[kMsb], sM[kMsb], sM2[kMsb];
+  unsigned long long m4lo[kMsb], m4hi[kMsb];
+  int emin[kMsb];
+  __device__ void reset(int k) {
+    sE[k] = sE2[k] = sM[k] = sM2[k] = 0;
+    m4lo[k] = m4hi[k] = 0;
+    emin[k] = INT_MAX;
+  }
+  __device__ void add(int k, int E, int Mg) {
+    const long long am = Mg < 0 ? -(long long)Mg : (long long)Mg;
+    sE[k] += E;
+    sE2[k] += (long long)E * E;
+    sM[k] += am;
+    sM2[k] += am * am;
+    unsigned long long lo, hi;
+    m4_of(Mg, lo, hi);
+    U128 m{m4lo[k], m4hi[k]};
+    u128_add(m, lo, hi);
+    m4lo[k] = m.lo;
+    m4hi[k] = m.hi;
+    emin[k] = E < emin[k] ? E : emin[k];
+  }
+  // warp 0 only, lane k = bit k
+  __device__ void flush(PopDev* st, int k) {
+    const long long e = warp_sum(sE[k]), e2 = warp_sum(sE2[k]), m = warp_sum(sM[k]), m2 = warp_sum(sM2[k]);
+    const int mn = warp_min(emin[k]);
+    U128 q{m4lo[k], m4hi[k]};
+    for (int o = 16; o > 0; o >>= 1) {  // 128-bit sum across the warp, carries into hi
+      const unsigned long long lo = __shfl_xor_sync(kFull, q.lo, o);
+      const unsigned long long hi = __shfl_xor_sync(kFull, q.hi, o);
+      u128_add(q, lo, hi);
+    }
+    if (k == 0 && mn != INT_MAX) {
+      atomicAdd((unsigned long long*)&st->sE, (unsigned long long)e);
+      atomicAdd((unsigned long long*)&st->sE2, (unsigned long long)e2);
+      atomicAdd((unsigned long long*)&st->sM, (unsigned long long)m);
+      atomicAdd((unsigned long long*)&st->sM2, (unsigned long long)m2);
+      u128_atomic_add(&st->sM4lo, &st->sM4hi, q.lo, q.hi);
+      atomicMin(&st->Emin_acc, mn);
+    }
+    reset(k);
+  }
+};
+
+}  // namespace msc
+}  // namespace pa
