@@ -1,0 +1,179 @@
+"""Reproducible studies on the GPU engine (run on a CUDA host):
+
+    python -m paising_gb300.studies precision   [--out FILE]
+    python -m paising_gb300.studies batch       [--out FILE]
+    python -m paising_gb300.studies large       [--out FILE]
+
+precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
+    sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
+    resampling weights (FP64 lnQ) against all-FP64 weights; errors of betaF/N,
+    E/N and C/N against the exact finite-lattice solution (Kaufman) at every
+    beta.  The exact values come from the formula in closed form (FP64),
+    evaluated inside this module.
+batch: 64 populations with L drawn from {16,32,48,64,96,128}, R uniform in
+    [1000, 20000], dbeta from {0.0025, 0.005, 0.01}, beta_final 1, 20 sweeps
+    (seed 2026), annealed as one batch and as 64 sequential plain runs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import sys
+import time
+
+import numpy as np
+
+import paising_gb300 as pa
+
+
+# ------------------------------------------------ exact solution (Kaufman)
+def _log2cosh(x):
+    x = abs(x)
+    return x + math.log1p(math.exp(-2 * x))
+
+
+def _log2sinh(x):
+    x = abs(x)
+    if x < 1e-3:
+        return math.log(2 * x) + math.log1p(x * x / 6)
+    return x + math.log(-math.expm1(-2 * x))
+
+
+def kaufman_lnz(L: int, K: float) -> float:
+    """ln Z of the L x L periodic Ising model at coupling K (B. Kaufman,
+    Phys. Rev. 76, 1232 (1949); form of Ferdinand and Fisher, Phys. Rev. 185,
+    832 (1969)), evaluated in the log domain."""
+    if K <= 0:
+        return L * L * math.log(2.0)
+    c2, s2 = math.cosh(2 * K), math.sinh(2 * K)
+    base = c2 * c2 / s2
+    l = [0.0, 0.0, 0.0, 0.0]
+    sign4 = 1
+    for r in range(L):
+        for par in (0, 1):
+            k = 2 * r + par
+            g = 2 * K + math.log(math.tanh(K)) if k == 0 else math.acosh(base - math.cos(math.pi * k / L))
+            x = 0.5 * L * g
+            ic, is_ = (0, 1) if par else (2, 3)
+            l[ic] += _log2cosh(x)
+            if x == 0:
+                l[is_] = -math.inf
+            else:
+                l[is_] += _log2sinh(x)
+            if is_ == 3 and x < 0:
+                sign4 = -sign4
+    mx = max(v for v in l if math.isfinite(v))
+    s = sum(math.exp(v - mx) * (sign4 if i == 3 else 1) for i, v in enumerate(l) if math.isfinite(v))
+    return -math.log(2) + 0.5 * L * L * math.log(2 * s2) + mx + math.log(s)
+
+
+def kaufman(L: int, beta: float):
+    """(betaF/N, E/N, C/N) by central differences of ln Z."""
+    N = L * L
+    lz = kaufman_lnz(L, beta)
+    if beta <= 0:
+        return -lz / N, 0.0, 0.0
+    h = 1e-4
+    lp, lm = kaufman_lnz(L, beta + h), kaufman_lnz(L, beta - h)
+    lpp, lmm = kaufman_lnz(L, beta + 2 * h), kaufman_lnz(L, beta - 2 * h)
+    d1 = (-lpp + 8 * lp - 8 * lm + lmm) / (12 * h)
+    d2 = (-lpp + 16 * lp - 30 * lz + 16 * lm - lmm) / (12 * h * h)
+    return -lz / N, -d1 / N, beta * beta * d2 / N
+
+
+# ----------------------------------------------------------------- studies
+def precision(seed: int = 31) -> dict:
+    out = {"workload": "MSC, 100 sweeps, dbeta=0.005, beta 0->1, native stream", "cases": []}
+    for L, R in ((32, 1_000_000), (64, 100_000), (128, 100_000)):
+        case = {"L": L, "R": R}
+        ex = None
+        for w in ("fp32", "fp64"):
+            with pa.Engine(L=L, R=R, sweeps=100, dbeta=0.005, coding="msc", weights=w, seed=seed) as e:
+                e.run()
+                rows = e.rows(0)
+                ms, att = e.timing()
+            if ex is None:
+                ex = np.array([kaufman(L, b) for b in rows[:, 0]])
+            case[w] = {
+                "max_abs_err_betaF_per_site": float(np.max(np.abs(rows[:, 6] - ex[:, 0]))),
+                "max_abs_err_E_per_site": float(np.max(np.abs(rows[1:, 1] - ex[1:, 1]))),
+                "max_abs_err_C_per_site": float(np.max(np.abs(rows[1:, 2] - ex[1:, 2]))),
+                "final_betaF_per_site": float(rows[-1, 6]),
+                "seconds": ms / 1e3, "attempts_per_ns": att / (ms * 1e6),
+                "lnQ": rows[:, 9].tolist(),
+            }
+        d = np.abs(np.array(case["fp32"]["lnQ"]) - np.array(case["fp64"]["lnQ"]))
+        case["max_abs_lnQ_fp32_minus_fp64"] = float(d.max())
+        for w in ("fp32", "fp64"):
+            del case[w]["lnQ"]
+        out["cases"].append(case)
+        print(json.dumps(case), flush=True)
+    return out
+
+
+def batch(seed: int = 2026) -> dict:
+    rng = np.random.default_rng(seed)
+    pops = [dict(L=int(rng.choice([16, 32, 48, 64, 96, 128])), R=int(rng.integers(1000, 20001)),
+                 dbeta=float(rng.choice([0.0025, 0.005, 0.01])), sweeps=20, seed=seed + k) for k in range(64)]
+    res = {"populations": pops}
+    with pa.Engine.batch(pops, coding="msc") as e:
+        e.run()  # warm (graph upload)
+        t0 = time.perf_counter()
+        e.run()
+        wall = time.perf_counter() - t0
+        ms, att = e.timing()
+    res["batched"] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6)}
+    tot_ms = tot_att = 0.0
+    t0 = time.perf_counter()
+    for p in pops:
+        with pa.Engine(coding="msc", **p) as e:
+            e.run()
+            m, a = e.timing()
+            tot_ms += m
+            tot_att += a
+    wall = time.perf_counter() - t0
+    res["sequential_plain"] = {"device_s": tot_ms / 1e3, "wall_s_including_setup": wall,
+                               "attempts_per_ns": tot_att / (tot_ms * 1e6)}
+    res["speedup_device"] = res["batched"]["attempts_per_ns"] / res["sequential_plain"]["attempts_per_ns"]
+    print(json.dumps({k: v for k, v in res.items() if k != "populations"}), flush=True)
+    return res
+
+
+def large(seed: int = 256, variants=(2, 4), sweeps: int = 50) -> dict:
+    """L=256, R=131072 MSC (one group: 256 KB, swept by a thread-block
+    cluster), dbeta=0.005, beta 0->1: throughput per cluster size, the
+    per-kernel split of one run timed launch by launch, and betaF/N against
+    the exact solution."""
+    L, R = 256, 131072
+    res = {"workload": f"MSC L={L} R={R} {sweeps} sweeps dbeta=0.005 beta 0->1, native stream, FP32 weights",
+           "variants": {}}
+    for v in variants:
+        with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=0.005, coding="msc", seed=seed, sweep_variant=v) as e:
+            e.run()
+            rows = e.rows(0)
+            ms, att = e.timing()
+            prof = e.profile()
+        ex = np.array([kaufman(L, b) for b in rows[:, 0]])
+        r = {"seconds": ms / 1e3, "attempts_per_ns": att / (ms * 1e6),
+             "max_abs_err_betaF_per_site": float(np.max(np.abs(rows[:, 6] - ex[:, 0]))),
+             "max_abs_err_E_per_site": float(np.max(np.abs(rows[1:, 1] - ex[1:, 1]))),
+             "kernels_ms": {k: [n, t] for k, (n, t) in prof.items()}}
+        res["variants"][str(v)] = r
+        print(json.dumps({"variant": v, **r}), flush=True)
+    return res
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("study", choices=["precision", "batch", "large"])
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    r = {"precision": precision, "batch": batch, "large": large}[a.study]()
+    if a.out:
+        json.dump(r, open(a.out, "w"), indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
