@@ -72,6 +72,8 @@ typedef struct pa_config {
   double capacity;   /* replica buffer = ceil(capacity * R) + 256; 0 selects 1.25 */
   int sweep_variant; /* MSC sweep kernel: 0 automatic, 1 one CTA per group, 2 or 4: a thread-block
                         cluster of that many CTAs per group (needed for L > 128) */
+  int tile_groups;   /* MSC groups stacked into one work unit of the one-CTA sweep: 0 automatic,
+                        1, 2, 4 or 8 (more than 1 needs L % 4 == 0 and at most 44 KB per tile) */
 } pa_config;
 
 /* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */
@@ -106,6 +108,17 @@ PA_API int pa_create_batch(const pa_config* cfgs, int n, pa_handle** out);
  * population-annealing loop of main() (PAisingSSC.cu:481-664,
  * PAisingMSC.cu:640-814). */
 PA_API int pa_run(pa_handle* h);
+
+/* Autotuner of the MSC one-CTA sweep: for every lattice size of the handle,
+ * times one sweep launch of its populations (freshly initialised, at the
+ * first temperature) with 1, 2, 4 and 8 groups stacked per work unit where
+ * valid, keeps the fastest per spin-flip attempt and rebuilds the launch plan
+ * (and graph).  Must precede the first pa_run; the runs that follow start
+ * from the configured state exactly as without it.  tiles[k] (k < n, may be
+ * null with n = 0) receives population k's choice.  Results are unchanged by
+ * the choice under the reference stream.  No counterpart in the reference,
+ * whose launch shapes are compile-time constants. */
+PA_API int pa_autotune(pa_handle* h, int* tiles, int n);
 
 /* Number of result sets a pa_run produces: one per population per
  * sequential run (PA_results_run_<set>.dat). */

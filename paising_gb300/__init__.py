@@ -50,7 +50,7 @@ class Config(ctypes.Structure):
                 ("beta_final", ctypes.c_double), ("runs", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("coding", ctypes.c_int), ("rng_mode", ctypes.c_int), ("weights", ctypes.c_int),
                 ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double),
-                ("sweep_variant", ctypes.c_int)]
+                ("sweep_variant", ctypes.c_int), ("tile_groups", ctypes.c_int)]
 
 
 class Row(ctypes.Structure):
@@ -67,6 +67,7 @@ _SIGS = {
     "pa_config_init": ([ctypes.POINTER(Config)], _i),
     "pa_create": ([ctypes.POINTER(Config), ctypes.POINTER(_vp)], _i),
     "pa_run": ([_vp], _i),
+    "pa_autotune": ([_vp, _vp, _i], _i),
     "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
@@ -128,15 +129,17 @@ _W = {"fp32": WEIGHTS_FP32, "fp64": WEIGHTS_FP64, WEIGHTS_FP32: WEIGHTS_FP32, WE
 
 
 def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, seed=1, coding="ssc",
-                rng="native", weights="fp32", graph=True, device=0, capacity=1.25, sweep_variant=0) -> Config:
+                rng="native", weights="fp32", graph=True, device=0, capacity=1.25, sweep_variant=0,
+                tile_groups=0) -> Config:
     """sweep_variant: CTAs per MSC group in the sweep kernel (0 automatic,
-    1 one CTA, 2 or 4 a thread-block cluster)."""
+    1 one CTA, 2 or 4 a thread-block cluster); tile_groups: MSC groups per
+    work unit of the one-CTA sweep (0 automatic, 1, 2, 4 or 8)."""
     c = Config()
     _check(lib().pa_config_init(ctypes.byref(c)))
     c.L, c.R, c.sweeps, c.dbeta, c.beta_final, c.runs = int(L), int(R), int(sweeps), float(dbeta), float(beta_final), int(runs)
     c.seed, c.coding, c.rng_mode, c.weights = int(seed), _CODING[coding], _RNG[rng], _W[weights]
     c.graph, c.device, c.capacity = int(bool(graph)), int(device), float(capacity)
-    c.sweep_variant = int(sweep_variant)
+    c.sweep_variant, c.tile_groups = int(sweep_variant), int(tile_groups)
     return c
 
 
@@ -170,6 +173,14 @@ class Engine:
 
     def run(self) -> None:
         _check(lib().pa_run(self._h), self._h)
+
+    def autotune(self) -> list[int]:
+        """Time the MSC tile sizes and keep the fastest (pa_autotune); returns
+        the groups per work unit chosen for each population."""
+        n = len(self.configs)
+        arr = (ctypes.c_int * n)()
+        _check(lib().pa_autotune(self._h, arr, n), self._h)
+        return list(arr)
 
     def num_rows(self) -> int:
         n = ctypes.c_int()

@@ -117,6 +117,7 @@ struct pa_handle {
   // rows[set] = rows of one population in one run; set = run * npop + user population index
   std::vector<std::vector<double>> rows;
   int sets_done = 0;
+  bool ran = false;  // pa_run has been called
   double ms = 0.0, attempts = 0.0;
   std::string err;
   std::vector<void*> staging;  // per population: device copy of a caller-supplied initial population
@@ -190,6 +191,65 @@ struct pa_handle {
     return e;
   }
 
+  // Persistent sweep grid for the populations' current geometry and, in
+  // graph mode, the run captured as one graph (again, after a re-tune).
+  cudaError_t setup_launches() {
+    int max_smem = 0;
+    for (const auto& P : pops) max_smem = std::max(max_smem, P.geom.smem);
+    cudaError_t e = cs > 1 ? msc_cluster_setup(cs, rng_mode, max_smem, &sweep)
+                           : sweep_setup(coding, rng_mode, max_smem, &sweep);
+    if (e != cudaSuccess || !graph) return e;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph_t) cudaGraphDestroy(graph_t);
+    exec = nullptr;
+    graph_t = nullptr;
+    e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t e1 = enqueue_run();
+    cudaError_t e2 = cudaStreamEndCapture(stream, &graph_t);
+    if (e1 != cudaSuccess) return e1;
+    if (e2 != cudaSuccess) return e2;
+    return cudaGraphInstantiate(&exec, graph_t, 0);
+  }
+
+  cudaError_t upload_pops(const std::vector<PopDev>& hp) {
+    return cudaMemcpy(d_pops, hp.data(), sizeof(PopDev) * npop, cudaMemcpyHostToDevice);
+  }
+
+  // Device time per spin-flip attempt of one sweep launch over the
+  // populations flagged in `part` (the others are marked finished), with
+  // geometry `geo` for them; the population state is the one left on the
+  // device by the caller (an initialised population at step 1).
+  cudaError_t time_sweep(const std::vector<PopDev>& state, const std::vector<char>& part, const SweepGeom& geo,
+                         double* ns_per_attempt) {
+    std::vector<PopDev> hp = state;
+    double attempts = 0;
+    for (int k = 0; k < npop; ++k) {
+      if (part[k]) {
+        geom_to_pop(geo, &hp[k]);
+        if (pop_stepping(&hp[k])) attempts += (double)pops[k].cfg.sweeps * hp[k].N * (double)hp[k].R_cur;
+      } else {
+        hp[k].step = hp[k].nsteps + 1;
+      }
+    }
+    cudaError_t e = upload_pops(hp);
+    SweepLaunch sl{};
+    if (e == cudaSuccess) e = sweep_setup(coding, rng_mode, geo.smem, &sl);
+    float best = 0.f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {  // the first launch warms up
+      e = launch_plan(d_batch, npop, 0, stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
+      if (e == cudaSuccess) e = launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sl, stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+      if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    *ns_per_attempt = attempts > 0 ? best * 1e6 / attempts : 0.0;
+    return e;
+  }
+
   ~pa_handle() {
     for (void* p : staging)
       if (p) cudaFree(p);
@@ -221,9 +281,15 @@ int validate(const pa_config& c) {
   if (c.sweep_variant != 0 && c.sweep_variant != 1 && c.sweep_variant != 2 && c.sweep_variant != 4)
     return bad("sweep_variant must be 0, 1, 2 or 4");
   if (c.coding == PA_CODING_SSC && c.sweep_variant > 1) return bad("cluster sweeps exist for MSC only");
+  if (c.tile_groups != 0 && c.tile_groups != 1 && c.tile_groups != 2 && c.tile_groups != 4 && c.tile_groups != 8)
+    return bad("tile_groups must be 0, 1, 2, 4 or 8");
+  if (c.tile_groups > 1 && (c.coding != PA_CODING_MSC || msc_variant(c.sweep_variant, c.L) > 1))
+    return bad("tiles of several groups exist for the one-CTA MSC sweep only");
   SweepGeom g;
   if (c.coding == PA_CODING_MSC) {
     const int cs = msc_variant(c.sweep_variant, c.L);
+    if (cs == 1 && c.tile_groups > 1 && !msc_geom(c.L, &g, c.tile_groups))
+      return bad("tile_groups > 1 needs L % 4 == 0 and at most 44 KB of spins per tile");
     const bool ok = cs == 1 ? msc_geom(c.L, &g) : msc_cluster_geom(c.L, cs, msc_cluster_threads(cs), &g);
     if (!ok) return bad("MSC needs even L in [8, 128] (one CTA per group) or L % 4 == 0 up to 256 (clusters)");
   } else if (!ssc_geom(c.L, &g)) {
@@ -258,9 +324,16 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
 
   // one sweep kernel serves the whole batch: clusters if any population needs them
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c0.device);
+  const int slots = 5 * nsm;  // resident one-CTA sweep CTAs (five per SM up to 44 KB of tile)
   H->cs = 1;
+  long long batch_groups = 0;  // work available to the one-CTA sweep: bounds automatic tile sizes
   if (H->coding == PA_CODING_MSC)
-    for (const auto& c : cfgs) H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
+    for (const auto& c : cfgs) {
+      H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
+      batch_groups += (c.R + kMsb - 1) / kMsb;
+    }
   H->pops.resize(cfgs.size());
   for (size_t k = 0; k < cfgs.size(); ++k) {
     PopHost& P = H->pops[k];
@@ -269,7 +342,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     if (P.cfg.capacity <= 0) P.cfg.capacity = 1.25;
     bool okg;
     if (P.cfg.coding == PA_CODING_SSC) okg = ssc_geom(P.cfg.L, &P.geom);
-    else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom);
+    else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_groups, slots);
     else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
     if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +
                                           std::to_string(H->cs) + " CTAs");
@@ -283,7 +356,6 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     return (long long)a.cfg.L * a.cfg.L * a.cfg.sweeps > (long long)b.cfg.L * b.cfg.L * b.cfg.sweeps;
   });
 
-  int max_smem = 0;
   long long max_units = 1;
   DevBuf& B = H->buf;
   auto chk = [&](cudaError_t err) {
@@ -314,7 +386,6 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     // reference stream: every population starts at initial_sequence = 0 like a
     // separate run of the reference program; native stream: disjoint ranges
     h.iseq = c.rng_mode == PA_RNG_REFERENCE ? 0ull : (unsigned long long)P.user_index << 40;
-    max_smem = std::max(max_smem, P.geom.smem);
     const size_t units = c.coding == PA_CODING_MSC ? (size_t)rgcap * kMsb : (size_t)Rcap;
     max_units = std::max(max_units, (long long)units);
     if (c.coding == PA_CODING_MSC) {
@@ -357,8 +428,6 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   }
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   H->rblocks = res_blocks(max_units);
-  chk(H->cs > 1 ? msc_cluster_setup(H->cs, H->rng_mode, max_smem, &H->sweep)
-                : sweep_setup(H->coding, H->rng_mode, max_smem, &H->sweep));
   chk(B.alloc(&H->d_pops, (size_t)H->npop));
   chk(B.alloc(&H->d_batch, 1));
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
@@ -374,16 +443,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   chk(cudaEventCreate(&H->ev0));
   chk(cudaEventCreate(&H->ev1));
   H->staging.assign(H->npop, nullptr);
-  if (e == cudaSuccess && H->graph) {
-    chk(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
-    if (e == cudaSuccess) {
-      cudaError_t e1 = H->enqueue_run();
-      cudaError_t e2 = cudaStreamEndCapture(H->stream, &H->graph_t);
-      chk(e1);
-      chk(e2);
-      if (e == cudaSuccess) chk(cudaGraphInstantiate(&H->exec, H->graph_t, 0));
-    }
-  }
+  if (e == cudaSuccess) chk(H->setup_launches());
   if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e));
   *out = H;
   return PA_OK;
@@ -483,6 +543,7 @@ int pa_run(pa_handle* H) {
   H->rows.assign((size_t)H->npop * H->seq_runs, {});
   H->sets_done = 0;
   H->attempts = 0;
+  H->ran = true;
   cudaError_t e = cudaEventRecord(H->ev0, H->stream);
   if (e != cudaSuccess) return H->cuda_fail(e, "event");
   int status = PA_OK;
@@ -535,6 +596,56 @@ int pa_run(pa_handle* H) {
   if (e != cudaSuccess) return H->cuda_fail(e, "timing");
   H->ms = ms;
   return status;
+}
+
+int pa_autotune(pa_handle* H, int* tiles, int n) {
+  if (!H || (n > 0 && !tiles)) return PA_ERR_ARG;
+  if (H->ran) {
+    H->err = "pa_autotune must precede the first pa_run";
+    return PA_ERR_STATE;
+  }
+  if (H->coding == PA_CODING_MSC && H->cs == 1) {
+    // an initialised population (step 1, random spins) to sweep
+    cudaError_t e = H->enqueue_init();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    std::vector<PopDev> state(H->npop);
+    if (e == cudaSuccess) e = cudaMemcpy(state.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
+    std::vector<int> done(H->npop, 0);
+    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+      if (done[k]) continue;
+      const int L = H->pops[k].cfg.L;
+      std::vector<char> part(H->npop, 0);
+      for (int j = 0; j < H->npop; ++j) part[j] = H->pops[j].cfg.L == L;
+      int best_G = 1;
+      double best = 0;
+      for (int G = 1; G <= 8 && e == cudaSuccess; G *= 2) {
+        SweepGeom g;
+        if (!msc_geom(L, &g, G)) continue;
+        double t = 0;
+        e = H->time_sweep(state, part, g, &t);
+        if (e == cudaSuccess && t > 0 && (best == 0 || t < best)) {
+          best = t;
+          best_G = G;
+        }
+      }
+      for (int j = 0; j < H->npop; ++j)
+        if (part[j]) {
+          done[j] = 1;
+          PopHost& P = H->pops[j];
+          msc_geom(L, &P.geom, best_G);
+          geom_to_pop(P.geom, &P.h);
+        }
+    }
+    // the run starts from the configured state again (stream positions included)
+    std::vector<PopDev> hp(H->npop);
+    for (int k = 0; k < H->npop; ++k) hp[k] = H->pops[k].h;
+    if (e == cudaSuccess) e = H->upload_pops(hp);
+    if (e == cudaSuccess) e = H->setup_launches();
+    if (e != cudaSuccess) return H->cuda_fail(e, "autotune");
+  }
+  for (int k = 0; k < H->npop; ++k)
+    if (H->pops[k].user_index < n) tiles[H->pops[k].user_index] = H->pops[k].geom.G;
+  return PA_OK;
 }
 
 int pa_num_rows(const pa_handle* H, int* n) {

@@ -24,10 +24,22 @@ struct SweepGeom {
   int npass;   // ceil(L / rpp)
   int kconst;  // (N/2)/128 when 128 divides N/2 (draws per reference thread per half sweep), else 0
   int smem;    // dynamic shared memory bytes for one work unit
+  int G = 1;   // MSC groups per work unit: G lattices stacked as G*L rows of one sweep
 };
 
+// ceil(2^32 / d) for 2 <= d < 2^16: then __umulhi(n, recip32(d)) == n / d
+// for every n < 2^16 (the rounding error n * (ceil - 2^32/d) / 2^32 < 2^-16 is
+// smaller than the distance 1/d from n/d to the next integer).
+inline unsigned int recip32(int d) {
+  return (unsigned int)((0x100000000ull + (unsigned long long)d - 1) / (unsigned long long)d);
+}
+
 bool ssc_geom(int L, SweepGeom* g);
-bool msc_geom(int L, SweepGeom* g);
+// tile: groups per work unit (0 automatic); groups: how many groups the
+// sweep launches will hold and slots: resident CTAs of the persistent grid,
+// which together drive the automatic choice (single-group tiles when either
+// is 0)
+bool msc_geom(int L, SweepGeom* g, int tile = 0, long long groups = 0, int slots = 0);
 void geom_to_pop(const SweepGeom& g, PopDev* h);
 
 struct SweepLaunch {

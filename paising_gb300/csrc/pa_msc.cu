@@ -12,7 +12,9 @@
 //
 // Layout in HBM: group g occupies N words at spins + g*N (sublattice A words,
 // then B); bit k of a word is replica k of the group, 1 == spin +1.
+#include <algorithm>
 #include <climits>
+#include <type_traits>
 
 #include "pa_kernels.h"
 #include "pa_msc_core.cuh"
@@ -54,10 +56,12 @@ __global__ void msc_init_kernel(PopDev* pops) {
 }
 
 // ----------------------------------------------------------------- sweep
-// Persistent: every CTA takes groups of 32 replicas of any population from
-// the batch's work queue and anneals one group at a time, both sublattices
-// resident in shared memory.  Thread (rsub, tx) owns site column tx of
-// sublattice rows rsub, rsub+rpp, ...
+// Persistent: every CTA takes tiles of G groups of 32 replicas of any
+// population from the batch's work queue and anneals one tile at a time,
+// resident in shared memory as all G sublattices A, then all G sublattices B
+// (so the tile is one stack of G*L sublattice rows of Wr words; a row's
+// vertical neighbours wrap inside its own group).  Thread (rsub, tx) owns
+// word column tx of stacked rows rsub, rsub+rpp, ...
 //
 // MODE kRefCoords: decisions of checkKerALL exactly -- one draw per word-site
 //   (ctr = sw*2K + hf*K + k of subsequence iseq + t + 128 g) expanded to 32
@@ -67,12 +71,13 @@ __global__ void msc_init_kernel(PopDev* pops) {
 //   (accept_native); each replica's acceptance probability is exactly
 //   T/2^32, as in the reference.  The stream is keyed by stream_seed (one
 //   per batch; populations differ in counter word 3).
+static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the tile, bit) in the epilogue");
 template <int MODE>
 __global__ void __launch_bounds__(kSweepThreads, 5)
     msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
-  extern __shared__ __align__(16) uint32_t lat[];  // N words: A then B
+  extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
   __shared__ int s_unit, s_pop;
-  __shared__ int s_cntE[kMsb], s_cntM[kMsb];
+  __shared__ int s_cntE[kMaxTile * kMsb], s_cntM[kMaxTile * kMsb];  // [group of the tile][bit]
   __shared__ uint2 s_dig[kMsb];  // per digit j: (D8_j, D4_j ^ D8_j)
   __shared__ UnitParams P;
   __shared__ BitStats stats;
@@ -100,6 +105,12 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
         P.step = st->step;
         P.sweeps = energy_only ? 0 : st->sweeps;
         P.nbatch = (st->npass + kKB - 1) / kKB;
+        P.G = st->gpt > 0 ? st->gpt : 1;
+        P.rg = (st->R_cur + kMsb - 1) / kMsb;
+        P.invL = st->invL;
+        P.invWr = st->invWr;
+        const unsigned long long h4 = (unsigned long long)(st->N >> 3);
+        P.invH4 = (uint32_t)((0x100000000ull + h4 - 1) / h4);
         P.tag = kTagMscSweep | (uint32_t)st->pop_id;
         P.T4 = st->thr[(size_t)st->step * kThrPerStep + 10];
         P.T8 = st->thr[(size_t)st->step * kThrPerStep + 11];
@@ -112,9 +123,10 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
         P.M = st->M;
       }
     }
-    if (tid < kMsb) { s_cntE[tid] = 0; s_cntM[tid] = 0; }
+    s_cntE[tid] = 0;  // kMaxTile * kMsb == kSweepThreads
+    s_cntM[tid] = 0;
     __syncthreads();
-    const int p = s_pop, gi = s_unit;
+    const int p = s_pop, ti = s_unit;  // population, tile
     if (p < 0) break;
     if (p != cur) {  // block-uniform
       if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
@@ -130,32 +142,71 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
         s_dig[tid] = make_uint2(d8, d4 ^ d8);
       }
     }
-    const int N = P.N, h = P.h;
+    const int N = P.N, h = P.h, G = P.G, gi0 = ti * G;
+    const int gc = min(G, P.rg - gi0);  // groups present in this tile
     uint32_t* words = P.words;
-    const uint4* gsrc = (const uint4*)(words + (size_t)gi * N);
-    uint4* lat4 = (uint4*)lat;
-    for (int v = tid; v < (N >> 2); v += blockDim.x) lat4[v] = gsrc[v];
+    // tile <-> HBM: group gi0+g's sublattice X goes to lat + X*G*h + g*h
+    // (for G = 1 simply the group's N words; G > 1 implies h % 4 == 0)
+    auto move_tile = [&](bool to_smem) {
+      uint4* lat4 = (uint4*)lat;
+      uint4* g4 = (uint4*)(words + (size_t)gi0 * N);
+      if (G == 1) {
+        for (int v = tid; v < (N >> 2); v += blockDim.x) {
+          if (to_smem) lat4[v] = g4[v];
+          else g4[v] = lat4[v];
+        }
+        return;
+      }
+      const int h4 = h >> 2, n4 = N >> 2;
+      for (int v = tid; v < 2 * gc * h4; v += blockDim.x) {
+        const int X = v >= gc * h4 ? 1 : 0, r = v - X * gc * h4;
+        const int g = (int)__umulhi((uint32_t)r, P.invH4), i = r - g * h4;
+        uint4* s = lat4 + X * G * h4 + g * h4 + i;
+        uint4* d = g4 + (size_t)g * n4 + X * h4 + i;
+        if (to_smem) *s = *d;
+        else *d = *s;
+      }
+    };
+    move_tile(true);
     __syncthreads();
 
+    // stacked row v of the tile -> group g, row y in the group, smem offsets
+    // of the row and its vertical neighbours (periodic inside the group)
+    struct RowPos {
+      int g, y, row, rowu, rowd;
+    };
+    auto row_pos = [&](int v) {
+      RowPos q;
+      const int L = P.L, Wr = P.Wr;
+      q.g = (int)__umulhi((uint32_t)v, P.invL);
+      q.y = v - q.g * L;
+      q.row = v * Wr;
+      q.rowu = (q.y == 0 ? v + L - 1 : v - 1) * Wr;
+      q.rowd = (q.y + 1 == L ? v + 1 - L : v + 1) * Wr;
+      return q;
+    };
+    const int vrows = gc * P.L;  // stacked rows present
     const int sweeps = P.sweeps;
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
       for (int hf = 0; hf < 2; ++hf) {
-        uint32_t* self = lat + (hf ? h : 0);
-        const uint32_t* oth = lat + (hf ? 0 : h);
-        const int L = P.L, Wr = P.Wr, rpp = P.rpp, npass = P.npass;
+        uint32_t* self = lat + (hf ? G * h : 0);
+        const uint32_t* oth = lat + (hf ? 0 : G * h);
+        const int Wr = P.Wr, rpp = P.rpp, npass = P.npass;
         if (MODE == kRefCoords) {
 #pragma unroll 1
           for (int pass = 0; pass < npass; ++pass) {
-            const int ty = rsub + pass * rpp;
-            const bool valid = worker && ty < L;
-            const int tyc = valid ? ty : 0;
-            const int row = tyc * Wr, rowu = (tyc == 0 ? L - 1 : tyc - 1) * Wr, rowd = (tyc + 1 == L ? 0 : tyc + 1) * Wr;
-            const int idx = row + tx;
+            const int v = rsub + pass * rpp;
+            const bool valid = worker && v < vrows;
+            const RowPos q = row_pos(valid ? v : 0);
+            const int sidx = q.row + tx;       // word in the tile's sublattice array
+            const int idx = q.y * Wr + tx;     // word in the group's sublattice
+            const int gi = gi0 + q.g;
             // horizontal neighbour not at the same idx (PAisingMSC.cu:203, 238)
-            const bool left = (hf == 0) == ((tyc & 1) == 0);
-            const uint32_t s = self[idx];
-            const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[idx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
+            const bool left = (hf == 0) == ((q.y & 1) == 0);
+            const uint32_t s = self[sidx];
+            const uint32_t n1 = oth[q.row + (left ? txl : txr)], n2 = oth[sidx], n3 = oth[q.rowu + tx],
+                           n4 = oth[q.rowd + tx];
             uint32_t s0, s1, s2;
             adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
             const int t = idx & (kRefThreads - 1), k = idx >> 7;
@@ -172,39 +223,59 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
             }
             const uint32_t hi = s1 | s2;
             const uint32_t acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
-            if (valid) self[idx] = s ^ acc;
+            if (valid) self[sidx] = s ^ acc;
           }
         } else {
-          const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+          // one code path for single-group tiles (the common L >= 64 case, kept
+          // free of the stacking arithmetic) and one for stacked tiles
+          auto native_half = [&](auto tiled_c) {
+            constexpr bool kTiled = decltype(tiled_c)::value;
+            const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+            const uint32_t base = (uint32_t)gi0 * (uint32_t)h;  // site number of the tile's first word
 #pragma unroll 1
-          for (int p0 = 0; p0 < npass; p0 += kKB) {
-            uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
-            int ix[kKB];
+            for (int p0 = 0; p0 < npass; p0 += kKB) {
+              uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+              uint32_t vm = 0;  // slots holding a site
 #pragma unroll
-            for (int k = 0; k < kKB; ++k) {
-              const int pass = p0 + k;
-              const int ty = rsub + pass * rpp;
-              const bool valid = worker && pass < npass && ty < L;
-              const int tyc = valid ? ty : 0;
-              const int row = tyc * Wr, rowu = (tyc == 0 ? L - 1 : tyc - 1) * Wr, rowd = (tyc + 1 == L ? 0 : tyc + 1) * Wr;
-              const int idx = row + tx;
-              const bool left = (hf == 0) == ((tyc & 1) == 0);
-              const uint32_t s = self[idx];
-              const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[idx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
-              uint32_t s0, s1, s2;
-              adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
-              av[k] = s0;
-              ac[k] = s1 | s2;
-              un[k] = valid ? ~(s1 | s2) : 0u;
-              ix[k] = valid ? idx : -1;
-              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)idx;
+              for (int k = 0; k < kKB; ++k) {
+                const int pass = p0 + k;
+                const int v = rsub + pass * rpp;
+                const bool valid = worker && pass < npass && v < (kTiled ? vrows : P.L);
+                const int vc = valid ? v : 0;
+                int row, rowu, rowd;
+                if (kTiled) {
+                  const RowPos q = row_pos(vc);
+                  row = q.row;
+                  rowu = q.rowu;
+                  rowd = q.rowd;
+                } else {
+                  const int L = P.L;
+                  row = vc * Wr;
+                  rowu = (vc == 0 ? L - 1 : vc - 1) * Wr;
+                  rowd = (vc + 1 == L ? 0 : vc + 1) * Wr;
+                }
+                const int sidx = row + tx;
+                // row parity: stacked groups have even L, so v and y agree
+                const bool left = (hf == 0) == ((vc & 1) == 0);
+                const uint32_t s = self[sidx];
+                const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[sidx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
+                uint32_t s0, s1, s2;
+                adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
+                av[k] = s0;
+                ac[k] = s1 | s2;
+                un[k] = valid ? ~(s1 | s2) : 0u;
+                vm |= valid ? 1u << k : 0u;
+                site[k] = base + (uint32_t)sidx;  // = group * h + word in the group
+              }
+              const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
+              accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0);
+#pragma unroll
+              for (int k = 0; k < kKB; ++k)
+                if (vm >> k & 1u) self[site[k] - base] ^= ac[k];
             }
-            const uint32_t chain = ((uint32_t)gi * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
-            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig);
-#pragma unroll
-            for (int k = 0; k < kKB; ++k)
-              if (ix[k] >= 0) self[ix[k]] ^= ac[k];
-          }
+          };
+          if (G == 1) native_half(std::integral_constant<bool, false>());
+          else native_half(std::integral_constant<bool, true>());
         }
         __syncthreads();
       }
@@ -212,41 +283,54 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
 
     // energy and magnetisation per replica bit: the left and up bond of every
     // A and B site (PAisingMSC.cu:272-294), counted per bit with warp ballots.
-    int cE = 0, cM = 0;  // lane k accumulates bit k
+    // Each warp works inside one group (kSweepThreads/32/G warps per group),
+    // so a ballot never mixes groups.
     {
-      const int L = P.L, Wr = P.Wr, rpp = P.rpp, npass = P.npass;
-      for (int pass = 0; pass < npass; ++pass) {
-        const int ty = rsub + pass * rpp;
-        const bool valid = worker && ty < L;
-        uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
-        if (valid) {
-          const int row = ty * Wr, idx = row + tx, iL = row + txl, iU = (ty + 1 == L ? 0 : ty + 1) * Wr + tx;
-          sA = lat[idx];
-          sB = lat[h + idx];
-          uint32_t Ai2, Bi2;
-          if (ty & 1) { Ai2 = sB; Bi2 = lat[iL]; }
-          else { Ai2 = lat[h + iL]; Bi2 = sA; }
-          adder4(sA ^ Ai2, sA ^ lat[h + iU], sB ^ Bi2, sB ^ lat[iU], s0, s1, s2);
-        }
+      const int L = P.L, Wr = P.Wr, wpg = (kSweepThreads / 32) / G;
+      const int w = tid >> 5, g = w / wpg, ws = w - g * wpg;
+      int cE = 0, cM = 0;  // lane k accumulates bit k
+      if (g < gc) {        // warp-uniform
+        const uint32_t* A = lat + g * h;
+        const uint32_t* B = lat + G * h + g * h;
+        for (int j0 = ws * 32; j0 < h; j0 += wpg * 32) {
+          const int j = j0 + lane;
+          uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
+          if (j < h) {
+            const int y = (int)__umulhi((uint32_t)j, P.invWr), x = j - y * Wr;
+            const int iL = y * Wr + (x == 0 ? Wr - 1 : x - 1), iU = (y + 1 == L ? 0 : y + 1) * Wr + x;
+            sA = A[j];
+            sB = B[j];
+            uint32_t Ai2, Bi2;
+            if (y & 1) { Ai2 = sB; Bi2 = A[iL]; }
+            else { Ai2 = B[iL]; Bi2 = sA; }
+            adder4(sA ^ Ai2, sA ^ B[iU], sB ^ Bi2, sB ^ A[iU], s0, s1, s2);
+          }
 #pragma unroll 4
-        for (int k = 0; k < kMsb; ++k) {
-          const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
-                        4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
-          const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
-          if (lane == k) { cE += e; cM += m; }
+          for (int k = 0; k < kMsb; ++k) {
+            const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) +
+                          2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
+                          4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
+            const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
+            if (lane == k) { cE += e; cM += m; }
+          }
         }
+        atomicAdd(&s_cntE[g * kMsb + lane], cE);
+        atomicAdd(&s_cntM[g * kMsb + lane], cM);
       }
     }
-    atomicAdd(&s_cntE[lane], cE);
-    atomicAdd(&s_cntM[lane], cM);
-    uint4* gdst = (uint4*)(words + (size_t)gi * N);
-    for (int v = tid; v < (N >> 2); v += blockDim.x) gdst[v] = lat4[v];
+    move_tile(false);
     __syncthreads();
-    if (tid < kMsb) {
+    if (tid < gc * kMsb) {
+      const int gi = gi0 + (tid >> 5);
       const int E = 2 * s_cntE[tid] - 2 * N, Mg = 2 * s_cntM[tid] - N;
-      P.E[gi * kMsb + tid] = E;
-      P.M[gi * kMsb + tid] = Mg;
-      if (P.act[gi * kMsb + tid]) stats.add(tid, E, Mg);
+      P.E[gi * kMsb + lane] = E;
+      P.M[gi * kMsb + lane] = Mg;
+    }
+    if (tid < kMsb) {  // lane k of warp 0 owns the statistics of bit k
+      for (int g = 0; g < gc; ++g) {
+        const int gi = gi0 + g, E = 2 * s_cntE[g * kMsb + tid] - 2 * N, Mg = 2 * s_cntM[g * kMsb + tid] - N;
+        if (P.act[gi * kMsb + tid]) stats.add(tid, E, Mg);
+      }
     }
   }
   if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
@@ -284,24 +368,64 @@ __global__ void msc_resample_kernel(PopDev* pops) {
 }
 
 // -------------------------------------------------------------- geometry
-static int pick_rpp(int L, int Wr) {
-  int best = 1;
-  for (int r = 1; r <= L; ++r)
-    if (L % r == 0 && Wr * r <= kSweepThreads) best = r;
-  return best;
+// A work unit is a tile of G groups whose lattices are stacked into G*L
+// sublattice rows; every pass of a half-sweep updates rpp of those rows with
+// Wr threads each.  G is chosen to fill the thread slots of whole kKB-site
+// batches: small lattices (L=16: 128 words per half-sweep) would otherwise
+// leave most of a 256-thread CTA idle.
+static double msc_fill(int L, int G, int* rpp, int* npass) {
+  const int Wr = L / 2, VR = G * L;
+  int r = kSweepThreads / Wr;
+  if (r > VR) r = VR;
+  const int np = (VR + r - 1) / r, padded = (np + kKB - 1) / kKB * kKB;
+  *rpp = r;
+  *npass = np;
+  return (double)VR * Wr / ((double)padded * kSweepThreads);
 }
 
-bool msc_geom(int L, SweepGeom* g) {
+bool msc_geom(int L, SweepGeom* g, int tile, long long groups, int slots) {
   if (L < 8 || L % 2 != 0 || L > 128) return false;
   g->L = L;
   g->N = L * L;
   g->half = g->N / 2;
   g->Wr = L / 2;
-  g->rpp = pick_rpp(L, g->Wr);
-  g->T = g->Wr * g->rpp;
-  g->npass = (L + g->rpp - 1) / g->rpp;
+  // G > 1 moves each sublattice with 16-byte vectors (h % 4 == 0) and keeps
+  // the tile within the shared memory of five resident CTAs per SM
+  auto allowed = [&](int G) {
+    return G == 1 || (G == 2 || G == 4 || G == kMaxTile) && g->half % 4 == 0 && G * g->N * 4 <= kTileSmemMax;
+  };
+  int best_G = 1, rpp = 0, npass = 0;
+  if (tile > 0) {
+    if (!allowed(tile)) return false;
+    best_G = tile;
+  } else if (groups > 0 && slots > 0) {
+    // automatic, by a cost model: waves of work units over the resident
+    // CTAs times the thread slots one unit occupies per half-sweep (whole
+    // kKB-site batches), with the stacking arithmetic of G > 1 counted as
+    // 7% more work (the measured gap at equal fill)
+    auto cost = [&](int G) {
+      int r, np;
+      msc_fill(L, G, &r, &np);
+      const double waves = std::max(1.0, (double)((groups + G - 1) / G) / slots);
+      return waves * ((np + kKB - 1) / kKB * kKB) * (G > 1 ? 1.07 : 1.0);
+    };
+    double best = cost(1);
+    for (int G = 2; G <= kMaxTile; G *= 2) {
+      if (!allowed(G)) continue;
+      const double c = cost(G);
+      if (c < best - 1e-9) {
+        best = c;
+        best_G = G;
+      }
+    }
+  }
+  g->G = best_G;
+  msc_fill(L, best_G, &rpp, &npass);
+  g->rpp = rpp;
+  g->T = g->Wr * rpp;
+  g->npass = npass;
   g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
-  g->smem = g->N * 4;
+  g->smem = best_G * g->N * 4;
   return true;
 }
 

@@ -15,6 +15,8 @@ constexpr uint32_t kLcgA = 1664525u;     // PAisingMSC.cu:53
 constexpr uint32_t kLcgC = 1013904223u;  // PAisingMSC.cu:54
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kKB = 4;  // word-sites per thread decided together (native stream)
+constexpr int kMaxTile = 8;                // groups per work unit of the one-CTA sweep (one warp each at least)
+constexpr int kTileSmemMax = 44 * 1024;    // shared memory of a tile of more than one group
 
 // Bitsliced count of anti-parallel neighbours (4 inputs -> 3 bit planes),
 // the adder of PAisingMSC.cu:212-218.
@@ -69,18 +71,28 @@ __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uin
 //   a[k]   : bits with one anti-parallel neighbour (threshold T4), else T8
 //   und[k] : bits needing a random decision (consumed)
 //   acc[k] : accepted bits (in: outright accepts; out: all accepts)
+//   nvalid : block-uniform count of the leading slots that hold sites; the
+//            other slots have und = 0 and draw nothing
 __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t (&und)[kKB], uint32_t (&acc)[kKB],
                                               const uint32_t (&site)[kKB], uint32_t chain_c0, uint32_t c1,
-                                              uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig) {
+                                              uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig,
+                                              int nvalid) {
   // independent Philox chains of the kKB sites, interleaved by the compiler
   const uint2 d0 = dig[0], d1 = dig[1], d2 = dig[2], d3 = dig[3];
-#pragma unroll
-  for (int k = 0; k < kKB; ++k) {
+  auto head = [&](int k) {
     const U4 r = philox10k(site[k], c1, step, tag, K);
     digit_step(r.x, a[k], d0, und[k], acc[k]);
     digit_step(r.y, a[k], d1, und[k], acc[k]);
     digit_step(r.z, a[k], d2, und[k], acc[k]);
     digit_step(r.w, a[k], d3, und[k], acc[k]);
+  };
+  if (nvalid >= kKB) {
+#pragma unroll
+    for (int k = 0; k < kKB; ++k) head(k);
+  } else {
+#pragma unroll
+    for (int k = 0; k < kKB; ++k)
+      if (k < nvalid) head(k);
   }
   uint32_t m = und[0], am = a[0] & und[0];
   uint32_t rot[kKB];
@@ -113,6 +125,8 @@ __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t
 // footprint independent of how many populations the batch holds.
 struct UnitParams {
   int L, N, h, Wr, rpp, npass, kconst, step, sweeps, nbatch;
+  int G, rg;                    // groups per tile, groups in the population
+  uint32_t invL, invWr, invH4;  // reciprocals (recip32) of L, Wr and h/4
   uint32_t tag, T4, T8;
   unsigned long long seed, iseq;
   uint32_t* words;

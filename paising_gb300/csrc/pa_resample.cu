@@ -240,7 +240,10 @@ __global__ void __launch_bounds__(1024) plan_kernel(BatchDev* b, int energy_only
   if (p < np) {
     const PopDev* st = b->pops + p;
     const bool part = energy_only ? (st->step == 0) : pop_stepping(st);
-    if (part) units = st->coding == kMSC ? (uint32_t)((st->R_cur + kMsb - 1) / kMsb) : (uint32_t)st->R_cur;
+    if (part) {
+      const int gpt = st->gpt > 0 ? st->gpt : 1;
+      units = st->coding == kMSC ? (uint32_t)(((st->R_cur + kMsb - 1) / kMsb + gpt - 1) / gpt) : (uint32_t)st->R_cur;
+    }
   }
   uint32_t total;
   const uint32_t ex = block_exscan(units, s_u, &total);
@@ -336,6 +339,9 @@ void geom_to_pop(const SweepGeom& g, PopDev* h) {
   h->T = g.T;
   h->npass = g.npass;
   h->kconst = g.kconst;
+  h->gpt = g.G;
+  h->invL = recip32(g.L);
+  h->invWr = recip32(g.Wr);
 }
 
 cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out) {

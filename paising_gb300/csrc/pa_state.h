@@ -28,8 +28,11 @@ struct PopDev {
   // ------------------------------------------------ configuration (constant)
   int L, N, coding, Rinit, Rcap, rgcap, sweeps, rng_mode, weights, pop_id, nsteps, pad0;
   // sweep thread layout (see SweepGeom): words per row, rows per pass,
-  // worker threads, passes, reference draws per thread per half sweep
-  int Wr, rpp, T, npass, kconst, pad1;
+  // worker threads, passes, reference draws per thread per half sweep,
+  // MSC groups per work unit (tile), and the reciprocals of L and Wr used
+  // to split row and word indices without division
+  int Wr, rpp, T, npass, kconst, gpt;
+  unsigned int invL, invWr;
   unsigned long long seed;
   // ------------------------------------------------ buffers
   void* spins[2];      // SSC: int8 [Rcap][N] (+-1, sublattice A then B); MSC: uint32 [rgcap][N]

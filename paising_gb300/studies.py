@@ -117,13 +117,20 @@ def batch(seed: int = 2026) -> dict:
     pops = [dict(L=int(rng.choice([16, 32, 48, 64, 96, 128])), R=int(rng.integers(1000, 20001)),
                  dbeta=float(rng.choice([0.0025, 0.005, 0.01])), sweeps=20, seed=seed + k) for k in range(64)]
     res = {"populations": pops}
-    with pa.Engine.batch(pops, coding="msc") as e:
-        e.run()  # warm (graph upload)
-        t0 = time.perf_counter()
-        e.run()
-        wall = time.perf_counter() - t0
-        ms, att = e.timing()
-    res["batched"] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6)}
+    for form, tune in (("batched", True), ("batched_model_tiles", False)):
+        with pa.Engine.batch(pops, coding="msc") as e:
+            t0 = time.perf_counter()
+            tiles = e.autotune() if tune else None
+            tune_s = time.perf_counter() - t0
+            e.run()  # warm (graph upload)
+            t0 = time.perf_counter()
+            e.run()
+            wall = time.perf_counter() - t0
+            ms, att = e.timing()
+        res[form] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6)}
+        if tune:
+            res[form]["autotune_s"] = tune_s
+            res[form]["tiles_by_L"] = {str(p["L"]): t for p, t in zip(pops, tiles)}
     tot_ms = tot_att = 0.0
     t0 = time.perf_counter()
     for p in pops:

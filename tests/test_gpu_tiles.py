@@ -1,0 +1,96 @@
+"""Tiles of several MSC groups per work unit of the one-CTA sweep
+(tile_groups 2, 4, 8: the groups' lattices stacked into one array of G*L
+sublattice rows whose vertical neighbours wrap inside each group).  Under the
+reference-coordinate stream every tile size must reproduce the reference's
+and the oracle's runs exactly, including tiles left partly empty at the end
+of a population."""
+import numpy as np
+import pytest
+
+import paising_gb300 as pa
+from conftest import compare_rows, load_dat
+
+pytestmark = pytest.mark.gpu
+
+
+def run(**kw):
+    with pa.Engine(**kw) as e:
+        e.run()
+        return [e.rows(r) for r in range(e.num_sets())]
+
+
+@pytest.mark.parametrize("tile", [2, 4, 8])
+@pytest.mark.parametrize("graph", [True, False])
+def test_tiles_reference_C1(cuda, tile, graph):
+    """L=16, R=1000 (32 groups: full tiles of 2, 4 and 8)."""
+    rows = run(L=16, R=1000, sweeps=10, seed=100, coding="msc", rng="reference", weights="fp64", graph=graph,
+               tile_groups=tile)
+    compare_rows(rows[0], load_dat("ref/inj_MSC_L16_R1000_t10_d0.005_s100.dat"), rtol=2e-10)
+
+
+@pytest.mark.parametrize("L,R,tile", [(24, 650, 8), (32, 300, 2), (48, 700, 4), (20, 170, 4), (64, 90, 2)])
+def test_tiles_partial_reference_stream(cuda, oracle, L, R, tile):
+    """Group counts that leave the last tile partly empty (and populations
+    whose size changes from step to step) against the oracle."""
+    sweeps, dbeta, bfin, seed = 3, 0.1, 1.0, 17
+    ref, _ = oracle.anneal("msc", L, R, sweeps, dbeta, bfin, 1, seed)
+    rows = run(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=bfin, seed=seed, coding="msc", rng="reference",
+               weights="fp64", tile_groups=tile)
+    compare_rows(rows[0], ref[0], rtol=1e-9)
+
+
+def test_tiles_batch_mixed(cuda, oracle):
+    """One batch whose populations use different tile sizes."""
+    pops = [dict(L=16, R=300, sweeps=5, dbeta=0.05, seed=100, tile_groups=8),
+            dict(L=32, R=500, sweeps=3, dbeta=0.1, seed=7, tile_groups=2),
+            dict(L=10, R=90, sweeps=7, dbeta=0.04, beta_final=0.6, seed=3, tile_groups=1),
+            dict(L=48, R=200, sweeps=2, dbeta=0.2, seed=11, tile_groups=4)]
+    with pa.Engine.batch(pops, coding="msc", rng="reference", weights="fp64") as e:
+        e.run()
+        for k, p in enumerate(pops):
+            ref, _ = oracle.anneal("msc", p["L"], p["R"], p["sweeps"], p["dbeta"], p.get("beta_final", 1.0), 1,
+                                   p["seed"])
+            compare_rows(e.rows(k), ref[0], rtol=1e-9)
+
+
+@pytest.mark.parametrize("tile", [2, 8])
+def test_tiles_native_free_energy_vs_kaufman_L16(cuda, oracle, tile):
+    """Native stream through stacked tiles: betaF/N within 3e-4 of the exact
+    value at every beta."""
+    r = run(L=16, R=20000, sweeps=20, seed=12, coding="msc", tile_groups=tile)[0]
+    exact = np.array([-oracle.kaufman(16, b)[0] / 256 for b in r[:, 0]])
+    assert np.max(np.abs(r[:, 6] - exact)) < 3e-4
+
+
+def test_tiles_rejected_where_invalid(cuda):
+    for kw in (dict(L=10, tile_groups=2), dict(L=128, tile_groups=2), dict(L=64, tile_groups=3),
+               dict(L=64, coding="ssc", tile_groups=2)):
+        with pytest.raises(pa.PaisingError):
+            pa.Engine(**{"coding": "msc", "R": 1000, **kw})
+
+
+def test_autotune_keeps_reference_results(cuda):
+    """pa_autotune times the tile sizes on the handle's own populations and
+    rebuilds the graph; the run that follows reproduces the reference."""
+    with pa.Engine(L=16, R=1000, sweeps=10, seed=100, coding="msc", rng="reference", weights="fp64") as e:
+        tiles = e.autotune()
+        assert tiles[0] in (1, 2, 4, 8)
+        e.run()
+        compare_rows(e.rows(0), load_dat("ref/inj_MSC_L16_R1000_t10_d0.005_s100.dat"), rtol=2e-10)
+        with pytest.raises(pa.PaisingError) as ei:
+            e.autotune()
+        assert ei.value.status == 5
+
+
+def test_autotune_batch(cuda, oracle):
+    """A batch of several lattice sizes: one choice per size, every
+    population still equal to the oracle's run of it."""
+    pops = [dict(L=16, R=3000, sweeps=3, dbeta=0.1, seed=5), dict(L=32, R=2000, sweeps=2, dbeta=0.2, seed=6),
+            dict(L=16, R=500, sweeps=3, dbeta=0.1, seed=8), dict(L=64, R=700, sweeps=2, dbeta=0.25, seed=9)]
+    with pa.Engine.batch(pops, coding="msc", rng="reference", weights="fp64") as e:
+        tiles = e.autotune()
+        assert tiles[0] == tiles[2] and all(t in (1, 2, 4, 8) for t in tiles)
+        e.run()
+        for k, p in enumerate(pops):
+            ref, _ = oracle.anneal("msc", p["L"], p["R"], p["sweeps"], p["dbeta"], 1.0, 1, p["seed"])
+            compare_rows(e.rows(k), ref[0], rtol=1e-9)
