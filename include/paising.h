@@ -74,6 +74,13 @@ typedef struct pa_config {
                         cluster of that many CTAs per group (needed for L > 128) */
   int tile_groups;   /* MSC groups stacked into one work unit of the one-CTA sweep: 0 automatic,
                         1, 2, 4 or 8 (more than 1 needs L % 4 == 0 and at most 44 KB per tile) */
+  int adaptive;      /* 1: adaptive temperature step, the reference's AdaptiveStep build
+                        (PAisingSSC.cu:23,306-334,644-660): after every temperature the next step is
+                        the largest (grown by 1.1x, else bisected) whose energy-histogram overlap lies
+                        in [min_overlap, max_overlap); dbeta is the first step.  Runs after the first
+                        reuse the first run's schedule, as in the reference. */
+  double min_overlap; /* MinOverlap (PAisingSSC.cu:42); 0 selects 0.85 */
+  double max_overlap; /* MaxOverlap (PAisingSSC.cu:43); 0 selects 0.87 */
 } pa_config;
 
 /* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */

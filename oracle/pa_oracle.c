@@ -416,8 +416,62 @@ void or_msc_resample(const uint32_t* old, const int32_t* E_old, int L, int rg_ol
  * stops each run after that many temperatures (bounded CPU samples).
  * Returns the number of rows per run, or -1 on error.  *attempts receives
  * sweeps * N * sum_i R_i (the reference's spin-flip count, PAisingSSC.cu:632). */
+/* Histogram overlap of inverse-temperature step dB for the current population
+ * (CalcOverlap + HistogramOverlap, PAisingSSC.cu:308-334, PAisingMSC.cu:464-500):
+ * lnQ from the Q sum around Emean, then the mean of min(1, Rinit/R exp(-dB E - lnQ)). */
+static double overlap(int msc, const int32_t* E, const uint8_t* act, int rg, int R, int Rinit, double dB,
+                      double Emean) {
+    const double q = msc ? or_msc_q(E, act, rg, dB, Emean) : or_ssc_q(E, R, dB, Emean);
+    const double lnQ = -dB * Emean + log(q) - log((double)R);
+    const int n = msc ? rg * MSB : R;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (!msc || act[i]) s += fmin(1.0, ((double)Rinit) / R * exp(-dB * (double)E[i] - lnQ));
+    return s / R;
+}
+
+/* Next inverse-temperature step of the AdaptiveStep build (PAisingSSC.cu:644-660):
+ * grow the previous step by 1.1x while the overlap is >= MaxOverlap and beta
+ * stays below Bfin; otherwise bisect in (0, step) until MinOverlap <= overlap
+ * < MaxOverlap (at most 200 halvings; the reference does not bound them);
+ * clamp the last step onto Bfin. */
+static double next_step(int msc, const int32_t* E, const uint8_t* act, int rg, int R, int Rinit, double Emean,
+                        double Bprev, double Bfin, double deltaBeta, double minov, double maxov) {
+    double ov, dBmin = 0, dBmax = deltaBeta, dBmean;
+    for (;;) {
+        ov = overlap(msc, E, act, rg, R, Rinit, dBmax, Emean);
+        if (ov >= maxov && Bprev + dBmax < Bfin) dBmax *= 1.1; else break;
+    }
+    if (ov >= minov) {
+        dBmean = dBmax;
+    } else {
+        for (int it = 0;; ++it) {
+            dBmean = 0.5 * (dBmin + dBmax);
+            ov = overlap(msc, E, act, rg, R, Rinit, dBmean, Emean);
+            if (it + 1 >= 200) break;
+            if (ov < minov) dBmax = dBmean;
+            else if (ov >= maxov) dBmin = dBmean;
+            else break;
+        }
+    }
+    return (Bprev < Bfin && Bprev + dBmean > Bfin) ? Bfin - Bprev : dBmean;
+}
+
+int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+               int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
+               double* attempts);
+
 int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
               int max_steps, double* rows, int max_rows, double* attempts) {
+    return or_anneal2(msc, L, Rinit, sweeps, dBinit, Bfin, runs, seed, max_steps, 0, 0.0, 0.0, rows, max_rows,
+                      attempts);
+}
+
+/* or_anneal with the adaptive temperature step (adaptive = 1): the first run
+ * chooses its schedule, later runs replay it (PAisingSSC.cu:644,662). */
+int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+               int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
+               double* attempts) {
     int N = L * L;
     const int nBmax = 10000;
     double* B = (double*)calloc(nBmax, sizeof(double));
@@ -462,6 +516,7 @@ int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin,
             or_msc_energy(wd, L, rg, Ev, Mm);
         }
         int i = 1;
+        double deltaBeta = dBinit;
         B[1] = B[0] + dBinit;
         while (B[i] <= Bfin) {
             double dB = B[i] - B[i - 1];
@@ -517,7 +572,13 @@ int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin,
             ++i;
             if (i >= nBmax || i > max_rows - 1) { ret = -1; break; }
             if (max_steps > 0 && i > max_steps) { B[i] = Bfin + 1.0; break; }
-            B[i] = B[i - 1] + dBinit;
+            if (!adaptive) {
+                B[i] = B[i - 1] + dBinit;
+            } else if (r == 0) {
+                deltaBeta = next_step(msc, Ev, act, rg, Rn[i - 1], Rinit, Emean, B[i - 1], Bfin, deltaBeta, minov,
+                                      maxov);
+                B[i] = B[i - 1] + deltaBeta;
+            }  /* later runs: B[i] as the first run left it */
         }
         nB = i;
         if (rows && ret == 0) {

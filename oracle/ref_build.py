@@ -12,7 +12,10 @@ changes are the ones CUDA 13 forces or the comparison needs:
   reference, so one binary is built per lattice size;
 * the ``inj`` variants are compiled with ``-include inj_shim.cuh``, which swaps
   cuRAND's Philox state for the injected stream H (see inj_stream.h).  The
-  ``curand`` variants keep cuRAND and are the reference's own GPU build.
+  ``curand`` variants keep cuRAND and are the reference's own GPU build;
+* the ``inj_adaptive`` variants (L=16) also define ``AdaptiveStep``, the
+  reference's compile-time switch for its adaptive temperature step
+  (PAisingSSC.cu:23, PAisingMSC.cu:23).
 
 Step 1 (patch) needs the reference checkout and runs in the build container;
 step 2 (nvcc) runs wherever the patched sources are, e.g. on the GPU host,
@@ -91,8 +94,10 @@ def _compile(src: str, variant: str) -> str:
     base = os.path.splitext(os.path.basename(src))[0]
     out = os.path.join(BIN_OUT, f"{base}_{variant}")
     cmd = ["nvcc", "-O3", ARCH, "-w", "-o", out, src]
-    if variant == "inj":
+    if variant.startswith("inj"):
         cmd[1:1] = ["-include", os.path.join(SRC_OUT, "inj_shim.cuh"), "-I", SRC_OUT]
+    if variant.endswith("adaptive"):  # the reference's AdaptiveStep build (its line 23 switch)
+        cmd[1:1] = ["-DAdaptiveStep"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {out}:\n{r.stderr[-2000:]}")
@@ -103,6 +108,7 @@ def compile_all(jobs: int) -> list[str]:
     os.makedirs(BIN_OUT, exist_ok=True)
     srcs = sorted(f for f in os.listdir(SRC_OUT) if f.endswith(".cu") and f.startswith("PAising"))
     tasks = [(os.path.join(SRC_OUT, s), v) for s in srcs for v in ("inj", "curand")]
+    tasks += [(os.path.join(SRC_OUT, s), "inj_adaptive") for s in srcs if s.endswith("_L16.cu")]
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         return list(ex.map(lambda a: _compile(*a), tasks))
 

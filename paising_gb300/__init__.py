@@ -50,7 +50,8 @@ class Config(ctypes.Structure):
                 ("beta_final", ctypes.c_double), ("runs", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("coding", ctypes.c_int), ("rng_mode", ctypes.c_int), ("weights", ctypes.c_int),
                 ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double),
-                ("sweep_variant", ctypes.c_int), ("tile_groups", ctypes.c_int)]
+                ("sweep_variant", ctypes.c_int), ("tile_groups", ctypes.c_int), ("adaptive", ctypes.c_int),
+                ("min_overlap", ctypes.c_double), ("max_overlap", ctypes.c_double)]
 
 
 class Row(ctypes.Structure):
@@ -130,16 +131,19 @@ _W = {"fp32": WEIGHTS_FP32, "fp64": WEIGHTS_FP64, WEIGHTS_FP32: WEIGHTS_FP32, WE
 
 def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, seed=1, coding="ssc",
                 rng="native", weights="fp32", graph=True, device=0, capacity=1.25, sweep_variant=0,
-                tile_groups=0) -> Config:
+                tile_groups=0, adaptive=False, min_overlap=0.0, max_overlap=0.0) -> Config:
     """sweep_variant: CTAs per MSC group in the sweep kernel (0 automatic,
     1 one CTA, 2 or 4 a thread-block cluster); tile_groups: MSC groups per
-    work unit of the one-CTA sweep (0 automatic, 1, 2, 4 or 8)."""
+    work unit of the one-CTA sweep (0 automatic, 1, 2, 4 or 8); adaptive:
+    the reference's adaptive temperature step with histogram overlap in
+    [min_overlap, max_overlap) (0 selects the reference's 0.85 / 0.87)."""
     c = Config()
     _check(lib().pa_config_init(ctypes.byref(c)))
     c.L, c.R, c.sweeps, c.dbeta, c.beta_final, c.runs = int(L), int(R), int(sweeps), float(dbeta), float(beta_final), int(runs)
     c.seed, c.coding, c.rng_mode, c.weights = int(seed), _CODING[coding], _RNG[rng], _W[weights]
     c.graph, c.device, c.capacity = int(bool(graph)), int(device), float(capacity)
     c.sweep_variant, c.tile_groups = int(sweep_variant), int(tile_groups)
+    c.adaptive, c.min_overlap, c.max_overlap = int(bool(adaptive)), float(min_overlap), float(max_overlap)
     return c
 
 

@@ -5,7 +5,10 @@
 // C ABI in include/paising.h.  L is a compile-time #define in the reference
 // (PAisingSSC.cu:27); here it is the extra option -L.  Further extensions:
 // -c ssc|msc (coding), -m native|reference (random stream), -w fp32|fp64
-// (resampling weights), -g 0|1 (host-stepped or graph), -D device.
+// (resampling weights), -g 0|1 (host-stepped or graph), -D device, -a (the
+// adaptive temperature step of the reference's AdaptiveStep build, with its
+// output directory ./data%s_L%d_R%d_EqSw%d/, PAisingSSC.cu:406-410), -T (time
+// the MSC tile sizes before the run, pa_autotune).
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -36,7 +39,9 @@ static void usage(const char* prog) {
       " -m native|reference( random stream, default native )\n"
       " -w fp32|fp64       ( resampling weights, default fp32 )\n"
       " -g 0|1             ( 1: one CUDA graph per run (default), 0: host steps each temperature )\n"
-      " -D device          ( CUDA device ordinal )\n",
+      " -D device          ( CUDA device ordinal )\n"
+      " -a                 ( adaptive temperature step, MinOverlap 0.85, MaxOverlap 0.87 )\n"
+      " -T                 ( autotune the MSC sweep's tile sizes before the run )\n",
       prog);
 }
 
@@ -46,10 +51,11 @@ int main(int argc, char** argv) {
   c.coding = PA_CODING_MSC;
   c.seed = (uint64_t)time(nullptr);  // RNGseed = time(NULL) (PAisingSSC.cu:31)
   int precision = 11;
+  bool tune = false;
   std::string dir;
   int opt;
   opterr = 0;
-  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:?")) != -1) {
+  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aT?")) != -1) {
     int i;
     double f;
     switch (opt) {  // same acceptance rules as PAisingSSC.cu:390-398
@@ -67,6 +73,8 @@ int main(int argc, char** argv) {
       case 'w': c.weights = std::strcmp(optarg, "fp64") == 0 ? PA_WEIGHTS_FP64 : PA_WEIGHTS_FP32; break;
       case 'g': c.graph = std::atoi(optarg) != 0; break;
       case 'D': c.device = std::atoi(optarg); break;
+      case 'a': c.adaptive = 1; break;
+      case 'T': tune = true; break;
       default:
         if (optopt && optopt != '?') std::printf("illegal option -- %c\n", optopt);
         usage(argv[0]);
@@ -78,9 +86,10 @@ int main(int argc, char** argv) {
     return 1;
   }
   const char* tag = c.coding == PA_CODING_MSC ? "MSC" : "SSC";
-  if (dir.empty()) {  // ./dataSSC_L%d_R%d_EqSw%d_dB%f/ (PAisingSSC.cu:409)
+  if (dir.empty()) {  // ./dataSSC_L%d_R%d_EqSw%d[_dB%f]/ (PAisingSSC.cu:406-410)
     char buf[256];
-    std::snprintf(buf, sizeof(buf), "./data%s_L%d_R%d_EqSw%d_dB%f/", tag, c.L, c.R, c.sweeps, c.dbeta);
+    if (c.adaptive) std::snprintf(buf, sizeof(buf), "./data%s_L%d_R%d_EqSw%d/", tag, c.L, c.R, c.sweeps);
+    else std::snprintf(buf, sizeof(buf), "./data%s_L%d_R%d_EqSw%d_dB%f/", tag, c.L, c.R, c.sweeps, c.dbeta);
     dir = buf;
   }
   mkdir(dir.c_str(), 0777);
@@ -97,7 +106,8 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "Error: %s (%s)\n", pa_status_string(st), pa_last_error(nullptr));
     return 1;
   }
-  st = pa_run(h);
+  if (tune) st = pa_autotune(h, nullptr, 0);
+  if (!st) st = pa_run(h);
   if (st) {
     std::fprintf(stderr, "Error: %s (%s)\n", pa_status_string(st), pa_last_error(h));
     pa_destroy(h);

@@ -26,6 +26,7 @@
 #include "pa_device.cuh"
 #include "pa_error.h"
 #include "pa_kernels.h"
+#include "pa_thresholds.h"
 
 using namespace pa;
 
@@ -48,26 +49,7 @@ struct DevBuf {
   }
 };
 
-constexpr int kNBmax = 10000;  // nBmax, PAisingSSC.cu:57
-
-double ceil_thr(double p) { return std::ceil(4294967296.0 * p); }
-
-// per-temperature acceptance thresholds (host exp, like the reference)
-void thresholds(double beta, uint32_t* t) {
-  // SSC Boltzmann table boltz[idxT0 + 2 idxT1] = min(1, exp(-2 s sum_nn beta))
-  // (PAisingSSC.cu:512-516); a reference uniform (H+1)/2^32 is below p iff
-  // H < ceil(2^32 p) - 1.
-  for (int i0 = 0; i0 <= 1; ++i0)
-    for (int i1 = 0; i1 <= 4; ++i1) {
-      double p = std::exp(-2 * (2 * i0 - 1) * (2 * i1 - 4) * beta);
-      if (p > 1.0) p = 1.0;
-      t[i0 + 2 * i1] = (uint32_t)(ceil_thr(p) - 1.0);
-    }
-  // MSC integer thresholds (PAisingMSC.cu:674-675), also the native SSC ones
-  const double t4 = ceil_thr(std::exp(-4 * beta)), t8 = ceil_thr(std::exp(-8 * beta));
-  t[10] = t4 >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t4;
-  t[11] = t8 >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t8;
-}
+constexpr double kMinOverlap = 0.85, kMaxOverlap = 0.87;  // PAisingSSC.cu:42-43
 
 std::vector<double> schedule(double dbeta, double bfin) {
   std::vector<double> b{0.0};
@@ -89,9 +71,10 @@ struct PopHost {
   pa_config cfg{};
   PopDev h{};
   SweepGeom geom{};
-  std::vector<double> betas;
+  std::vector<double> betas;  // the schedule (adaptive: its first two temperatures)
   std::vector<uint32_t> thr;
-  int nsteps = 0;
+  int nsteps = 0;             // steps of the schedule (adaptive: the most the buffers allow)
+  int cap = 0;                // rows the device buffers hold
   int user_index = 0;
 };
 
@@ -105,6 +88,10 @@ struct pa_handle {
   int max_steps = 0;
   int rblocks = 1;
   int cs = 1;  // CTAs per MSC group in the sweep (1, or a cluster of 2 / 4)
+  bool adaptive = false;  // some population chooses its temperatures as it goes
+  static constexpr int kChunk = 16;  // adaptive runs: steps per graph launch between host checks
+  cudaGraph_t chunk_t = nullptr;
+  cudaGraphExec_t chunk_exec = nullptr;
   unsigned long long stream_seed = 0;  // key of the native sweep stream (seed of the first population)
   SweepLaunch sweep{};
   PopDev* d_pops = nullptr;
@@ -118,6 +105,7 @@ struct pa_handle {
   std::vector<std::vector<double>> rows;
   int sets_done = 0;
   bool ran = false;  // pa_run has been called
+  int runs_done = 0;  // completed runs: the first one chooses adaptive schedules, the others replay them
   double ms = 0.0, attempts = 0.0;
   std::string err;
   std::vector<void*> staging;  // per population: device copy of a caller-supplied initial population
@@ -182,12 +170,78 @@ struct pa_handle {
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 0, stream); })) != cudaSuccess) return e;
     e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return sweep_launch(0); });
     if (e != cudaSuccess) return e;
-    return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+    e = launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+    if (e != cudaSuccess || !adaptive) return e;
+    return launch("adapt", [&] { return launch_adapt(d_pops, npop, stream); });
   }
 
+  // A whole run as one launch sequence (fixed schedules: the graph of a run).
   cudaError_t enqueue_run() {
     cudaError_t e = enqueue_init();
     for (int i = 1; i <= max_steps && e == cudaSuccess; ++i) e = enqueue_step();
+    return e;
+  }
+
+  // Adaptive schedules end when the device says so: every population has
+  // passed its last step or stopped with an error.
+  cudaError_t all_done(bool* done) {
+    std::vector<PopDev> st(npop);
+    cudaError_t e = cudaMemcpyAsync(st.data(), d_pops, sizeof(PopDev) * npop, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    *done = true;
+    for (const auto& s : st)
+      if (!s.error && s.step <= s.nsteps) *done = false;
+    return e;
+  }
+
+  // The device values of the adaptive-step switch and step bound that a run
+  // starts from: the handle's first run chooses its temperatures, every later
+  // run (of the same or a later pa_run) replays that schedule, as the
+  // reference's runs after the first do (PAisingSSC.cu:644,662).
+  cudaError_t set_adaptive(bool first_run) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < npop && e == cudaSuccess; ++k) {
+      if (!pops[k].cfg.adaptive) continue;
+      const int on = first_run ? 1 : 0;
+      e = cudaMemcpy(&d_pops[k].adaptive, &on, sizeof(int), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess && first_run)
+        e = cudaMemcpy(&d_pops[k].nsteps, &pops[k].nsteps, sizeof(int), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess && first_run)
+        e = cudaMemcpy(&d_pops[k].dbeta_cur, &pops[k].cfg.dbeta, sizeof(double), cudaMemcpyHostToDevice);
+    }
+    return e;
+  }
+
+  // One run, on the stream: graph replays or host-stepped launches.
+  cudaError_t run_once() {
+    cudaError_t e;
+    if (graph) {
+      e = cudaGraphLaunch(exec, stream);
+      while (adaptive && e == cudaSuccess) {
+        bool done = false;
+        e = all_done(&done);
+        if (e != cudaSuccess || done) break;
+        e = cudaGraphLaunch(chunk_exec, stream);
+      }
+      return e;
+    }
+    e = enqueue_init();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    for (int i = 1; i <= max_steps && e == cudaSuccess; ++i) {
+      e = enqueue_step();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+      // the host reads every step's result, like the reference's host loop
+      for (int k = 0; k < npop && e == cudaSuccess; ++k) {
+        if (i >= pops[k].cap) continue;
+        double row[kRowCols];
+        e = cudaMemcpy(row, pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
+      }
+      if (adaptive && e == cudaSuccess) {
+        bool done = false;
+        e = all_done(&done);
+        if (done) break;
+      }
+    }
     return e;
   }
 
@@ -201,15 +255,26 @@ struct pa_handle {
     if (e != cudaSuccess || !graph) return e;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph_t) cudaGraphDestroy(graph_t);
-    exec = nullptr;
-    graph_t = nullptr;
-    e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    cudaError_t e1 = enqueue_run();
-    cudaError_t e2 = cudaStreamEndCapture(stream, &graph_t);
-    if (e1 != cudaSuccess) return e1;
-    if (e2 != cudaSuccess) return e2;
-    return cudaGraphInstantiate(&exec, graph_t, 0);
+    if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    if (chunk_t) cudaGraphDestroy(chunk_t);
+    exec = chunk_exec = nullptr;
+    graph_t = chunk_t = nullptr;
+    // fixed schedules: one graph per run; adaptive: the set-up plus a first
+    // chunk of steps, then chunks of kChunk steps until the device is done
+    auto capture = [&](int steps, bool with_init, cudaGraph_t* g, cudaGraphExec_t* x) {
+      cudaError_t c = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+      if (c != cudaSuccess) return c;
+      cudaError_t e1 = with_init ? enqueue_init() : cudaSuccess;
+      for (int i = 1; i <= steps && e1 == cudaSuccess; ++i) e1 = enqueue_step();
+      cudaError_t e2 = cudaStreamEndCapture(stream, g);
+      if (e1 != cudaSuccess) return e1;
+      if (e2 != cudaSuccess) return e2;
+      return cudaGraphInstantiate(x, *g, 0);
+    };
+    if (!adaptive) return capture(max_steps, true, &graph_t, &exec);
+    e = capture(kChunk, true, &graph_t, &exec);
+    if (e == cudaSuccess) e = capture(kChunk, false, &chunk_t, &chunk_exec);
+    return e;
   }
 
   cudaError_t upload_pops(const std::vector<PopDev>& hp) {
@@ -255,6 +320,8 @@ struct pa_handle {
       if (p) cudaFree(p);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph_t) cudaGraphDestroy(graph_t);
+    if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    if (chunk_t) cudaGraphDestroy(chunk_t);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -295,7 +362,12 @@ int validate(const pa_config& c) {
   } else if (!ssc_geom(c.L, &g)) {
     return bad("SSC needs L % 8 == 0, 8 <= L <= 256");
   }
-  if ((int)schedule(c.dbeta, c.beta_final).size() > kNBmax - 1) {
+  if (c.adaptive != 0 && c.adaptive != 1) return bad("adaptive must be 0 or 1");
+  if (c.adaptive) {
+    const double lo = c.min_overlap > 0 ? c.min_overlap : kMinOverlap;
+    const double hi = c.max_overlap > 0 ? c.max_overlap : kMaxOverlap;
+    if (!(lo > 0 && lo < hi && hi < 1)) return bad("adaptive step needs 0 < min_overlap < max_overlap < 1");
+  } else if ((int)schedule(c.dbeta, c.beta_final).size() > kNBmax - 1) {
     pa::g_last_error = "number of temperature steps exceeds nBmax=10000";
     return PA_ERR_TOO_MANY_STEPS;
   }
@@ -346,8 +418,19 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
     if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +
                                           std::to_string(H->cs) + " CTAs");
-    P.betas = schedule(P.cfg.dbeta, P.cfg.beta_final);
-    P.nsteps = (int)P.betas.size() - 1;
+    if (P.cfg.adaptive) {
+      // the first step is dbeta; the device chooses the others (at most the
+      // rows nBmax allows) and ends the schedule at beta_final
+      P.betas = {0.0};
+      if (P.cfg.dbeta <= P.cfg.beta_final) P.betas.push_back(P.cfg.dbeta);
+      P.nsteps = P.betas.size() > 1 ? kNBmax - 1 : 0;
+      P.cap = kNBmax;
+      H->adaptive = true;
+    } else {
+      P.betas = schedule(P.cfg.dbeta, P.cfg.beta_final);
+      P.nsteps = (int)P.betas.size() - 1;
+      P.cap = (int)P.betas.size();
+    }
     P.thr.assign(P.betas.size() * kThrPerStep, 0u);
     for (size_t i = 0; i < P.betas.size(); ++i) thresholds(P.betas[i], &P.thr[i * kThrPerStep]);
   }
@@ -413,14 +496,22 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     chk(B.alloc(&h.qpart_d, kResBlocksMax));
     chk(B.alloc(&h.qpart_f, 2 * kResBlocksMax));
     double* rows = nullptr;
-    chk(B.alloc(&rows, P.betas.size() * kRowCols));
+    chk(B.alloc(&rows, (size_t)P.cap * kRowCols));
     h.rows = rows;
     double* bet = nullptr;
-    chk(B.alloc(&bet, P.betas.size()));
+    chk(B.alloc(&bet, (size_t)P.cap));
     h.betas = bet;
     uint32_t* th = nullptr;
-    chk(B.alloc(&th, P.thr.size()));
+    chk(B.alloc(&th, (size_t)P.cap * kThrPerStep));
     h.thr = th;
+    if (c.adaptive) {
+      chk(B.alloc(&h.hist, (size_t)N + 1));
+      h.adaptive = 1;
+      h.dbeta_cur = c.dbeta;  // deltaBeta = dBinit (PAisingSSC.cu:508)
+      h.min_ov = c.min_overlap > 0 ? c.min_overlap : kMinOverlap;
+      h.max_ov = c.max_overlap > 0 ? c.max_overlap : kMaxOverlap;
+      h.beta_fin = c.beta_final;
+    }
     if (e != cudaSuccess) break;
     chk(cudaMemcpy(bet, P.betas.data(), P.betas.size() * sizeof(double), cudaMemcpyHostToDevice));
     chk(cudaMemcpy(th, P.thr.data(), P.thr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -506,8 +597,10 @@ int pa_create(const pa_config* cfg, pa_handle** out) {
   if (rc) return rc;
   // independent runs: concurrent populations with disjoint native streams; with
   // the reference stream they must run one after the other, because each run
-  // continues the subsequence counter of the previous one (PAisingSSC.cu:481-486)
-  if (cfg->rng_mode == PA_RNG_REFERENCE || cfg->runs == 1) {
+  // continues the subsequence counter of the previous one (PAisingSSC.cu:481-486);
+  // with the adaptive step too, because later runs replay the first run's
+  // schedule (PAisingSSC.cu:644,662)
+  if (cfg->rng_mode == PA_RNG_REFERENCE || cfg->runs == 1 || cfg->adaptive) {
     pa_config c = *cfg;
     return build_handle({c}, cfg->runs, out);
   }
@@ -549,45 +642,50 @@ int pa_run(pa_handle* H) {
   int status = PA_OK;
   std::vector<PopDev> back(H->npop);
   for (int r = 0; r < H->seq_runs && status == PA_OK; ++r) {
-    if (H->graph) {
-      e = cudaGraphLaunch(H->exec, H->stream);
-      if (e != cudaSuccess) return H->cuda_fail(e, "graph launch");
-    } else {
-      e = H->enqueue_init();
-      if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-      for (int i = 1; i <= H->max_steps && e == cudaSuccess; ++i) {
-        e = H->enqueue_step();
-        if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-        for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
-          if (i > H->pops[k].nsteps) continue;
-          double row[kRowCols];
-          e = cudaMemcpy(row, H->pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
-        }
-      }
-      if (e != cudaSuccess) return H->cuda_fail(e, "plain step");
+    if (H->adaptive) {
+      e = H->set_adaptive(H->runs_done == 0);
+      if (e != cudaSuccess) return H->cuda_fail(e, "adaptive set-up");
     }
-    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
-      const PopHost& P = H->pops[k];
-      std::vector<double>& dst = H->rows[(size_t)r * H->npop + P.user_index];
-      dst.assign(P.betas.size() * kRowCols, 0.0);
-      e = cudaMemcpyAsync(dst.data(), P.h.rows, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
-    }
+    e = H->run_once();
+    if (e != cudaSuccess) return H->cuda_fail(e, H->graph ? "graph launch" : "plain step");
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(back.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+      // rows of the schedule the run followed (adaptive: as long as the device made it)
+      const PopHost& P = H->pops[k];
+      const int nrows = std::min(back[k].nsteps + 1, P.cap);
+      std::vector<double>& dst = H->rows[(size_t)r * H->npop + P.user_index];
+      dst.assign((size_t)nrows * kRowCols, 0.0);
+      e = cudaMemcpyAsync(dst.data(), P.h.rows, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     if (e != cudaSuccess) return H->cuda_fail(e, "run");
     for (int k = 0; k < H->npop; ++k) {
       if (back[k].error) {
-        status = back[k].error == 2 ? PA_ERR_EXTINCT : PA_ERR_CAPACITY;
-        H->err = back[k].error == 2 ? "resampling produced an empty population"
-                                    : "population exceeded its buffer capacity (raise pa_config.capacity)";
+        switch (back[k].error) {
+          case kErrExtinct:
+            status = PA_ERR_EXTINCT;
+            H->err = "resampling produced an empty population";
+            break;
+          case kErrTooManySteps:
+            status = PA_ERR_TOO_MANY_STEPS;
+            H->err = "number of temperature steps exceeds nBmax=10000 (raise R or lower min_overlap)";
+            break;
+          default:
+            status = PA_ERR_CAPACITY;
+            H->err = "population exceeded its buffer capacity (raise pa_config.capacity)";
+        }
       }
       const PopHost& P = H->pops[k];
       const std::vector<double>& rw = H->rows[(size_t)r * H->npop + P.user_index];
-      for (size_t i = 1; i < P.betas.size(); ++i)
+      for (size_t i = 1; i < rw.size() / kRowCols; ++i)
         H->attempts += (double)P.cfg.sweeps * (double)P.h.N * rw[i * kRowCols + 8];
     }
-    if (status == PA_OK) H->sets_done = (r + 1) * H->npop;
+    if (status == PA_OK) {
+      H->sets_done = (r + 1) * H->npop;
+      ++H->runs_done;
+    }
   }
   e = cudaEventRecord(H->ev1, H->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(H->ev1);
@@ -651,7 +749,11 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
 int pa_num_rows(const pa_handle* H, int* n) {
   if (!H || !n) return PA_ERR_ARG;
   int m = 0;
-  for (const auto& P : H->pops) m = std::max(m, (int)P.betas.size());
+  if (H->sets_done > 0) {  // rows of the last run (adaptive schedules are known only then)
+    for (int s = 0; s < H->sets_done; ++s) m = std::max(m, (int)(H->rows[s].size() / kRowCols));
+  } else {
+    for (const auto& P : H->pops) m = std::max(m, P.cfg.adaptive ? P.cap : (int)P.betas.size());
+  }
   *n = m;
   return PA_OK;
 }

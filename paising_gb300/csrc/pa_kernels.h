@@ -88,5 +88,7 @@ cudaError_t launch_msc_cluster_sweep(int cs, BatchDev* b, int rng_mode, int ener
 // Per-run / per-step bookkeeping.
 cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s);
+// Adaptive populations: choose the next temperature (after launch_finish_step).
+cudaError_t launch_adapt(PopDev* pops, int npop, cudaStream_t s);
 
 }  // namespace pa

@@ -125,7 +125,7 @@ int pa_resample_plan_noalloc(const int32_t* E, const uint8_t* active, int coding
   h.blk_off = reinterpret_cast<uint32_t*>(base + kOffBlkOff);
   h.qpart_d = reinterpret_cast<double*>(base + kOffQd);
   h.qpart_f = reinterpret_cast<float*>(base + kOffQf);
-  h.betas = reinterpret_cast<const double*>(base + kOffBetas);
+  h.betas = reinterpret_cast<double*>(base + kOffBetas);
   PopDev* st = reinterpret_cast<PopDev*>(base + kOffState);
 
   const int blocks = res_blocks(units);

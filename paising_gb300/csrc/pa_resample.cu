@@ -24,6 +24,7 @@
 
 #include "pa_device.cuh"
 #include "pa_kernels.h"
+#include "pa_thresholds.h"
 
 namespace pa {
 
@@ -326,6 +327,89 @@ __global__ void finish_step_kernel(PopDev* pops) {
   st->Emin_acc = INT_MAX;
 }
 
+// ------------------------------------------------- adaptive temperature step
+// After temperature step-1 (>= 1) of an adaptive population: the next beta,
+// as the reference's AdaptiveStep build chooses it (PAisingSSC.cu:644-660):
+// starting from the previous step, grow it by 1.1x while the energy-histogram
+// overlap stays >= MaxOverlap (and beta stays below beta_final), otherwise
+// bisect between 0 and the step until MinOverlap <= overlap < MaxOverlap,
+// and clamp the last step onto beta_final.  The overlap of step dB
+// (CalcOverlap, PAisingSSC.cu:316-334) is
+//   lnQ = -dB Emean + ln sum_i exp(-dB (E_i - Emean)) - ln R,
+//   overlap = (1/R) sum_i min(1, Rinit/R exp(-dB E_i - lnQ)),
+// evaluated here over the histogram of the population's energies (energies
+// are -2N + 4k), so each evaluation costs a pass over at most N+1 bins
+// instead of R replicas; one CTA per population, FP64 throughout.
+constexpr int kAdaptThreads = 1024;
+constexpr int kMaxBisect = 200;  // the reference bisects without a bound
+
+__global__ void __launch_bounds__(kAdaptThreads) adapt_kernel(PopDev* pops) {
+  __shared__ double s_red[32];
+  PopDev* st = pops + blockIdx.x;
+  const int step = st->step;  // index of the temperature to choose (finish_step has advanced it)
+  if (!st->adaptive || step < 2 || step > st->nsteps || st->error) return;
+  const int N = st->N, nb = N + 1, R = st->R_cur;
+  uint32_t* hist = st->hist;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0u;
+  __syncthreads();
+  const bool msc = st->coding == kMSC;
+  const int units = pop_units(st, R);
+  const uint8_t* act = msc ? st->active[st->parity] : nullptr;
+  for (int i = threadIdx.x; i < units; i += blockDim.x)
+    if (!msc || act[i]) atomicAdd(&hist[(st->E[i] + 2 * N) >> 2], 1u);
+  __syncthreads();
+
+  const double Em = st->Emean, Rd = (double)R, Rinit = (double)st->Rinit;
+  auto overlap = [&](double dB) {
+    double q = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      const uint32_t c = hist[i];
+      if (c) q += (double)c * exp(-dB * ((double)(4 * i - 2 * N) - Em));
+    }
+    q = block_sum(q, s_red);
+    const double lnQ = -dB * Em + log(q) - log(Rd);
+    double o = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      const uint32_t c = hist[i];
+      if (c) o += (double)c * fmin(1.0, Rinit / Rd * exp(-dB * (double)(4 * i - 2 * N) - lnQ));
+    }
+    return block_sum(o, s_red) / Rd;
+  };
+
+  const double Bp = st->betas[step - 1], Bfin = st->beta_fin, lo = st->min_ov, hi = st->max_ov;
+  double dBmin = 0.0, dBmax = st->dbeta_cur, dBmean, ov;
+  for (;;) {
+    ov = overlap(dBmax);
+    if (ov >= hi && Bp + dBmax < Bfin) dBmax *= 1.1;
+    else break;
+  }
+  if (ov >= lo) {
+    dBmean = dBmax;
+  } else {
+    for (int it = 0;; ++it) {
+      dBmean = 0.5 * (dBmin + dBmax);
+      ov = overlap(dBmean);
+      if (it + 1 >= kMaxBisect) break;
+      if (ov < lo) dBmax = dBmean;
+      else if (ov >= hi) dBmin = dBmean;
+      else break;
+    }
+  }
+  const double dB = (Bp < Bfin && Bp + dBmean > Bfin) ? Bfin - Bp : dBmean;
+  const double Bn = Bp + dB;
+  if (threadIdx.x == 0) {
+    st->dbeta_cur = dB;
+    if (!(Bn <= Bfin)) {
+      st->nsteps = step - 1;  // the schedule ends with the temperature just computed
+    } else if (step >= kNBmax - 1) {
+      st->error = kErrTooManySteps;  // PAisingSSC.cu:634-641
+    } else {
+      st->betas[step] = Bn;
+      thresholds(Bn, st->thr + (size_t)step * kThrPerStep);
+    }
+  }
+}
+
 // ------------------------------------------------------------ launchers
 int res_blocks(long long units) {
   long long b = (units + kResThreads - 1) / kResThreads;
@@ -390,6 +474,11 @@ cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s) {
 
 cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s) {
   finish_step_kernel<<<npop, 1, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adapt(PopDev* pops, int npop, cudaStream_t s) {
+  adapt_kernel<<<npop, kAdaptThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@
 #include "pa_device.cuh"
 #include "pa_error.h"
 #include "pa_kernels.h"
+#include "pa_thresholds.h"
 
 using namespace pa;
 
@@ -55,17 +56,7 @@ struct Scratch {
   }
 };
 
-void fill_thr(double beta, uint32_t* t) {
-  for (int i0 = 0; i0 <= 1; ++i0)
-    for (int i1 = 0; i1 <= 4; ++i1) {
-      double p = std::exp(-2 * (2 * i0 - 1) * (2 * i1 - 4) * beta);
-      if (p > 1.0) p = 1.0;
-      t[i0 + 2 * i1] = (uint32_t)(std::ceil(4294967296.0 * p) - 1.0);
-    }
-  const double t4 = std::ceil(4294967296.0 * std::exp(-4 * beta)), t8 = std::ceil(4294967296.0 * std::exp(-8 * beta));
-  t[10] = t4 >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t4;
-  t[11] = t8 >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t8;
-}
+void fill_thr(double beta, uint32_t* t) { thresholds(beta, t); }
 
 // A one-population state at temperature step 1 of a one-step schedule.
 PopDev base_state(int coding, int L) {

@@ -47,8 +47,9 @@ struct PopDev {
   double* qpart_d;     // [kResBlocksMax] FP64 partial sums of the weights
   float* qpart_f;      // [2*kResBlocksMax] FP32 (sum, compensation) partials
   double* rows;        // [(nsteps+1) * 10] output rows (columns of PA_results_run_<r>.dat)
-  const double* betas; // [nsteps+1]
-  const uint32_t* thr; // [(nsteps+1) * kThrPerStep]
+  double* betas;       // [nsteps+1] (adaptive: [kNBmax], filled in as the run goes)
+  uint32_t* thr;       // [(nsteps+1) * kThrPerStep], same
+  uint32_t* hist;      // adaptive only: [N+1] energy histogram, bin (E + 2N) / 4
   const void* init_src;  // device copy of a caller-supplied initial population, or null (random init)
   // ------------------------------------------------ dynamic scalars
   int step;            // temperature index being computed (1..nsteps); nsteps+1 when done
@@ -69,7 +70,16 @@ struct PopDev {
   long long sE, sE2, sM, sM2;
   unsigned long long sM4lo, sM4hi;
   int Emin_acc, pad3;
+  // ------------------------------------------------ adaptive temperature step
+  int adaptive;        // 1: the next beta is chosen after every temperature
+  int pad4;
+  double dbeta_cur;    // deltaBeta carried from step to step (PAisingSSC.cu:508,659)
+  double min_ov, max_ov, beta_fin;
 };
+
+constexpr int kNBmax = 10000;  // nBmax, PAisingSSC.cu:57: rows of a schedule at most
+// error codes in PopDev::error
+constexpr int kErrCapacity = 1, kErrExtinct = 2, kErrTooManySteps = 3;
 
 // Populations advancing together.  unit_prefix[p] .. unit_prefix[p+1]-1 are
 // the sweep work units (SSC replicas, MSC groups) of population p in the

@@ -26,6 +26,21 @@ def test_oracle_matches_reference_two_runs(oracle, coding):
         compare_rows(rows[r], ref, rtol=2e-10)
 
 
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_oracle_adaptive_matches_reference(oracle, coding):
+    """The AdaptiveStep build of the reference (-DAdaptiveStep): temperatures
+    chosen from the energy-histogram overlap, 57 rows ending on beta=1; and
+    with -M 2 the second run replays the first run's schedule."""
+    rows, _ = oracle.anneal(coding, 16, 1000, 10, 0.005, 1.0, 1, 100, adaptive=True)
+    ref = load_dat(f"ref/inj_{coding.upper()}_L16_R1000_t10_d0.005_s100_adaptive.dat")
+    assert ref.shape[0] == 57 and ref[-1, 0] == 1.0
+    compare_rows(rows[0], ref, rtol=2e-10)
+    rows, _ = oracle.anneal(coding, 16, 1000, 10, 0.01, 1.0, 2, 7, adaptive=True)
+    for r in range(2):
+        ref = load_dat(f"ref/inj_{coding.upper()}_L16_R1000_t10_d0.01_s7_M2_adaptive_run{r}.dat")
+        compare_rows(rows[r], ref, rtol=2e-10)
+
+
 def test_injected_stream_known_values(oracle):
     # Philox4x32-10 known-answer vectors (Salmon et al., Random123 kat_vectors):
     # counter 0, key 0 and counter/key all-ones
