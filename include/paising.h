@@ -81,6 +81,12 @@ typedef struct pa_config {
                         reuse the first run's schedule, as in the reference. */
   double min_overlap; /* MinOverlap (PAisingSSC.cu:42); 0 selects 0.85 */
   double max_overlap; /* MaxOverlap (PAisingSSC.cu:43); 0 selects 0.87 */
+  int mhr;            /* 1: multi-histogram reweighting, the reference's MHR build (PAisingSSC.cu:22,
+                         294-302,694-790): the energy histogram of every temperature of a run is
+                         accumulated on the device and reweighted after the run (pa_get_mhr_rows,
+                         PA_MHR_results_run_<r>.dat) */
+  int store_energies; /* 1: keep the energies of every temperature, the reference's EnergiesPopStore
+                         build (PAisingSSC.cu:24,563-578): pa_get_energies, PA_energies_<i>.dat */
 } pa_config;
 
 /* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */
@@ -139,6 +145,19 @@ PA_API int pa_num_rows(const pa_handle* h, int* nrows);
  * *nrows receives the number copied. */
 PA_API int pa_get_rows(const pa_handle* h, int set, pa_row* rows, int max_rows, int* nrows);
 
+/* Multi-histogram reweighting of result set `set` (config mhr = 1): 4
+ * doubles per temperature, beta, E/N, C/N and betaF/N, the columns of the
+ * reference's PA_MHR_results_run_<r>.dat (PAisingSSC.cu:694-786).  At most
+ * max_rows rows are copied; *nrows receives the number available. */
+PA_API int pa_get_mhr_rows(const pa_handle* h, int set, double* rows, int max_rows, int* nrows);
+
+/* Energies of the population of result set `set` at temperature `step`
+ * (config store_energies = 1; step 0 is the initial population), in the
+ * reference's replica order (MSC: group-major, active replicas only): the
+ * contents of PA_energies_<step>.dat (PAisingSSC.cu:563-578).  At most max
+ * values are copied; *n receives the population size. */
+PA_API int pa_get_energies(const pa_handle* h, int set, int step, int32_t* out, int max, int* n);
+
 /* Device time of the last pa_run in milliseconds (CUDA events around all
  * runs), and the reference's spin-flip attempt count
  * sweeps * N * sum_{i>=1} R_i over all runs (PAisingSSC.cu:632,806). */
@@ -175,7 +194,9 @@ PA_API int pa_profile_run(pa_handle* h, pa_kernel_time* out, int max, int* n);
 PA_API int pa_probe_int_issue(int device, double* lane_ops_per_s);
 
 /* Writes dir/PA_results_run_<r>.dat for every run with `precision`
- * significant digits (PAisingSSC.cu:670-692). */
+ * significant digits (PAisingSSC.cu:670-692), PA_MHR_results_run_<r>.dat
+ * where mhr is on, and PA_energies_<i>.dat (i >= 1, last run) where
+ * store_energies is on and the handle holds one population. */
 PA_API int pa_write_results(const pa_handle* h, const char* dir, int precision);
 
 PA_API int pa_destroy(pa_handle* h);

@@ -15,7 +15,9 @@ changes are the ones CUDA 13 forces or the comparison needs:
   ``curand`` variants keep cuRAND and are the reference's own GPU build;
 * the ``inj_adaptive`` variants (L=16) also define ``AdaptiveStep``, the
   reference's compile-time switch for its adaptive temperature step
-  (PAisingSSC.cu:23, PAisingMSC.cu:23).
+  (PAisingSSC.cu:23, PAisingMSC.cu:23); the ``inj_records`` variants define
+  ``MHR`` and ``EnergiesPopStore`` (multi-histogram reweighting and the
+  per-temperature energy files, PAisingSSC.cu:22,24).
 
 Step 1 (patch) needs the reference checkout and runs in the build container;
 step 2 (nvcc) runs wherever the patched sources are, e.g. on the GPU host,
@@ -98,6 +100,8 @@ def _compile(src: str, variant: str) -> str:
         cmd[1:1] = ["-include", os.path.join(SRC_OUT, "inj_shim.cuh"), "-I", SRC_OUT]
     if variant.endswith("adaptive"):  # the reference's AdaptiveStep build (its line 23 switch)
         cmd[1:1] = ["-DAdaptiveStep"]
+    if variant.endswith("records"):  # its MHR and EnergiesPopStore builds (lines 22, 24)
+        cmd[1:1] = ["-DMHR", "-DEnergiesPopStore"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {out}:\n{r.stderr[-2000:]}")
@@ -108,7 +112,7 @@ def compile_all(jobs: int) -> list[str]:
     os.makedirs(BIN_OUT, exist_ok=True)
     srcs = sorted(f for f in os.listdir(SRC_OUT) if f.endswith(".cu") and f.startswith("PAising"))
     tasks = [(os.path.join(SRC_OUT, s), v) for s in srcs for v in ("inj", "curand")]
-    tasks += [(os.path.join(SRC_OUT, s), "inj_adaptive") for s in srcs if s.endswith("_L16.cu")]
+    tasks += [(os.path.join(SRC_OUT, s), v) for s in srcs if s.endswith("_L16.cu") for v in ("inj_adaptive", "inj_records")]
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         return list(ex.map(lambda a: _compile(*a), tasks))
 

@@ -61,6 +61,68 @@ std::vector<double> schedule(double dbeta, double bfin) {
   return b;
 }
 
+// Multi-histogram reweighting of one run (the MHR build's analysis,
+// PAisingSSC.cu:694-767, one iteration as MHR_Niter = 1): from the energy
+// histogram of all temperatures, the free energies betaF_i and population
+// sizes R_i, the density of states
+//   ln Omega(E) = ln H(E) - max_i S_i - ln sum_i R_i exp(S_i - max S),
+//   S_i = betaF_i - beta_i E,
+// then at every beta_i the reweighted E/N, C/N and betaF/N.  rows: the run's
+// results rows; betaF_i is recomputed from the lnQ column exactly as the
+// reference accumulates it (BF_i = -N ln 2 + sum_{j<=i} -lnQ_j).  Returns
+// 4 doubles per temperature: beta, E/N, C/N, betaF/N.
+std::vector<double> mhr_analysis(int N, const std::vector<double>& rows, const std::vector<unsigned long long>& hist) {
+  const int nB = (int)(rows.size() / kRowCols);
+  std::vector<double> B(nB), BF(nB), R(nB);
+  double sumlnQ = 0.0;
+  for (int i = 0; i < nB; ++i) {
+    B[i] = rows[(size_t)i * kRowCols];
+    R[i] = rows[(size_t)i * kRowCols + 8];
+    if (i > 0) sumlnQ -= rows[(size_t)i * kRowCols + 9];
+    BF[i] = -N * std::log(2.0) + sumlnQ;
+  }
+  auto Ei = [N](int k) { return (double)(4 * k - 2 * N); };
+  std::vector<double> lnOmega((size_t)N + 1, 0.0), Sigma(nB);
+  std::vector<char> rel((size_t)N + 1, 0);
+  for (int k = 0; k <= N; ++k) {
+    double mSigma = Sigma[0] = BF[0] - B[0] * Ei(k);
+    for (int i = 1; i < nB; ++i) {
+      Sigma[i] = BF[i] - B[i] * Ei(k);
+      if (mSigma < Sigma[i]) mSigma = Sigma[i];
+    }
+    double sD = 0;
+    for (int i = 0; i < nB; ++i) sD += R[i] * std::exp(Sigma[i] - mSigma);
+    if (hist[k] == 0 || sD == 0) continue;
+    rel[k] = 1;
+    lnOmega[k] = std::log((double)hist[k]) - mSigma - std::log(sD);
+  }
+  std::vector<double> out((size_t)nB * 4), expOm((size_t)N + 1), Om((size_t)N + 1);
+  for (int i = 0; i < nB; ++i) {
+    double mOm = lnOmega[0] - B[i] * Ei(0);
+    for (int k = 0; k <= N; ++k) {
+      Om[k] = lnOmega[k] - B[i] * Ei(k);
+      if (mOm < Om[k]) mOm = Om[k];
+    }
+    double p = 0;
+    for (int k = 0; k <= N; ++k) {
+      expOm[k] = std::exp(Om[k] - mOm);
+      if (rel[k]) p += expOm[k];
+    }
+    double s = 0;
+    for (int k = 0; k <= N; ++k)
+      if (rel[k]) s += Ei(k) * expOm[k];
+    const double E = s / p / N, BFm = -mOm - std::log(p);
+    s = 0;
+    for (int k = 0; k <= N; ++k)
+      if (rel[k]) s += std::pow(Ei(k) - E * N, 2) * expOm[k];
+    out[(size_t)i * 4 + 0] = B[i];
+    out[(size_t)i * 4 + 1] = E;
+    out[(size_t)i * 4 + 2] = B[i] * B[i] * s / p / N;
+    out[(size_t)i * 4 + 3] = BFm / N;
+  }
+  return out;
+}
+
 size_t population_bytes(int coding, int L, int R) {
   const size_t N = (size_t)L * L;
   return coding == PA_CODING_MSC ? (size_t)((R + kMsb - 1) / kMsb) * N * 4 : (size_t)R * N;
@@ -106,6 +168,10 @@ struct pa_handle {
   int sets_done = 0;
   bool ran = false;  // pa_run has been called
   int runs_done = 0;  // completed runs: the first one chooses adaptive schedules, the others replay them
+  bool records = false;  // some population keeps an MHR histogram or its energies
+  std::vector<std::vector<double>> mhr;                    // per set: rows of (beta, E/N, C/N, betaF/N)
+  std::vector<std::vector<std::vector<int32_t>>> energies;  // per set, per temperature: energies
+  std::vector<int> drained;                                 // per population: last temperature read back
   double ms = 0.0, attempts = 0.0;
   std::string err;
   std::vector<void*> staging;  // per population: device copy of a caller-supplied initial population
@@ -146,16 +212,25 @@ struct pa_handle {
                   : launch_sweep(d_batch, coding, rng_mode, energy_only, stream_seed, sweep, stream);
   }
 
+  cudaError_t enqueue_record() {
+    return records ? launch("record", [&] { return launch_record(d_pops, npop, rblocks, stream); }) : cudaSuccess;
+  }
+
   cudaError_t enqueue_init() {
     cudaError_t e;
     const bool msc = coding == PA_CODING_MSC;
+    for (const auto& P : pops)  // the run's MHR histogram starts empty (PAisingSSC.cu:497-499)
+      if (P.h.mhr_hist &&
+          (e = cudaMemsetAsync(P.h.mhr_hist, 0, sizeof(unsigned long long) * (P.h.N + 1), stream)) != cudaSuccess)
+        return e;
     if ((e = launch("begin_run", [&] { return launch_begin_run(d_pops, npop, stream); })) != cudaSuccess) return e;
     if ((e = launch(msc ? "msc_init" : "ssc_init", [&] { return launch_init(d_pops, npop, coding, stream); })) != cudaSuccess)
       return e;
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 1, stream); })) != cudaSuccess) return e;
     e = launch(msc ? "msc_energy" : "ssc_energy", [&] { return sweep_launch(1); });
     if (e != cudaSuccess) return e;
-    return launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+    e = launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+    return e != cudaSuccess ? e : enqueue_record();
   }
 
   cudaError_t enqueue_step() {
@@ -171,8 +246,44 @@ struct pa_handle {
     e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return sweep_launch(0); });
     if (e != cudaSuccess) return e;
     e = launch("finish_step", [&] { return launch_finish_step(d_pops, npop, stream); });
+    if (e == cudaSuccess) e = enqueue_record();
     if (e != cudaSuccess || !adaptive) return e;
     return launch("adapt", [&] { return launch_adapt(d_pops, npop, stream); });
+  }
+
+  // Energies of the temperatures recorded since the last call, from the
+  // device ring into energies[r * npop + population] (active replicas only,
+  // in the reference's replica order).
+  cudaError_t drain(int r) {
+    if (!records) return cudaSuccess;
+    std::vector<PopDev> st(npop);
+    cudaError_t e = cudaMemcpyAsync(st.data(), d_pops, sizeof(PopDev) * npop, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    std::vector<int32_t> ev;
+    std::vector<uint8_t> av;
+    for (int k = 0; k < npop && e == cudaSuccess; ++k) {
+      const PopDev& h = pops[k].h;
+      if (!(h.rec & kRecEnergies)) continue;
+      auto& dst = energies[(size_t)r * npop + pops[k].user_index];
+      const size_t stride = h.coding == PA_CODING_MSC ? (size_t)h.rgcap * kMsb : (size_t)h.Rcap;
+      for (int s = drained[k] + 1; s <= st[k].last_rec && e == cudaSuccess; ++s) {
+        const int slot = s % h.ring;
+        int n = 0;
+        e = cudaMemcpy(&n, h.nlog + slot, sizeof(int), cudaMemcpyDeviceToHost);
+        ev.resize((size_t)n);
+        av.assign((size_t)n, 1);
+        if (e == cudaSuccess && n > 0)
+          e = cudaMemcpy(ev.data(), h.elog + slot * stride, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && n > 0 && h.alog)
+          e = cudaMemcpy(av.data(), h.alog + slot * stride, (size_t)n, cudaMemcpyDeviceToHost);
+        if ((int)dst.size() <= s) dst.resize((size_t)s + 1);
+        dst[s].clear();
+        for (int j = 0; j < n; ++j)
+          if (av[j]) dst[s].push_back(ev[j]);
+      }
+      drained[k] = std::max(drained[k], st[k].last_rec);
+    }
+    return e;
   }
 
   // A whole run as one launch sequence (fixed schedules: the graph of a run).
@@ -212,21 +323,25 @@ struct pa_handle {
     return e;
   }
 
-  // One run, on the stream: graph replays or host-stepped launches.
-  cudaError_t run_once() {
+  // Run r, on the stream: graph replays or host-stepped launches.  Recorded
+  // energies are read back whenever the device ring may be about to wrap.
+  cudaError_t run_once(int r) {
     cudaError_t e;
+    drained.assign(npop, -1);
     if (graph) {
       e = cudaGraphLaunch(exec, stream);
       while (adaptive && e == cudaSuccess) {
         bool done = false;
-        e = all_done(&done);
+        e = drain(r);
+        if (e == cudaSuccess) e = all_done(&done);
         if (e != cudaSuccess || done) break;
         e = cudaGraphLaunch(chunk_exec, stream);
       }
-      return e;
+      return e == cudaSuccess ? drain(r) : e;
     }
     e = enqueue_init();
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess) e = drain(r);
     for (int i = 1; i <= max_steps && e == cudaSuccess; ++i) {
       e = enqueue_step();
       if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -236,6 +351,7 @@ struct pa_handle {
         double row[kRowCols];
         e = cudaMemcpy(row, pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
       }
+      if (e == cudaSuccess) e = drain(r);
       if (adaptive && e == cudaSuccess) {
         bool done = false;
         e = all_done(&done);
@@ -363,6 +479,8 @@ int validate(const pa_config& c) {
     return bad("SSC needs L % 8 == 0, 8 <= L <= 256");
   }
   if (c.adaptive != 0 && c.adaptive != 1) return bad("adaptive must be 0 or 1");
+  if ((c.mhr != 0 && c.mhr != 1) || (c.store_energies != 0 && c.store_energies != 1))
+    return bad("mhr and store_energies must be 0 or 1");
   if (c.adaptive) {
     const double lo = c.min_overlap > 0 ? c.min_overlap : kMinOverlap;
     const double hi = c.max_overlap > 0 ? c.max_overlap : kMaxOverlap;
@@ -504,6 +622,20 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     uint32_t* th = nullptr;
     chk(B.alloc(&th, (size_t)P.cap * kThrPerStep));
     h.thr = th;
+    if (c.mhr) {
+      chk(B.alloc(&h.mhr_hist, (size_t)N + 1));
+      h.rec |= kRecMhr;
+    }
+    if (c.store_energies) {
+      // fixed schedules: every temperature of a run; adaptive: one graph
+      // chunk (plus the set-up) between read-backs
+      h.ring = c.adaptive ? pa_handle::kChunk + 1 : P.nsteps + 1;
+      chk(B.alloc(&h.elog, (size_t)h.ring * units));
+      if (c.coding == PA_CODING_MSC) chk(B.alloc(&h.alog, (size_t)h.ring * units));
+      chk(B.alloc(&h.nlog, (size_t)h.ring));
+      h.rec |= kRecEnergies;
+    }
+    if (h.rec) H->records = true;
     if (c.adaptive) {
       chk(B.alloc(&h.hist, (size_t)N + 1));
       h.adaptive = 1;
@@ -634,6 +766,8 @@ int pa_num_sets(const pa_handle* H, int* n) {
 int pa_run(pa_handle* H) {
   if (!H) return PA_ERR_ARG;
   H->rows.assign((size_t)H->npop * H->seq_runs, {});
+  H->mhr.assign((size_t)H->npop * H->seq_runs, {});
+  H->energies.assign((size_t)H->npop * H->seq_runs, {});
   H->sets_done = 0;
   H->attempts = 0;
   H->ran = true;
@@ -646,7 +780,7 @@ int pa_run(pa_handle* H) {
       e = H->set_adaptive(H->runs_done == 0);
       if (e != cudaSuccess) return H->cuda_fail(e, "adaptive set-up");
     }
-    e = H->run_once();
+    e = H->run_once(r);
     if (e != cudaSuccess) return H->cuda_fail(e, H->graph ? "graph launch" : "plain step");
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(back.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost, H->stream);
@@ -681,6 +815,12 @@ int pa_run(pa_handle* H) {
       const std::vector<double>& rw = H->rows[(size_t)r * H->npop + P.user_index];
       for (size_t i = 1; i < rw.size() / kRowCols; ++i)
         H->attempts += (double)P.cfg.sweeps * (double)P.h.N * rw[i * kRowCols + 8];
+      if (P.h.mhr_hist && !back[k].error) {
+        std::vector<unsigned long long> hist((size_t)P.h.N + 1);
+        e = cudaMemcpy(hist.data(), P.h.mhr_hist, sizeof(unsigned long long) * hist.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return H->cuda_fail(e, "MHR histogram");
+        H->mhr[(size_t)r * H->npop + P.user_index] = mhr_analysis(P.h.N, rw, hist);
+      }
     }
     if (status == PA_OK) {
       H->sets_done = (r + 1) * H->npop;
@@ -766,6 +906,28 @@ int pa_get_rows(const pa_handle* H, int set, pa_row* rows, int max_rows, int* nr
   const int m = n < max_rows ? n : max_rows;
   for (int i = 0; i < m; ++i) std::memcpy(&rows[i], src.data() + (size_t)i * kRowCols, sizeof(pa_row));
   if (nrows) *nrows = m;
+  return PA_OK;
+}
+
+int pa_get_mhr_rows(const pa_handle* H, int set, double* rows, int max_rows, int* nrows) {
+  if (!H || (max_rows > 0 && !rows)) return PA_ERR_ARG;
+  if (set < 0 || set >= H->sets_done || H->mhr[set].empty()) return PA_ERR_STATE;
+  const std::vector<double>& src = H->mhr[set];
+  const int n = (int)(src.size() / 4), m = std::min(n, max_rows);
+  if (m > 0) std::memcpy(rows, src.data(), sizeof(double) * 4 * (size_t)m);
+  if (nrows) *nrows = n;
+  return PA_OK;
+}
+
+int pa_get_energies(const pa_handle* H, int set, int step, int32_t* out, int max, int* n) {
+  if (!H || (max > 0 && !out)) return PA_ERR_ARG;
+  if (set < 0 || set >= H->sets_done) return PA_ERR_STATE;
+  const auto& per = H->energies[set];
+  if (step < 0 || step >= (int)per.size()) return per.empty() ? PA_ERR_STATE : PA_ERR_ARG;
+  const std::vector<int32_t>& e = per[step];
+  const int k = std::min((int)e.size(), max);
+  if (k > 0) std::memcpy(out, e.data(), sizeof(int32_t) * (size_t)k);
+  if (n) *n = (int)e.size();
   return PA_OK;
 }
 
@@ -858,6 +1020,33 @@ int pa_write_results(const pa_handle* H, const char* dir, int precision) {
       std::fprintf(f, "%d %.*g\n", (int)w[8], precision, w[9]);
     }
     std::fclose(f);
+    // PA_MHR_results_run_<r>.dat: beta E/N C/N betaF/N (PAisingSSC.cu:768-786)
+    if (!H->mhr[r].empty()) {
+      std::string mp = path.substr(0, path.rfind('/') + 1) + "PA_MHR_results_run_" + std::to_string(r) + ".dat";
+      FILE* g = std::fopen(mp.c_str(), "w");
+      if (!g) return PA_ERR_ARG;
+      const std::vector<double>& m = H->mhr[r];
+      for (size_t i = 0; i < m.size() / 4; ++i) {
+        for (int k = 0; k < 4; ++k) std::fprintf(g, "%.*g ", precision, m[i * 4 + k]);
+        std::fprintf(g, "\n");
+      }
+      std::fclose(g);
+    }
+  }
+  // PA_energies_<i>.dat: energies of temperature i >= 1, space separated, of
+  // the last run (each run overwrites them, PAisingSSC.cu:563-578); one
+  // population per handle, as the files carry no population index
+  if (H->npop == 1 && !H->energies[H->sets_done - 1].empty()) {
+    const auto& per = H->energies[H->sets_done - 1];
+    for (size_t i = 1; i < per.size(); ++i) {
+      std::string ep = std::string(dir);
+      if (!ep.empty() && ep.back() != '/') ep += '/';
+      ep += "PA_energies_" + std::to_string(i) + ".dat";
+      FILE* g = std::fopen(ep.c_str(), "w");
+      if (!g) return PA_ERR_ARG;
+      for (int32_t v : per[i]) std::fprintf(g, "%d ", (int)v);
+      std::fclose(g);
+    }
   }
   return PA_OK;
 }

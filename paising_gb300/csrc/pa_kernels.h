@@ -88,6 +88,9 @@ cudaError_t launch_msc_cluster_sweep(int cs, BatchDev* b, int rng_mode, int ener
 // Per-run / per-step bookkeeping.
 cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s);
+// Populations with records: histogram / energy ring of the temperature just
+// finished (after launch_finish_step); `blocks` from res_blocks().
+cudaError_t launch_record(PopDev* pops, int npop, int blocks, cudaStream_t s);
 // Adaptive populations: choose the next temperature (after launch_finish_step).
 cudaError_t launch_adapt(PopDev* pops, int npop, cudaStream_t s);
 

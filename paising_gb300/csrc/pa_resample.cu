@@ -275,6 +275,47 @@ __global__ void begin_run_kernel(PopDev* pops) {
   for (int c = 0; c < kRowCols; ++c) row[c] = 0.0;
   row[6] = st->bf0 / st->N;
   row[8] = (double)st->Rinit;
+  st->last_rec = -1;
+}
+
+// ---------------------------------------------- per-temperature records
+// After finish_step: the population of temperature step-1, if not recorded
+// yet in this run, enters the run's energy histogram (UpdateShistE,
+// PAisingSSC.cu:296-302, PAisingMSC.cu:454-460: active replicas only) and/or
+// the energy ring (EnergiesPopStore, PAisingSSC.cu:563-578: energies in
+// replica order; MSC group-major with the active flags).  The last block to
+// finish (ticket) marks the temperature recorded, so every block has tested
+// the guard before it changes.
+__global__ void __launch_bounds__(kResThreads) record_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  const int s = st->step - 1;
+  if (!st->rec || s <= st->last_rec || st->error) return;
+  const int R = st->R_cur, n = pop_units(st, R), N = st->N;
+  const bool msc = st->coding == kMSC;
+  const uint8_t* act = msc ? st->active[st->parity] : nullptr;
+  const int32_t* E = st->E;
+  int32_t* el = nullptr;
+  uint8_t* al = nullptr;
+  if (st->rec & kRecEnergies) {
+    const size_t stride = msc ? (size_t)st->rgcap * kMsb : (size_t)st->Rcap;
+    const size_t slot = (size_t)(s % st->ring) * stride;
+    el = st->elog + slot;
+    if (msc) al = st->alog + slot;
+  }
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int e = E[j];
+    const bool a = !act || act[j];
+    if ((st->rec & kRecMhr) && a) atomicAdd(&st->mhr_hist[(e + 2 * N) >> 2], 1ull);
+    if (el) el[j] = e;
+    if (al) al[j] = a ? 1 : 0;
+  }
+  if (last_block(&st->ticket)) {
+    if (threadIdx.x == 0) {
+      if (el) st->nlog[s % st->ring] = n;
+      st->last_rec = s;
+      st->ticket = 0;
+    }
+  }
 }
 
 // After a sweep kernel: observables of the step (PAisingSSC.cu:620-630)
@@ -474,6 +515,11 @@ cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s) {
 
 cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s) {
   finish_step_kernel<<<npop, 1, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  record_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

@@ -75,7 +75,18 @@ struct PopDev {
   int pad4;
   double dbeta_cur;    // deltaBeta carried from step to step (PAisingSSC.cu:508,659)
   double min_ov, max_ov, beta_fin;
+  // ------------------------------------------------ per-temperature records
+  int rec;             // kRecMhr | kRecEnergies
+  int last_rec;        // last temperature index recorded in this run (-1: none)
+  int ring;            // temperatures the energy ring holds (slot = index % ring)
+  int pad5;
+  unsigned long long* mhr_hist;  // [N+1] energy histogram of all temperatures of the run
+  int32_t* elog;       // [ring][units] energies of recorded temperatures
+  uint8_t* alog;       // MSC: [ring][units] active flags of the same
+  int* nlog;           // [ring] units recorded per slot
 };
+
+constexpr int kRecMhr = 1, kRecEnergies = 2;
 
 constexpr int kNBmax = 10000;  // nBmax, PAisingSSC.cu:57: rows of a schedule at most
 // error codes in PopDev::error

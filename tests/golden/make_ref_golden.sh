@@ -20,6 +20,10 @@ for p in SSC MSC; do
   cp $T/e_$p/PA_results_run_0.dat "$OUT/inj_${p}_L16_R1000_t10_d0.005_s100_adaptive.dat"
   $B/PAising${p}_L16_inj_adaptive -R 1000 -t 10 -s 7 -M 2 -d 0.01 -o $T/f_$p > "$OUT/logs/inj_${p}_L16_M2_adaptive.log"
   for k in 0 1; do cp $T/f_$p/PA_results_run_$k.dat "$OUT/inj_${p}_L16_R1000_t10_d0.01_s7_M2_adaptive_run$k.dat"; done
+  # MHR + EnergiesPopStore build: reweighted observables and per-temperature energies
+  $B/PAising${p}_L16_inj_records -R 1000 -t 10 -s 100 -d 0.05 -o $T/g_$p > "$OUT/logs/inj_${p}_L16_records.log"
+  mkdir -p "$OUT/inj_${p}_L16_R1000_t10_d0.05_s100_records"
+  cp $T/g_$p/*.dat "$OUT/inj_${p}_L16_R1000_t10_d0.05_s100_records/"
   $B/PAising${p}_L64_inj -s 100 -o $T/c_$p > "$OUT/logs/inj_${p}_L64.log"
   cp $T/c_$p/PA_results_run_0.dat "$OUT/inj_${p}_L64_R20000_t100_d0.005_s100.dat"
   $B/PAising${p}_L64_curand -s 100 -o $T/d_$p > "$OUT/logs/cur_${p}_L64.log"
