@@ -8,7 +8,9 @@
 // (resampling weights), -g 0|1 (host-stepped or graph), -D device, -a (the
 // adaptive temperature step of the reference's AdaptiveStep build, with its
 // output directory ./data%s_L%d_R%d_EqSw%d/, PAisingSSC.cu:406-410), -T (time
-// the MSC tile sizes before the run, pa_autotune).
+// the MSC tile sizes before the run, pa_autotune), -H (multi-histogram
+// reweighting, the MHR build: PA_MHR_results_run_<r>.dat), -E (energies of
+// every temperature, the EnergiesPopStore build: PA_energies_<i>.dat).
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -41,7 +43,9 @@ static void usage(const char* prog) {
       " -g 0|1             ( 1: one CUDA graph per run (default), 0: host steps each temperature )\n"
       " -D device          ( CUDA device ordinal )\n"
       " -a                 ( adaptive temperature step, MinOverlap 0.85, MaxOverlap 0.87 )\n"
-      " -T                 ( autotune the MSC sweep's tile sizes before the run )\n",
+      " -T                 ( autotune the MSC sweep's tile sizes before the run )\n"
+      " -H                 ( multi-histogram reweighting: PA_MHR_results_run_<r>.dat )\n"
+      " -E                 ( store the energies of every temperature: PA_energies_<i>.dat )\n",
       prog);
 }
 
@@ -55,7 +59,7 @@ int main(int argc, char** argv) {
   std::string dir;
   int opt;
   opterr = 0;
-  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aT?")) != -1) {
+  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aTHE?")) != -1) {
     int i;
     double f;
     switch (opt) {  // same acceptance rules as PAisingSSC.cu:390-398
@@ -75,6 +79,8 @@ int main(int argc, char** argv) {
       case 'D': c.device = std::atoi(optarg); break;
       case 'a': c.adaptive = 1; break;
       case 'T': tune = true; break;
+      case 'H': c.mhr = 1; break;
+      case 'E': c.store_energies = 1; break;
       default:
         if (optopt && optopt != '?') std::printf("illegal option -- %c\n", optopt);
         usage(argv[0]);
