@@ -341,7 +341,19 @@ __global__ void __launch_bounds__(kSweepThreads, 5)
 // (old group, bit)) at new group s % rg_new, bit s / rg_new
 // (PAisingMSC.cu:413-414).  Here every new word gathers its 32 bits:
 // bit k of new group j comes from old replica src[k*rg_new + j].
-__global__ void msc_resample_kernel(PopDev* pops) {
+//
+// A block takes work items (new group j, chunk of kResChunk sites): the 32
+// source rows and bit positions of group j are resolved once into shared
+// memory, after which every site's 32 loads are independent of each other
+// (many in flight per thread) and coalesced across the warp.  Items run in
+// site-chunk-major order over consecutive groups, whose sources are
+// neighbouring replicas, so the old rows being read stay in L2.
+constexpr int kResChunk = 1024;
+constexpr int kResampleThreads = 256;
+
+__global__ void __launch_bounds__(kResampleThreads) msc_resample_kernel(PopDev* pops) {
+  __shared__ uint32_t s_off[kMsb], s_sh[kMsb];
+  __shared__ uint32_t s_valid;
   PopDev* st = pops + blockIdx.y;
   if (!pop_stepping(st)) return;
   const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb;
@@ -349,21 +361,30 @@ __global__ void msc_resample_kernel(PopDev* pops) {
   uint32_t* neu = (uint32_t*)st->spins[st->parity];
   uint8_t* act = st->active[st->parity];
   const uint32_t* src = st->src;
-  const long long total = (long long)rgn * N;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(e / N), t = (int)(e - (long long)j * N);
-    uint32_t w = 0;
-#pragma unroll 4
-    for (int k = 0; k < kMsb; ++k) {
-      const int s = k * rgn + j;
-      if (s < Rn) {
-        const uint32_t lin = src[s];
-        w |= ((old[(size_t)(lin >> 5) * N + t] >> (lin & 31u)) & 1u) << k;
-      }
+  const int tid = threadIdx.x, nchunk = (N + kResChunk - 1) / kResChunk;
+  const int items = rgn * nchunk;
+  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+    const int c = it / rgn, j = it - c * rgn;  // chunk-major: consecutive items, consecutive groups
+    __syncthreads();                           // the previous item's sources are no longer read
+    if (tid < kMsb) {
+      const int s = tid * rgn + j;
+      const bool v = s < Rn;
+      const uint32_t lin = v ? src[s] : 0u;  // an invalid bit reads old word 0 and is masked off
+      s_off[tid] = (lin >> 5) * (uint32_t)N;
+      s_sh[tid] = lin & 31u;
+      const uint32_t m = __ballot_sync(kFull, v);
+      if (tid == 0) s_valid = m;
+      if (c == 0) act[j * kMsb + tid] = v ? 1 : 0;
     }
-    neu[e] = w;
-    if (t < kMsb) act[j * kMsb + t] = (t * rgn + j) < Rn;
+    __syncthreads();
+    const uint32_t vmask = s_valid;
+    const int t1 = min(N, (c + 1) * kResChunk);
+    for (int t = c * kResChunk + tid; t < t1; t += blockDim.x) {
+      uint32_t w = 0;
+#pragma unroll 16
+      for (int k = 0; k < kMsb; ++k) w |= ((__ldg(old + s_off[k] + t) >> s_sh[k]) & 1u) << k;
+      neu[(size_t)j * N + t] = w & vmask;
+    }
   }
 }
 
