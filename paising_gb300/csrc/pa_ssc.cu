@@ -99,10 +99,15 @@ __global__ void ssc_init_kernel(PopDev* pops) {
 // t = idx mod 128, k = idx div 128, K = draws per reference thread per half
 // sweep, and flips iff (H+1)/2^32 < boltz[idxT0 + 2 idxT1], evaluated as the
 // integer test H < thr10[...] with thr10 = ceil(2^32 p) - 1 (exact).
-// MODE kNative draws one Philox4x32-10 block per 4-site word and flips
-// iff dE <= 0 or H < ceil(2^32 exp(-beta dE)).
+// MODE kNative flips iff dE <= 0 or U < T = ceil(2^32 exp(-beta dE)) for a
+// uniform 32-bit U, decided one byte at a time: U's top byte b against T's
+// top byte t settles the test unless b == t (probability 1/256), and only
+// then are U's low 24 bits drawn and compared with T's.  One Philox4x32-10
+// block serves two words (8 sites): words x, y give the top bytes, z, w the
+// low bits of up to two undecided sites; more than two take another block.
+// Each site's acceptance probability is exactly T / 2^32.
 template <int MODE>
-__global__ void __launch_bounds__(kSweepThreads)
+__global__ void __launch_bounds__(kSweepThreads, 4)
     ssc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
   extern __shared__ __align__(16) uint32_t lat[];  // N/4 words: A then B
   __shared__ uint32_t s_thr[16];
@@ -167,19 +172,82 @@ __global__ void __launch_bounds__(kSweepThreads)
       for (int hf = 0; hf < 2; ++hf) {
         uint32_t* self = lat + (hf ? hw : 0);
         const uint32_t* oth = lat + (hf ? 0 : hw);
-        if (worker) {
+        // anti-parallel neighbour count (0..4) of each of the 4 sites of word
+        // (ty, cw); the horizontal neighbour that is not at the same idx is x-1
+        // for A on even rows and B on odd rows, x+1 otherwise (PAisingSSC.cu:170,182)
+        auto anti = [&](int ty, const uint32_t* oth, uint32_t s, int hf_) {
+          const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
+          const uint32_t o = oth[row + cw];
+          const bool left = (hf_ == 0) == ((ty & 1) == 0);
+          const uint32_t oside = left ? __byte_perm(oth[row + cwl], o, 0x6543) : __byte_perm(o, oth[row + cwr], 0x4321);
+          const uint32_t ou = oth[rowu + cw], od = oth[rowd + cw];
+          return ((s ^ o) >> 1 & kLsb) + ((s ^ oside) >> 1 & kLsb) + ((s ^ ou) >> 1 & kLsb) + ((s ^ od) >> 1 & kLsb);
+        };
+        if (worker && MODE == kNative) {
+          const uint32_t T4 = s_thr[10], T8 = s_thr[11];
+          const uint32_t t4b = (T4 >> 24) * kLsb, t8b = (T8 >> 24) * kLsb;
+          const uint32_t c1 = (uint32_t)(sw * 2 + hf) * 2u;
+          for (int ty0 = rsub; ty0 < L; ty0 += 2 * rpp) {
+            const int ty1 = ty0 + rpp;
+            const bool two = ty1 < L;
+            const int w0 = ty0 * Wr + cw, w1 = two ? ty1 * Wr + cw : w0;
+            uint32_t s[2], na[2], flip[2], strag[2];
+            s[0] = self[w0];
+            s[1] = self[w1];
+            na[0] = anti(ty0, oth, s[0], hf);
+            na[1] = two ? anti(ty1, oth, s[1], hf) : 0x02020202u;  // no decision needed
+            const U4 rn = philox10((uint32_t)(r * hw + w0), c1, (uint32_t)step, tag, k0, k1);
+            const uint32_t top[2] = {rn.x, rn.y};
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const uint32_t one = __vcmpeq4(na[q], kLsb), need = __vcmpleu4(na[q], kLsb);
+              const uint32_t tb = (t4b & one) | (t8b & ~one);  // T's top byte per site
+              flip[q] = (~need | (need & __vcmpltu4(top[q], tb))) & 0xFEFEFEFEu;
+              strag[q] = need & __vcmpeq4(top[q], tb);  // top bytes equal: undecided
+            }
+            if (strag[0] | strag[1]) {  // probability ~ 2/256 per site needing a decision
+              // undecided sites as bits q*4 + j; their low 24 bits come from
+              // rn.z, rn.w, then from further blocks, four words each
+              uint32_t pend = (((strag[0] & kLsb) * 0x01020408u) >> 24) | ((((strag[1] & kLsb) * 0x01020408u) >> 24) << 4);
+              uint32_t a0 = rn.z, a1 = rn.w, a2 = 0u, a3 = 0u, fl = 0u;
+              int used = 0;
+#pragma unroll 1
+              while (pend) {
+                const int bit = __ffs(pend) - 1;
+                pend &= pend - 1;
+                if (used == 2 || used == 6) {
+                  const U4 x = philox10((uint32_t)(r * hw + w0), c1 + 1u, (uint32_t)step,
+                                        tag | ((uint32_t)(used >> 2) << 12), k0, k1);
+                  a0 = x.x; a1 = x.y; a2 = x.z; a3 = x.w;
+                }
+                const int slot = used < 2 ? used : (used - 2) & 3;
+                const uint32_t u = slot == 0 ? a0 : slot == 1 ? a1 : slot == 2 ? a2 : a3;
+                ++used;
+                const uint32_t nq = bit < 4 ? na[0] : na[1];
+                const uint32_t T = ((nq >> (8 * (bit & 3))) & 0xFFu) == 1u ? T4 : T8;
+                if ((u & 0xFFFFFFu) < (T & 0xFFFFFFu)) fl |= 1u << bit;
+              }
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                flip[0] |= ((fl >> j) & 1u) ? 0xFEu << (8 * j) : 0u;
+                flip[1] |= ((fl >> (4 + j)) & 1u) ? 0xFEu << (8 * j) : 0u;
+              }
+            }
+            self[w0] = s[0] ^ flip[0];
+            if (two) self[w1] = s[1] ^ flip[1];
+          }
+        }
+        if (worker && MODE == kRefCoords) {
           for (int ty = rsub; ty < L; ty += rpp) {
             const int row = ty * Wr, rowu = (ty == 0 ? L - 1 : ty - 1) * Wr, rowd = (ty + 1 == L ? 0 : ty + 1) * Wr;
             const int w = row + cw;
             const uint32_t s = self[w];
             const uint32_t o = oth[w];
-            // the horizontal neighbour that is not at the same idx: x-1 for A
-            // on even rows and B on odd rows, x+1 otherwise (PAisingSSC.cu:170,182)
             const bool left = (hf == 0) == ((ty & 1) == 0);
             const uint32_t oside = left ? __byte_perm(oth[row + cwl], o, 0x6543) : __byte_perm(o, oth[row + cwr], 0x4321);
             const uint32_t ou = oth[rowu + cw], od = oth[rowd + cw];
             uint32_t flip = 0;
-            if (MODE == kRefCoords) {
+            {
               const uint32_t nminus = minus_bits(o) + minus_bits(oside) + minus_bits(ou) + minus_bits(od);
               // idxT0 + 2 idxT1 = (1 - s_minus) + 2 (4 - n_minus) per byte
               const uint32_t tix = 0x09090909u - minus_bits(s) - (nminus << 1);
@@ -192,18 +260,6 @@ __global__ void __launch_bounds__(kSweepThreads)
                 const unsigned long long ctr = (unsigned long long)sw * 2 * K + (unsigned long long)hf * K + k;
                 const uint32_t u = ref_word(seed, sub, ctr);
                 if (u < s_thr[(tix >> (8 * j)) & 0xFFu]) flip |= 0xFEu << (8 * j);
-              }
-            } else {
-              const uint32_t na = ((s ^ o) >> 1 & kLsb) + ((s ^ oside) >> 1 & kLsb) + ((s ^ ou) >> 1 & kLsb) +
-                                  ((s ^ od) >> 1 & kLsb);
-              const U4 rn = philox10((uint32_t)(r * hw + w), (uint32_t)(sw * 2 + hf), (uint32_t)step, tag, k0, k1);
-              const uint32_t T4 = s_thr[10], T8 = s_thr[11];
-              const uint32_t uu[4] = {rn.x, rn.y, rn.z, rn.w};
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                const uint32_t a = (na >> (8 * j)) & 0xFFu;
-                const bool acc_ = a >= 2u || uu[j] < (a ? T4 : T8);
-                if (acc_) flip |= 0xFEu << (8 * j);
               }
             }
             self[w] = s ^ flip;
