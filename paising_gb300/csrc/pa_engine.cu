@@ -150,6 +150,7 @@ struct pa_handle {
   int max_steps = 0;
   int rblocks = 1;
   int cs = 1;  // CTAs per MSC group in the sweep (1, or a cluster of 2 / 4)
+  bool ssc_bits = false;  // SSC swept on bit planes (pa_ssc_bits.cu)
   bool adaptive = false;  // some population chooses its temperatures as it goes
   static constexpr int kChunk = 16;  // adaptive runs: steps per graph launch between host checks
   cudaGraph_t chunk_t = nullptr;
@@ -208,6 +209,7 @@ struct pa_handle {
   }
 
   cudaError_t sweep_launch(int energy_only) {
+    if (ssc_bits) return launch_ssc_bits_sweep(d_batch, energy_only, stream_seed, sweep, stream);
     return cs > 1 ? launch_msc_cluster_sweep(cs, d_batch, rng_mode, energy_only, stream_seed, sweep, stream)
                   : launch_sweep(d_batch, coding, rng_mode, energy_only, stream_seed, sweep, stream);
   }
@@ -366,8 +368,9 @@ struct pa_handle {
   cudaError_t setup_launches() {
     int max_smem = 0;
     for (const auto& P : pops) max_smem = std::max(max_smem, P.geom.smem);
-    cudaError_t e = cs > 1 ? msc_cluster_setup(cs, rng_mode, max_smem, &sweep)
-                           : sweep_setup(coding, rng_mode, max_smem, &sweep);
+    cudaError_t e = ssc_bits ? ssc_bits_setup(max_smem, &sweep)
+                    : cs > 1 ? msc_cluster_setup(cs, rng_mode, max_smem, &sweep)
+                             : sweep_setup(coding, rng_mode, max_smem, &sweep);
     if (e != cudaSuccess || !graph) return e;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph_t) cudaGraphDestroy(graph_t);
@@ -516,7 +519,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   // one sweep kernel serves the whole batch: clusters if any population needs them
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c0.device);
-  const int slots = 5 * nsm;  // resident one-CTA sweep CTAs (five per SM up to 44 KB of tile)
+  const int slots = 4 * nsm;  // resident one-CTA sweep CTAs (four per SM, register-bound)
   H->cs = 1;
   long long batch_groups = 0;  // work available to the one-CTA sweep: bounds automatic tile sizes
   if (H->coding == PA_CODING_MSC)
@@ -524,6 +527,13 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
       batch_groups += (c.R + kMsb - 1) / kMsb;
     }
+  // SSC with the native stream: bit-plane sweep when every lattice allows it
+  // (sweep_variant 1 keeps the int8 sweep)
+  H->ssc_bits = H->coding == PA_CODING_SSC && H->rng_mode == PA_RNG_NATIVE;
+  for (const auto& c : cfgs) {
+    SweepGeom gb;
+    if (c.sweep_variant == 1 || !ssc_bits_geom(c.L, &gb)) H->ssc_bits = false;
+  }
   H->pops.resize(cfgs.size());
   for (size_t k = 0; k < cfgs.size(); ++k) {
     PopHost& P = H->pops[k];
@@ -531,7 +541,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     P.user_index = (int)k;
     if (P.cfg.capacity <= 0) P.cfg.capacity = 1.25;
     bool okg;
-    if (P.cfg.coding == PA_CODING_SSC) okg = ssc_geom(P.cfg.L, &P.geom);
+    if (P.cfg.coding == PA_CODING_SSC) okg = H->ssc_bits ? ssc_bits_geom(P.cfg.L, &P.geom) : ssc_geom(P.cfg.L, &P.geom);
     else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_groups, slots);
     else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
     if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +

@@ -77,6 +77,13 @@ cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_ssc_resample(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_msc_resample(PopDev* pops, int npop, cudaStream_t s);
 
+// SSC populations swept on bit planes (native stream, L = 64, 128, 256):
+// tiles of G replicas packed to one bit per site in shared memory.
+bool ssc_bits_geom(int L, SweepGeom* g);
+cudaError_t ssc_bits_setup(int smem, SweepLaunch* out);
+cudaError_t launch_ssc_bits_sweep(BatchDev* b, int energy_only, unsigned long long seed, const SweepLaunch& sl,
+                                  cudaStream_t s);
+
 // MSC sweep by thread-block clusters of cs = 2 or 4 CTAs (one horizontal
 // stripe of the group per CTA), for lattices too large for one CTA.
 bool msc_cluster_geom(int L, int cs, int threads, SweepGeom* g);

@@ -73,7 +73,7 @@ __global__ void msc_init_kernel(PopDev* pops) {
 //   per batch; populations differ in counter word 3).
 static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the tile, bit) in the epilogue");
 template <int MODE>
-__global__ void __launch_bounds__(kSweepThreads, 5)
+__global__ void __launch_bounds__(kSweepThreads, 4)
     msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
   extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
   __shared__ int s_unit, s_pop;
@@ -411,7 +411,7 @@ bool msc_geom(int L, SweepGeom* g, int tile, long long groups, int slots) {
   g->half = g->N / 2;
   g->Wr = L / 2;
   // G > 1 moves each sublattice with 16-byte vectors (h % 4 == 0) and keeps
-  // the tile within the shared memory of five resident CTAs per SM
+  // the tile small enough for four resident CTAs per SM
   auto allowed = [&](int G) {
     return G == 1 || (G == 2 || G == 4 || G == kMaxTile) && g->half % 4 == 0 && G * g->N * 4 <= kTileSmemMax;
   };

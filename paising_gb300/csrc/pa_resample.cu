@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(1024) plan_kernel(BatchDev* b, int energy_only
     const bool part = energy_only ? (st->step == 0) : pop_stepping(st);
     if (part) {
       const int gpt = st->gpt > 0 ? st->gpt : 1;
-      units = st->coding == kMSC ? (uint32_t)(((st->R_cur + kMsb - 1) / kMsb + gpt - 1) / gpt) : (uint32_t)st->R_cur;
+      units = st->coding == kMSC ? (uint32_t)(((st->R_cur + kMsb - 1) / kMsb + gpt - 1) / gpt)
+                                 : (uint32_t)((st->R_cur + gpt - 1) / gpt);
     }
   }
   uint32_t total;
