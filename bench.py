@@ -258,6 +258,7 @@ def run_ours(a):
             out.update(profile_leg(a, eng, pa))
         if not a.no_plain and P > 1:
             out["plain"] = plain_leg(a, dev, flush)
+            out["other_coding"] = other_coding_leg(a, dev, flush)
         if not a.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(a)
     eng.close()
@@ -291,6 +292,31 @@ def plain_leg(a, dev, flush) -> dict:
     return out
 
 
+def other_coding_leg(a, dev, flush) -> dict:
+    """The same workload in the other coding (SSC for an MSC run and vice
+    versa): batched like the headline and plain (one population, graph)."""
+    import torch
+
+    import paising_gb300 as pa
+    coding = "ssc" if a.coding == "msc" else "msc"
+    out = {"coding": coding}
+    for key, runs in (("batched", a.populations), ("plain_graph", 1)):
+        with pa.Engine(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=runs, seed=777,
+                       coding=coding, rng="native", weights="fp32", graph=True, device=dev) as e:
+            e.run()
+            ms, att = [], []
+            for _ in range(max(1, a.steps // 2)):
+                flush.zero_()
+                torch.cuda.synchronize(dev)
+                e.run()
+                t, n = e.timing()
+                ms.append(t)
+                att.append(n)
+        out[key] = {"value": sum(att) / (sum(ms) * 1e6), "unit": UNIT, "ms_per_anneal": sum(ms) / len(ms),
+                    "populations": runs}
+    return out
+
+
 def profile_leg(a, eng, pa) -> dict:
     """Per-kernel device times of one run (CUDA events around each launch on
     the engine's stream) and the roofline of the dominant kernel."""
@@ -305,8 +331,11 @@ def profile_leg(a, eng, pa) -> dict:
     attempts_per_launch = a.sweeps * N * Rs.mean()
     # algorithmic INT32 operations per spin-flip attempt: MSC ~5 (bitsliced
     # neighbour count and acceptance mask shared by 32 replicas), SSC ~33 (a
-    # 32-bit Philox word, ~25 operations, plus the update of one site)
-    ops_per_attempt = 5.0 if a.coding == "msc" else 33.0
+    # 32-bit Philox word, ~25 operations, plus the update of one site).  The
+    # native SSC sweep at L = 64, 128, 256 runs on bit planes (32 sites of one
+    # replica per word) and so does the bitsliced work of the MSC figure.
+    ssc_bits = a.coding == "ssc" and a.L in (64, 128, 256)
+    ops_per_attempt = 5.0 if a.coding == "msc" or ssc_bits else 33.0
     achieved = attempts_per_launch * ops_per_attempt / (avg_ms * 1e-3) / 1e12
     peaks = pa.probe_int_issue(eng.config.device)
     peak = max(peaks) / 1e12

@@ -352,7 +352,7 @@ constexpr int kResChunk = 1024;
 constexpr int kResampleThreads = 256;
 
 __global__ void __launch_bounds__(kResampleThreads) msc_resample_kernel(PopDev* pops) {
-  __shared__ uint32_t s_off[kMsb], s_sh[kMsb];
+  __shared__ uint32_t s_off[kMsb], s_rot[kMsb];  // source word offset; rotation moving its bit to bit k
   __shared__ uint32_t s_valid;
   PopDev* st = pops + blockIdx.y;
   if (!pop_stepping(st)) return;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kResampleThreads) msc_resample_kernel(PopDev* 
       const bool v = s < Rn;
       const uint32_t lin = v ? src[s] : 0u;  // an invalid bit reads old word 0 and is masked off
       s_off[tid] = (lin >> 5) * (uint32_t)N;
-      s_sh[tid] = lin & 31u;
+      s_rot[tid] = ((uint32_t)tid - (lin & 31u)) & 31u;
       const uint32_t m = __ballot_sync(kFull, v);
       if (tid == 0) s_valid = m;
       if (c == 0) act[j * kMsb + tid] = v ? 1 : 0;
@@ -382,7 +382,10 @@ __global__ void __launch_bounds__(kResampleThreads) msc_resample_kernel(PopDev* 
     for (int t = c * kResChunk + tid; t < t1; t += blockDim.x) {
       uint32_t w = 0;
 #pragma unroll 16
-      for (int k = 0; k < kMsb; ++k) w |= ((__ldg(old + s_off[k] + t) >> s_sh[k]) & 1u) << k;
+      for (int k = 0; k < kMsb; ++k) {
+        const uint32_t v = __ldg(old + s_off[k] + t);
+        w |= __funnelshift_l(v, v, s_rot[k]) & (1u << k);  // source bit rotated into bit k
+      }
       neu[(size_t)j * N + t] = w & vmask;
     }
   }
