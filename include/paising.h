@@ -87,6 +87,9 @@ typedef struct pa_config {
                          PA_MHR_results_run_<r>.dat) */
   int store_energies; /* 1: keep the energies of every temperature, the reference's EnergiesPopStore
                          build (PAisingSSC.cu:24,563-578): pa_get_energies, PA_energies_<i>.dat */
+  int family;         /* 1: family statistics at every temperature (no counterpart in the reference):
+                         every replica carries the initial replica it descends from through the
+                         resampling; pa_get_family_rows, PA_family_run_<r>.dat */
 } pa_config;
 
 /* One line of PA_results_run_<r>.dat (PAisingSSC.cu:679-690), per site. */
@@ -157,6 +160,13 @@ PA_API int pa_get_mhr_rows(const pa_handle* h, int set, double* rows, int max_ro
  * contents of PA_energies_<step>.dat (PAisingSSC.cu:563-578).  At most max
  * values are copied; *n receives the population size. */
 PA_API int pa_get_energies(const pa_handle* h, int set, int step, int32_t* out, int max, int* n);
+
+/* Family statistics of result set `set` (config family = 1), 3 doubles per
+ * temperature: the number of families (initial replicas with descendants),
+ * rho_t = sum_f c_f^2 / R and the family entropy S_f = -sum_f (c_f/R)
+ * ln(c_f/R), c_f the replicas descended from initial replica f.  No
+ * counterpart in the reference. */
+PA_API int pa_get_family_rows(const pa_handle* h, int set, double* rows, int max_rows, int* nrows);
 
 /* Device time of the last pa_run in milliseconds (CUDA events around all
  * runs), and the reference's spin-flip attempt count

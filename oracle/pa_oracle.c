@@ -364,8 +364,8 @@ double or_msc_q(const int32_t* E, const uint8_t* active, int rg, double dB, doub
             f[k] = active[b * MSB + k] ? exp(-dB * (E[b * MSB + k] - Emean)) : 0.0;
         g[b] = warp_tree(f);
     }
-    int nb = (rg + NT - 1) / NT;
-    double* part = (double*)malloc(sizeof(double) * (nb ? nb : 1));
+    const int nb = rg > 0 ? (rg + NT - 1) / NT : 0;
+    double* part = (double*)malloc(sizeof(double) * (size_t)(nb > 0 ? nb : 1));
     double buf[NT];
     for (int b = 0; b < nb; ++b) {
         for (int t = 0; t < NT; ++t) buf[t] = (t + NT * b < rg) ? g[t + NT * b] : 0.0;
@@ -457,21 +457,51 @@ static double next_step(int msc, const int32_t* E, const uint8_t* act, int rg, i
     return (Bprev < Bfin && Bprev + dBmean > Bfin) ? Bfin - Bprev : dBmean;
 }
 
+/* Family statistics of a population (not written by the reference; the
+ * usual equilibration diagnostics of population annealing): with c_f the
+ * replicas descended from initial replica f and R the population size,
+ * out = {number of families with c_f > 0, rho_t = sum_f c_f^2 / R,
+ *        S_f = -sum_f (c_f/R) ln(c_f/R) = ln R - (1/R) sum_f c_f ln c_f}.
+ * anc[i] is the ancestor of replica slot i (MSC: linear 32*group + bit,
+ * counted where active). */
+static void family_stats(const int32_t* anc, const uint8_t* act, int n, int Rinit, int R, double out[3]) {
+    uint32_t* cnt = (uint32_t*)calloc((size_t)Rinit, sizeof(uint32_t));
+    for (int i = 0; i < n; ++i)
+        if (!act || act[i]) cnt[anc[i]]++;
+    long long nf = 0, c2 = 0;
+    double clnc = 0.0;
+    for (int f = 0; f < Rinit; ++f) {
+        const long long c = cnt[f];
+        if (!c) continue;
+        nf++;
+        c2 += c * c;
+        clnc += (double)c * log((double)c);
+    }
+    out[0] = (double)nf;
+    out[1] = (double)c2 / R;
+    out[2] = log((double)R) - clnc / R;
+    free(cnt);
+}
+
 int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
-               double* attempts);
+               double* fam, double* attempts);
 
 int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
               int max_steps, double* rows, int max_rows, double* attempts) {
     return or_anneal2(msc, L, Rinit, sweeps, dBinit, Bfin, runs, seed, max_steps, 0, 0.0, 0.0, rows, max_rows,
-                      attempts);
+                      NULL, attempts);
 }
 
 /* or_anneal with the adaptive temperature step (adaptive = 1): the first run
- * chooses its schedule, later runs replay it (PAisingSSC.cu:644,662). */
+ * chooses its schedule, later runs replay it (PAisingSSC.cu:644,662).  fam
+ * (optional) receives per run and temperature the family statistics above
+ * (max_rows x 3 per run); the ancestors follow the replicas through every
+ * resampling (SSC: new replica offs[j] + p copies old j; MSC: offspring s at
+ * group s % rg_new, bit s / rg_new, PAisingMSC.cu:413-414). */
 int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
-               double* attempts) {
+               double* fam, double* attempts) {
     int N = L * L;
     const int nBmax = 10000;
     double* B = (double*)calloc(nBmax, sizeof(double));
@@ -500,6 +530,11 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
         int32_t* Mm = (int32_t*)malloc(sizeof(int32_t) * (size_t)rgcap * MSB);
         uint32_t* roff = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)rgcap * MSB);
         uint32_t* offs = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)rgcap * MSB);
+        int32_t* anc = (int32_t*)calloc((size_t)rgcap * MSB, sizeof(int32_t));
+        int32_t* anc2 = (int32_t*)calloc((size_t)rgcap * MSB, sizeof(int32_t));
+        double* fr = fam ? fam + (size_t)r * max_rows * 3 : NULL;
+        for (int j = 0; j < Rinit; ++j) anc[j] = j;  /* MSC: linear 32*group + bit */
+        if (fr) family_stats(anc, NULL, Rinit, Rinit, Rinit, fr);
         if (!msc) {
             sp = (int8_t*)malloc((size_t)Rcap * N);
             sp2 = (int8_t*)malloc((size_t)Rcap * N);
@@ -531,7 +566,11 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                 if ((int)Rnew > Rcap) { ret = -1; break; }
                 or_ssc_resample(sp, L, Rp, roff, offs, sp2);
                 int8_t* t = sp; sp = sp2; sp2 = t;
+                for (int j = 0; j < Rp; ++j)
+                    for (uint32_t p = 0; p < roff[j]; ++p) anc2[offs[j] + p] = anc[j];
+                int32_t* ta2 = anc; anc = anc2; anc2 = ta2;
                 Rn[i] = (int)Rnew;
+                if (fr) family_stats(anc, NULL, Rn[i], Rinit, Rn[i], fr + (size_t)i * 3);
                 double tab[10];
                 or_ssc_boltz(B[i], tab);
                 or_ssc_sweep(sp, L, Rn[i], sweeps, tab, seed, iseq);
@@ -550,10 +589,17 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                 int rgn = (int)((Rnew + MSB - 1) / MSB);
                 memset(wd2, 0, (size_t)rgn * N * 4);
                 or_msc_resample(wd, Ev, L, rg, roff, offs, rgn, wd2, act2, NULL);
+                for (int lin = 0; lin < rg * MSB; ++lin)
+                    for (uint32_t p = 0; p < roff[lin]; ++p) {
+                        const uint32_t s = offs[lin] + p;
+                        anc2[(s % rgn) * MSB + s / rgn] = anc[lin];
+                    }
+                int32_t* ta2 = anc; anc = anc2; anc2 = ta2;
                 uint32_t* t = wd; wd = wd2; wd2 = t;
                 uint8_t* ta = act; act = act2; act2 = ta;
                 rg = rgn;
                 Rn[i] = (int)Rnew;
+                if (fr) family_stats(anc, act, rg * MSB, Rinit, Rn[i], fr + (size_t)i * 3);
                 uint32_t thr[2];
                 or_msc_thresholds(B[i], thr);
                 or_msc_sweep(wd, L, rg, sweeps, thr, seed, iseq);
@@ -591,7 +637,7 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
             }
         }
         free(sp); free(sp2); free(wd); free(wd2); free(act); free(act2);
-        free(Ev); free(Mm); free(roff); free(offs);
+        free(Ev); free(Mm); free(roff); free(offs); free(anc); free(anc2);
     }
     if (attempts) *attempts = tot_att;
     free(B); free(E); free(C); free(Mv); free(M2); free(M4); free(lnQ); free(BF); free(S); free(Rn);

@@ -41,7 +41,7 @@ _SIGS = {
     "or_msc_copy_numbers": ([_vp, _vp, _i, _i, _i, _d, _d, _u64, _u64, _vp], _u32),
     "or_msc_resample": ([_vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp, _vp], None),
     "or_anneal": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _vp, _i, _vp], _i),
-    "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp], _i),
+    "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
 }
 
@@ -219,14 +219,26 @@ def anneal(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005, beta_
     """Rows of PA_results_run_<r>.dat for every run (shape runs x nrows x 10)
     and the spin-flip attempt count.  adaptive: the AdaptiveStep build, with
     dbeta the first step."""
+    rows, _, att = anneal_family(coding, L, R, sweeps, dbeta, beta_final, runs, seed, max_steps, adaptive,
+                                 min_overlap, max_overlap, family=False)
+    return rows, att
+
+
+def anneal_family(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005, beta_final: float = 1.0,
+                  runs: int = 1, seed: int = 1, max_steps: int = 0, adaptive: bool = False,
+                  min_overlap: float = 0.85, max_overlap: float = 0.87, family: bool = True):
+    """anneal() plus the family statistics of every temperature (runs x nrows
+    x 3: families, rho_t, S_f)."""
     maxr = 10000 if adaptive else int(beta_final / dbeta) + 8
     rows = np.zeros((runs, maxr, 10))
+    fam = np.zeros((runs, maxr, 3)) if family else None
     att = ctypes.c_double()
     n = lib().or_anneal2(1 if coding == "msc" else 0, L, R, sweeps, dbeta, beta_final, runs, seed, max_steps,
-                         int(adaptive), min_overlap, max_overlap, _p(rows), maxr, ctypes.byref(att))
+                         int(adaptive), min_overlap, max_overlap, _p(rows), maxr,
+                         _p(fam) if family else None, ctypes.byref(att))
     if n < 0:
         raise RuntimeError("oracle anneal failed")
-    return rows[:, :n], att.value
+    return rows[:, :n], (fam[:, :n] if family else None), att.value
 
 
 def kaufman(L: int, beta: float):

@@ -52,7 +52,7 @@ class Config(ctypes.Structure):
                 ("graph", ctypes.c_int), ("device", ctypes.c_int), ("capacity", ctypes.c_double),
                 ("sweep_variant", ctypes.c_int), ("tile_groups", ctypes.c_int), ("adaptive", ctypes.c_int),
                 ("min_overlap", ctypes.c_double), ("max_overlap", ctypes.c_double), ("mhr", ctypes.c_int),
-                ("store_energies", ctypes.c_int)]
+                ("store_energies", ctypes.c_int), ("family", ctypes.c_int)]
 
 
 class Row(ctypes.Structure):
@@ -72,6 +72,7 @@ _SIGS = {
     "pa_autotune": ([_vp, _vp, _i], _i),
     "pa_get_mhr_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_energies": ([_vp, _i, _i, _vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_get_family_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
@@ -135,14 +136,14 @@ _W = {"fp32": WEIGHTS_FP32, "fp64": WEIGHTS_FP64, WEIGHTS_FP32: WEIGHTS_FP32, WE
 def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, seed=1, coding="ssc",
                 rng="native", weights="fp32", graph=True, device=0, capacity=1.25, sweep_variant=0,
                 tile_groups=0, adaptive=False, min_overlap=0.0, max_overlap=0.0, mhr=False,
-                store_energies=False) -> Config:
+                store_energies=False, family=False) -> Config:
     """sweep_variant: CTAs per MSC group in the sweep kernel (0 automatic,
     1 one CTA, 2 or 4 a thread-block cluster); tile_groups: MSC groups per
     work unit of the one-CTA sweep (0 automatic, 1, 2, 4 or 8); adaptive:
     the reference's adaptive temperature step with histogram overlap in
     [min_overlap, max_overlap) (0 selects the reference's 0.85 / 0.87); mhr:
     multi-histogram reweighting after every run; store_energies: keep every
-    temperature's energies."""
+    temperature's energies; family: family statistics every temperature."""
     c = Config()
     _check(lib().pa_config_init(ctypes.byref(c)))
     c.L, c.R, c.sweeps, c.dbeta, c.beta_final, c.runs = int(L), int(R), int(sweeps), float(dbeta), float(beta_final), int(runs)
@@ -150,7 +151,7 @@ def make_config(L=64, R=20000, sweeps=100, dbeta=0.005, beta_final=1.0, runs=1, 
     c.graph, c.device, c.capacity = int(bool(graph)), int(device), float(capacity)
     c.sweep_variant, c.tile_groups = int(sweep_variant), int(tile_groups)
     c.adaptive, c.min_overlap, c.max_overlap = int(bool(adaptive)), float(min_overlap), float(max_overlap)
-    c.mhr, c.store_energies = int(bool(mhr)), int(bool(store_energies))
+    c.mhr, c.store_energies, c.family = int(bool(mhr)), int(bool(store_energies)), int(bool(family))
     return c
 
 
@@ -192,6 +193,14 @@ class Engine:
         _check(lib().pa_get_mhr_rows(self._h, set_index, None, 0, ctypes.byref(n)), self._h)
         out = np.zeros((n.value, 4))
         _check(lib().pa_get_mhr_rows(self._h, set_index, out.ctypes.data, n.value, ctypes.byref(n)), self._h)
+        return out
+
+    def family_rows(self, set_index: int = 0) -> np.ndarray:
+        """Family statistics of a result set: rows of (families, rho_t, S_f)."""
+        n = ctypes.c_int()
+        _check(lib().pa_get_family_rows(self._h, set_index, None, 0, ctypes.byref(n)), self._h)
+        out = np.zeros((n.value, 3))
+        _check(lib().pa_get_family_rows(self._h, set_index, out.ctypes.data, n.value, ctypes.byref(n)), self._h)
         return out
 
     def energies(self, set_index: int = 0, step: int = 0) -> np.ndarray:

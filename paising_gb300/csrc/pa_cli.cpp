@@ -10,7 +10,8 @@
 // output directory ./data%s_L%d_R%d_EqSw%d/, PAisingSSC.cu:406-410), -T (time
 // the MSC tile sizes before the run, pa_autotune), -H (multi-histogram
 // reweighting, the MHR build: PA_MHR_results_run_<r>.dat), -E (energies of
-// every temperature, the EnergiesPopStore build: PA_energies_<i>.dat).
+// every temperature, the EnergiesPopStore build: PA_energies_<i>.dat), -F
+// (family statistics, PA_family_run_<r>.dat; not in the reference).
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -45,7 +46,8 @@ static void usage(const char* prog) {
       " -a                 ( adaptive temperature step, MinOverlap 0.85, MaxOverlap 0.87 )\n"
       " -T                 ( autotune the MSC sweep's tile sizes before the run )\n"
       " -H                 ( multi-histogram reweighting: PA_MHR_results_run_<r>.dat )\n"
-      " -E                 ( store the energies of every temperature: PA_energies_<i>.dat )\n",
+      " -E                 ( store the energies of every temperature: PA_energies_<i>.dat )\n"
+      " -F                 ( family statistics of every temperature: PA_family_run_<r>.dat )\n",
       prog);
 }
 
@@ -59,7 +61,7 @@ int main(int argc, char** argv) {
   std::string dir;
   int opt;
   opterr = 0;
-  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aTHE?")) != -1) {
+  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aTHEF?")) != -1) {
     int i;
     double f;
     switch (opt) {  // same acceptance rules as PAisingSSC.cu:390-398
@@ -81,6 +83,7 @@ int main(int argc, char** argv) {
       case 'T': tune = true; break;
       case 'H': c.mhr = 1; break;
       case 'E': c.store_energies = 1; break;
+      case 'F': c.family = 1; break;
       default:
         if (optopt && optopt != '?') std::printf("illegal option -- %c\n", optopt);
         usage(argv[0]);

@@ -170,6 +170,8 @@ struct pa_handle {
   bool ran = false;  // pa_run has been called
   int runs_done = 0;  // completed runs: the first one chooses adaptive schedules, the others replay them
   bool records = false;  // some population keeps an MHR histogram or its energies
+  bool family = false;   // some population keeps family statistics
+  std::vector<std::vector<double>> fam;  // per set: rows of (families, rho_t, S_f)
   std::vector<std::vector<double>> mhr;                    // per set: rows of (beta, E/N, C/N, betaF/N)
   std::vector<std::vector<std::vector<int32_t>>> energies;  // per set, per temperature: energies
   std::vector<int> drained;                                 // per population: last temperature read back
@@ -214,8 +216,12 @@ struct pa_handle {
                   : launch_sweep(d_batch, coding, rng_mode, energy_only, stream_seed, sweep, stream);
   }
 
+  // after finish_step: energy records and family statistics of the temperature just finished
   cudaError_t enqueue_record() {
-    return records ? launch("record", [&] { return launch_record(d_pops, npop, rblocks, stream); }) : cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (records) e = launch("record", [&] { return launch_record(d_pops, npop, rblocks, stream); });
+    if (e == cudaSuccess && family) e = launch("family", [&] { return launch_family_stats(d_pops, npop, rblocks, stream); });
+    return e;
   }
 
   cudaError_t enqueue_init() {
@@ -227,6 +233,9 @@ struct pa_handle {
         return e;
     if ((e = launch("begin_run", [&] { return launch_begin_run(d_pops, npop, stream); })) != cudaSuccess) return e;
     if ((e = launch(msc ? "msc_init" : "ssc_init", [&] { return launch_init(d_pops, npop, coding, stream); })) != cudaSuccess)
+      return e;
+    if (family && (e = launch("family_init", [&] { return launch_family_init(d_pops, npop, rblocks, stream); })) !=
+                      cudaSuccess)
       return e;
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 1, stream); })) != cudaSuccess) return e;
     e = launch(msc ? "msc_energy" : "ssc_energy", [&] { return sweep_launch(1); });
@@ -244,6 +253,9 @@ struct pa_handle {
     if ((e = launch("scatter", [&] { return launch_scatter(d_pops, npop, rblocks, stream); })) != cudaSuccess) return e;
     e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_pops, npop, coding, stream); });
     if (e != cudaSuccess) return e;
+    if (family && (e = launch("family_resample", [&] { return launch_family_resample(d_pops, npop, rblocks, stream); })) !=
+                      cudaSuccess)
+      return e;
     if ((e = launch("plan", [&] { return launch_plan(d_batch, npop, 0, stream); })) != cudaSuccess) return e;
     e = launch(msc ? "msc_sweep" : "ssc_sweep", [&] { return sweep_launch(0); });
     if (e != cudaSuccess) return e;
@@ -482,8 +494,9 @@ int validate(const pa_config& c) {
     return bad("SSC needs L % 8 == 0, 8 <= L <= 256");
   }
   if (c.adaptive != 0 && c.adaptive != 1) return bad("adaptive must be 0 or 1");
-  if ((c.mhr != 0 && c.mhr != 1) || (c.store_energies != 0 && c.store_energies != 1))
-    return bad("mhr and store_energies must be 0 or 1");
+  if ((c.mhr != 0 && c.mhr != 1) || (c.store_energies != 0 && c.store_energies != 1) ||
+      (c.family != 0 && c.family != 1))
+    return bad("mhr, store_energies and family must be 0 or 1");
   if (c.adaptive) {
     const double lo = c.min_overlap > 0 ? c.min_overlap : kMinOverlap;
     const double hi = c.max_overlap > 0 ? c.max_overlap : kMaxOverlap;
@@ -646,6 +659,16 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       h.rec |= kRecEnergies;
     }
     if (h.rec) H->records = true;
+    if (c.family) {
+      chk(B.alloc(&h.anc[0], units));
+      chk(B.alloc(&h.anc[1], units));
+      chk(B.alloc(&h.fam_cnt, (size_t)c.R));
+      chk(B.alloc(&h.fam_rows, (size_t)P.cap * 3));
+      chk(B.alloc(&h.fam_part, (size_t)kResBlocksMax * 3));
+      if (e == cudaSuccess) chk(cudaMemset(h.fam_cnt, 0, sizeof(uint32_t) * (size_t)c.R));
+      h.family = 1;
+      H->family = true;
+    }
     if (c.adaptive) {
       chk(B.alloc(&h.hist, (size_t)N + 1));
       h.adaptive = 1;
@@ -778,6 +801,7 @@ int pa_run(pa_handle* H) {
   H->rows.assign((size_t)H->npop * H->seq_runs, {});
   H->mhr.assign((size_t)H->npop * H->seq_runs, {});
   H->energies.assign((size_t)H->npop * H->seq_runs, {});
+  H->fam.assign((size_t)H->npop * H->seq_runs, {});
   H->sets_done = 0;
   H->attempts = 0;
   H->ran = true;
@@ -830,6 +854,12 @@ int pa_run(pa_handle* H) {
         e = cudaMemcpy(hist.data(), P.h.mhr_hist, sizeof(unsigned long long) * hist.size(), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return H->cuda_fail(e, "MHR histogram");
         H->mhr[(size_t)r * H->npop + P.user_index] = mhr_analysis(P.h.N, rw, hist);
+      }
+      if (P.h.family && !back[k].error) {
+        std::vector<double>& f = H->fam[(size_t)r * H->npop + P.user_index];
+        f.assign(rw.size() / kRowCols * 3, 0.0);
+        e = cudaMemcpy(f.data(), P.h.fam_rows, sizeof(double) * f.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return H->cuda_fail(e, "family statistics");
       }
     }
     if (status == PA_OK) {
@@ -925,6 +955,16 @@ int pa_get_mhr_rows(const pa_handle* H, int set, double* rows, int max_rows, int
   const std::vector<double>& src = H->mhr[set];
   const int n = (int)(src.size() / 4), m = std::min(n, max_rows);
   if (m > 0) std::memcpy(rows, src.data(), sizeof(double) * 4 * (size_t)m);
+  if (nrows) *nrows = n;
+  return PA_OK;
+}
+
+int pa_get_family_rows(const pa_handle* H, int set, double* rows, int max_rows, int* nrows) {
+  if (!H || (max_rows > 0 && !rows)) return PA_ERR_ARG;
+  if (set < 0 || set >= H->sets_done || H->fam[set].empty()) return PA_ERR_STATE;
+  const std::vector<double>& src = H->fam[set];
+  const int n = (int)(src.size() / 3), m = std::min(n, max_rows);
+  if (m > 0) std::memcpy(rows, src.data(), sizeof(double) * 3 * (size_t)m);
   if (nrows) *nrows = n;
   return PA_OK;
 }
@@ -1040,6 +1080,17 @@ int pa_write_results(const pa_handle* H, const char* dir, int precision) {
         for (int k = 0; k < 4; ++k) std::fprintf(g, "%.*g ", precision, m[i * 4 + k]);
         std::fprintf(g, "\n");
       }
+      std::fclose(g);
+    }
+    // PA_family_run_<r>.dat: beta, families, rho_t, S_f (no reference counterpart)
+    if (!H->fam[r].empty()) {
+      std::string fp = path.substr(0, path.rfind('/') + 1) + "PA_family_run_" + std::to_string(r) + ".dat";
+      FILE* g = std::fopen(fp.c_str(), "w");
+      if (!g) return PA_ERR_ARG;
+      const std::vector<double>& fr = H->fam[r];
+      for (size_t i = 0; i < fr.size() / 3; ++i)
+        std::fprintf(g, "%.*g %d %.*g %.*g\n", precision, o[i * kRowCols], (int)fr[i * 3], precision, fr[i * 3 + 1],
+                     precision, fr[i * 3 + 2]);
       std::fclose(g);
     }
   }

@@ -98,6 +98,11 @@ cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s);
 // Populations with records: histogram / energy ring of the temperature just
 // finished (after launch_finish_step); `blocks` from res_blocks().
 cudaError_t launch_record(PopDev* pops, int npop, int blocks, cudaStream_t s);
+// Family statistics: ancestors set at the initial population, carried by
+// each resampling (after launch_resample), counted after launch_finish_step.
+cudaError_t launch_family_init(PopDev* pops, int npop, int blocks, cudaStream_t s);
+cudaError_t launch_family_resample(PopDev* pops, int npop, int blocks, cudaStream_t s);
+cudaError_t launch_family_stats(PopDev* pops, int npop, int blocks, cudaStream_t s);
 // Adaptive populations: choose the next temperature (after launch_finish_step).
 cudaError_t launch_adapt(PopDev* pops, int npop, cudaStream_t s);
 

@@ -277,6 +277,97 @@ __global__ void begin_run_kernel(PopDev* pops) {
   row[6] = st->bf0 / st->N;
   row[8] = (double)st->Rinit;
   st->last_rec = -1;
+  st->last_fam = -1;
+}
+
+// ------------------------------------------------------ family statistics
+// Not written by the reference: with c_f the replicas descended from initial
+// replica f and R the population size, every temperature records
+//   {families with c_f > 0, rho_t = sum_f c_f^2 / R,
+//    S_f = -sum_f (c_f/R) ln(c_f/R) = ln R - (1/R) sum_f c_f ln c_f}.
+// Ancestors are initial linear replica indices (MSC: 32 * group + bit) and
+// follow every copy the resampling makes.
+
+// After the initial population: every replica is its own family.
+__global__ void family_init_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  if (!st->family) return;
+  const int n = pop_units(st, st->R_cur), R = st->R_cur;
+  int32_t* a = st->anc[st->parity];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) a[j] = j < R ? j : -1;
+}
+
+// After the spin gather of a temperature step: new replica slots take the
+// ancestor of their source (SSC: slot s <- src[s]; MSC: slot 32 g + b holds
+// offspring s = b rg_new + g, PAisingMSC.cu:413-414).
+__global__ void family_resample_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  if (!st->family || !pop_stepping(st)) return;
+  const int Rn = st->R_cur, n = pop_units(st, Rn);
+  const int32_t* old = st->anc[st->parity ^ 1];
+  int32_t* neu = st->anc[st->parity];
+  const uint32_t* src = st->src;
+  const bool msc = st->coding == kMSC;
+  const int rgn = (Rn + kMsb - 1) / kMsb;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int s = msc ? (j & (kMsb - 1)) * rgn + (j >> 5) : j;
+    neu[j] = s < Rn ? old[src[s]] : -1;
+  }
+}
+
+// After finish_step: count the families of the temperature just finished
+// (once per temperature, like the records) ...
+__global__ void __launch_bounds__(kResThreads) family_count_kernel(PopDev* pops) {
+  PopDev* st = pops + blockIdx.y;
+  const int s = st->step - 1;
+  if (!st->family || s <= st->last_fam || st->error) return;
+  const int n = pop_units(st, st->R_cur);
+  const int32_t* a = st->anc[st->parity];
+  const uint8_t* act = st->coding == kMSC ? st->active[st->parity] : nullptr;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    if ((!act || act[j]) && a[j] >= 0) atomicAdd(&st->fam_cnt[a[j]], 1u);
+}
+
+// ... then reduce the counts (clearing them for the next temperature); the
+// last block combines the per-block partial sums in block order.
+__global__ void __launch_bounds__(kResThreads) family_reduce_kernel(PopDev* pops) {
+  __shared__ double s_d[33];
+  PopDev* st = pops + blockIdx.y;
+  const int s = st->step - 1;
+  if (!st->family || s <= st->last_fam || st->error) return;
+  const int nf_bins = st->Rinit;
+  double nf = 0.0, c2 = 0.0, clnc = 0.0;
+  int lo, hi;
+  block_chunk(nf_bins, lo, hi);
+  for (int f = lo + (int)threadIdx.x; f < hi; f += blockDim.x) {
+    const uint32_t c = st->fam_cnt[f];
+    if (!c) continue;
+    st->fam_cnt[f] = 0u;
+    const double cd = (double)c;
+    nf += 1.0;
+    c2 += cd * cd;
+    clnc += cd * log(cd);
+  }
+  nf = block_sum(nf, s_d);
+  c2 = block_sum(c2, s_d);
+  clnc = block_sum(clnc, s_d);
+  if (threadIdx.x == 0) {
+    st->fam_part[3 * blockIdx.x] = nf;
+    st->fam_part[3 * blockIdx.x + 1] = c2;
+    st->fam_part[3 * blockIdx.x + 2] = clnc;
+  }
+  if (last_block(&st->ticket) && threadIdx.x == 0) {
+    double a = 0.0, b2 = 0.0, c = 0.0;
+    const volatile double* p = st->fam_part;
+    for (int k = 0; k < (int)gridDim.x; ++k) { a += p[3 * k]; b2 += p[3 * k + 1]; c += p[3 * k + 2]; }
+    const double R = (double)st->R_cur;
+    double* row = st->fam_rows + (size_t)s * 3;
+    row[0] = a;
+    row[1] = b2 / R;
+    row[2] = log(R) - c / R;
+    st->last_fam = s;
+    st->ticket = 0;
+  }
 }
 
 // ---------------------------------------------- per-temperature records
@@ -516,6 +607,24 @@ cudaError_t launch_begin_run(PopDev* pops, int npop, cudaStream_t s) {
 
 cudaError_t launch_finish_step(PopDev* pops, int npop, cudaStream_t s) {
   finish_step_kernel<<<npop, 1, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_family_init(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  family_init_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_family_resample(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  family_resample_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_family_stats(PopDev* pops, int npop, int blocks, cudaStream_t s) {
+  family_count_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  family_reduce_kernel<<<dim3(blocks, npop), kResThreads, 0, s>>>(pops);
   return cudaGetLastError();
 }
 

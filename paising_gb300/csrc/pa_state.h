@@ -84,6 +84,13 @@ struct PopDev {
   int32_t* elog;       // [ring][units] energies of recorded temperatures
   uint8_t* alog;       // MSC: [ring][units] active flags of the same
   int* nlog;           // [ring] units recorded per slot
+  // ------------------------------------------------ family statistics
+  int family;          // 1: ancestors follow the replicas; statistics every temperature
+  int last_fam;        // last temperature whose statistics are done in this run (-1: none)
+  int32_t* anc[2];     // [units] initial replica each slot descends from, double-buffered like spins
+  uint32_t* fam_cnt;   // [Rinit] replicas per family; zero between temperatures
+  double* fam_rows;    // [rows][3] families, rho_t, S_f per temperature
+  double* fam_part;    // [kResBlocksMax][3] per-block partial sums
 };
 
 constexpr int kRecMhr = 1, kRecEnergies = 2;

@@ -110,3 +110,16 @@ def test_schedule_has_200_rows(engine_lib):
         while py[-1] + d <= 1.0:
             py.append(py[-1] + d)
         assert list(pa.schedule(d, 1.0)) == py
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_oracle_family_statistics_definition(oracle, coding):
+    """Family statistics of the oracle (the definition the engine is checked
+    against): R families at beta = 0 with rho_t = 1 and S_f = ln R; counts
+    never grow; S_f <= ln(families); rho_t >= R / families (Cauchy-Schwarz)."""
+    rows, fam, _ = oracle.anneal_family(coding, 16, 600, 5, 0.05, 1.0, 1, 9)
+    f, r = fam[0], rows[0]
+    assert f[0, 0] == 600 and f[0, 1] == 1.0 and f[0, 2] == pytest.approx(np.log(600))
+    assert np.all(np.diff(f[:, 0]) <= 0)
+    assert np.all(f[:, 2] <= np.log(f[:, 0]) + 1e-12)
+    assert np.all(f[:, 1] >= r[:, 8] / f[:, 0] - 1e-9)
