@@ -161,6 +161,15 @@ PA_API int pa_get_mhr_rows(const pa_handle* h, int set, double* rows, int max_ro
  * values are copied; *n receives the population size. */
 PA_API int pa_get_energies(const pa_handle* h, int set, int step, int32_t* out, int max, int* n);
 
+/* The reference's LatticePopStore build (PAisingSSC.cu:25,580-605): during the
+ * handle's first run, after every temperature i >= 1 the population is
+ * appended as text to dir/PA_lattice_<i>.dat ("i=..; beta=..; R=..;" and one
+ * "P={{row},..};" line per replica, `precision` digits for beta).  The run is
+ * then stepped from the host.  MSC populations (not in the reference) list
+ * their active replicas group-major.  One population per handle; dir = NULL
+ * switches the dumps off. */
+PA_API int pa_set_lattice_dump(pa_handle* h, const char* dir, int precision);
+
 /* Family statistics of result set `set` (config family = 1), 3 doubles per
  * temperature: the number of families (initial replicas with descendants),
  * rho_t = sum_f c_f^2 / R and the family entropy S_f = -sum_f (c_f/R)

@@ -17,7 +17,8 @@ changes are the ones CUDA 13 forces or the comparison needs:
   reference's compile-time switch for its adaptive temperature step
   (PAisingSSC.cu:23, PAisingMSC.cu:23); the ``inj_records`` variants define
   ``MHR`` and ``EnergiesPopStore`` (multi-histogram reweighting and the
-  per-temperature energy files, PAisingSSC.cu:22,24).
+  per-temperature energy files, PAisingSSC.cu:22,24); the ``inj_lattice``
+  variant (SSC, L=16) defines ``LatticePopStore`` (PAisingSSC.cu:25).
 
 Step 1 (patch) needs the reference checkout and runs in the build container;
 step 2 (nvcc) runs wherever the patched sources are, e.g. on the GPU host,
@@ -102,6 +103,8 @@ def _compile(src: str, variant: str) -> str:
         cmd[1:1] = ["-DAdaptiveStep"]
     if variant.endswith("records"):  # its MHR and EnergiesPopStore builds (lines 22, 24)
         cmd[1:1] = ["-DMHR", "-DEnergiesPopStore"]
+    if variant.endswith("lattice"):  # its LatticePopStore build (PAisingSSC.cu line 25; SSC only)
+        cmd[1:1] = ["-DLatticePopStore"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {out}:\n{r.stderr[-2000:]}")
@@ -113,6 +116,7 @@ def compile_all(jobs: int) -> list[str]:
     srcs = sorted(f for f in os.listdir(SRC_OUT) if f.endswith(".cu") and f.startswith("PAising"))
     tasks = [(os.path.join(SRC_OUT, s), v) for s in srcs for v in ("inj", "curand")]
     tasks += [(os.path.join(SRC_OUT, s), v) for s in srcs if s.endswith("_L16.cu") for v in ("inj_adaptive", "inj_records")]
+    tasks += [(os.path.join(SRC_OUT, s), "inj_lattice") for s in srcs if s == "PAisingSSC_L16.cu"]
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         return list(ex.map(lambda a: _compile(*a), tasks))
 

@@ -73,6 +73,7 @@ _SIGS = {
     "pa_get_mhr_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_energies": ([_vp, _i, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_family_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_set_lattice_dump": ([_vp, ctypes.c_char_p, _i], _i),
     "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
@@ -194,6 +195,12 @@ class Engine:
         out = np.zeros((n.value, 4))
         _check(lib().pa_get_mhr_rows(self._h, set_index, out.ctypes.data, n.value, ctypes.byref(n)), self._h)
         return out
+
+    def set_lattice_dump(self, directory: str | None, precision: int = 11) -> None:
+        """Per-temperature population text files of the first run
+        (PA_lattice_<i>.dat); None switches them off."""
+        d = None if directory is None else directory.encode()
+        _check(lib().pa_set_lattice_dump(self._h, d, int(precision)), self._h)
 
     def family_rows(self, set_index: int = 0) -> np.ndarray:
         """Family statistics of a result set: rows of (families, rho_t, S_f)."""

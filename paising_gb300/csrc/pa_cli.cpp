@@ -11,7 +11,8 @@
 // the MSC tile sizes before the run, pa_autotune), -H (multi-histogram
 // reweighting, the MHR build: PA_MHR_results_run_<r>.dat), -E (energies of
 // every temperature, the EnergiesPopStore build: PA_energies_<i>.dat), -F
-// (family statistics, PA_family_run_<r>.dat; not in the reference).
+// (family statistics, PA_family_run_<r>.dat; not in the reference), -S (the
+// LatticePopStore build: PA_lattice_<i>.dat of run 0).
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -47,7 +48,8 @@ static void usage(const char* prog) {
       " -T                 ( autotune the MSC sweep's tile sizes before the run )\n"
       " -H                 ( multi-histogram reweighting: PA_MHR_results_run_<r>.dat )\n"
       " -E                 ( store the energies of every temperature: PA_energies_<i>.dat )\n"
-      " -F                 ( family statistics of every temperature: PA_family_run_<r>.dat )\n",
+      " -F                 ( family statistics of every temperature: PA_family_run_<r>.dat )\n"
+      " -S                 ( store the lattices of every temperature of run 0: PA_lattice_<i>.dat )\n",
       prog);
 }
 
@@ -57,11 +59,11 @@ int main(int argc, char** argv) {
   c.coding = PA_CODING_MSC;
   c.seed = (uint64_t)time(nullptr);  // RNGseed = time(NULL) (PAisingSSC.cu:31)
   int precision = 11;
-  bool tune = false;
+  bool tune = false, lattices = false;
   std::string dir;
   int opt;
   opterr = 0;
-  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aTHEF?")) != -1) {
+  while ((opt = getopt(argc, argv, "R:t:d:f:M:s:P:o:L:c:m:w:g:D:aTHEFS?")) != -1) {
     int i;
     double f;
     switch (opt) {  // same acceptance rules as PAisingSSC.cu:390-398
@@ -84,6 +86,7 @@ int main(int argc, char** argv) {
       case 'H': c.mhr = 1; break;
       case 'E': c.store_energies = 1; break;
       case 'F': c.family = 1; break;
+      case 'S': lattices = true; break;
       default:
         if (optopt && optopt != '?') std::printf("illegal option -- %c\n", optopt);
         usage(argv[0]);
@@ -116,6 +119,7 @@ int main(int argc, char** argv) {
     return 1;
   }
   if (tune) st = pa_autotune(h, nullptr, 0);
+  if (!st && lattices) st = pa_set_lattice_dump(h, dir.c_str(), precision);
   if (!st) st = pa_run(h);
   if (st) {
     std::fprintf(stderr, "Error: %s (%s)\n", pa_status_string(st), pa_last_error(h));

@@ -123,6 +123,63 @@ std::vector<double> mhr_analysis(int N, const std::vector<double>& rows, const s
   return out;
 }
 
+// Appends the population of temperature i to dir/PA_lattice_<i>.dat in the
+// reference's LatticePopStore text (PAisingSSC.cu:580-605): a header line
+// "i=..; beta=..; R=..;", then per replica "P={{..},{..},..};" with the L rows
+// of the lattice in x order (A and B sites interleaved, A first on even rows),
+// and an empty line.  MSC populations (no counterpart in the reference) list
+// their active replicas group-major.  spins: the coding's layout; act: MSC
+// active flags.
+int write_lattice(const std::string& dir, int i, double beta, int precision, int coding, int L, int R,
+                  const void* spins, const uint8_t* act, int units) {
+  std::string path = dir;
+  if (!path.empty() && path.back() != '/') path += '/';
+  path += "PA_lattice_" + std::to_string(i) + ".dat";
+  FILE* f = std::fopen(path.c_str(), "a");
+  if (!f) return PA_ERR_ARG;
+  std::fprintf(f, "i=%d; beta=%.*g; R=%d;\n", i, precision, beta, R);
+  const int N = L * L, h = N / 2, W = L / 2;
+  std::vector<int> s(N);
+  auto emit = [&]() {  // s: sublattice A then B, +-1
+    std::string line = "P={";
+    int ab = 0;
+    for (int k = 0; k < h; ++k) {
+      if (k % W == 0) {
+        line += '{';
+        ab = 1 - ab;
+      }
+      const int a = s[k], b = s[h + k];
+      line += std::to_string(ab ? a : b) + "," + std::to_string(ab ? b : a);
+      if ((k + 1) % W == 0) {
+        line += '}';
+        if (k + 1 < h) line += ',';
+      } else {
+        line += ',';
+      }
+    }
+    line += "};\n";
+    std::fputs(line.c_str(), f);
+  };
+  if (coding == PA_CODING_SSC) {
+    const int8_t* p = (const int8_t*)spins;
+    for (int j = 0; j < R; ++j) {
+      for (int x = 0; x < N; ++x) s[x] = p[(size_t)j * N + x];
+      emit();
+    }
+  } else {
+    const uint32_t* w = (const uint32_t*)spins;
+    for (int j = 0; j < units; ++j) {
+      if (!act[j]) continue;
+      const int g = j / 32, b = j % 32;
+      for (int x = 0; x < N; ++x) s[x] = (w[(size_t)g * N + x] >> b) & 1u ? 1 : -1;
+      emit();
+    }
+  }
+  std::fputs("\n", f);
+  std::fclose(f);
+  return PA_OK;
+}
+
 size_t population_bytes(int coding, int L, int R) {
   const size_t N = (size_t)L * L;
   return coding == PA_CODING_MSC ? (size_t)((R + kMsb - 1) / kMsb) * N * 4 : (size_t)R * N;
@@ -171,6 +228,9 @@ struct pa_handle {
   int runs_done = 0;  // completed runs: the first one chooses adaptive schedules, the others replay them
   bool records = false;  // some population keeps an MHR histogram or its energies
   bool family = false;   // some population keeps family statistics
+  std::string lattice_dir;  // pa_set_lattice_dump: per-temperature population text of the first run
+  int lattice_prec = 11;
+  bool lattice_failed = false;
   std::vector<std::vector<double>> fam;  // per set: rows of (families, rho_t, S_f)
   std::vector<std::vector<double>> mhr;                    // per set: rows of (beta, E/N, C/N, betaF/N)
   std::vector<std::vector<std::vector<int32_t>>> energies;  // per set, per temperature: energies
@@ -337,12 +397,31 @@ struct pa_handle {
     return e;
   }
 
+  // The population of population k after temperature i to the lattice files
+  // (only when it did advance to i).
+  cudaError_t dump_lattice(int k, int i, double beta) {
+    PopDev st;
+    cudaError_t e = cudaMemcpy(&st, d_pops + k, sizeof(PopDev), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || st.error || st.step - 1 != i) return e;
+    const int units = st.coding == PA_CODING_MSC ? (st.R_cur + kMsb - 1) / kMsb * kMsb : st.R_cur;
+    std::vector<uint8_t> sp(population_bytes(st.coding, st.L, st.R_cur));
+    std::vector<uint8_t> act(st.coding == PA_CODING_MSC ? (size_t)units : 0);
+    e = cudaMemcpy(sp.data(), st.spins[st.parity], sp.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && !act.empty())
+      e = cudaMemcpy(act.data(), st.active[st.parity], act.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess &&
+        write_lattice(lattice_dir, i, beta, lattice_prec, st.coding, st.L, st.R_cur, sp.data(), act.data(), units))
+      lattice_failed = true;
+    return e;
+  }
+
   // Run r, on the stream: graph replays or host-stepped launches.  Recorded
   // energies are read back whenever the device ring may be about to wrap.
   cudaError_t run_once(int r) {
     cudaError_t e;
     drained.assign(npop, -1);
-    if (graph) {
+    const bool lattices = !lattice_dir.empty() && runs_done == 0 && r == 0;  // the first run, as the reference
+    if (graph && !lattices) {
       e = cudaGraphLaunch(exec, stream);
       while (adaptive && e == cudaSuccess) {
         bool done = false;
@@ -364,6 +443,7 @@ struct pa_handle {
         if (i >= pops[k].cap) continue;
         double row[kRowCols];
         e = cudaMemcpy(row, pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && lattices) e = dump_lattice(k, i, row[0]);
       }
       if (e == cudaSuccess) e = drain(r);
       if (adaptive && e == cudaSuccess) {
@@ -814,8 +894,13 @@ int pa_run(pa_handle* H) {
       e = H->set_adaptive(H->runs_done == 0);
       if (e != cudaSuccess) return H->cuda_fail(e, "adaptive set-up");
     }
+    H->lattice_failed = false;
     e = H->run_once(r);
     if (e != cudaSuccess) return H->cuda_fail(e, H->graph ? "graph launch" : "plain step");
+    if (H->lattice_failed) {
+      H->err = "cannot append to the lattice files in " + H->lattice_dir;
+      return PA_ERR_ARG;
+    }
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(back.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost, H->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
@@ -956,6 +1041,17 @@ int pa_get_mhr_rows(const pa_handle* H, int set, double* rows, int max_rows, int
   const int n = (int)(src.size() / 4), m = std::min(n, max_rows);
   if (m > 0) std::memcpy(rows, src.data(), sizeof(double) * 4 * (size_t)m);
   if (nrows) *nrows = n;
+  return PA_OK;
+}
+
+int pa_set_lattice_dump(pa_handle* H, const char* dir, int precision) {
+  if (!H) return PA_ERR_ARG;
+  if (dir && H->npop != 1) {
+    H->err = "lattice dumps need a handle with one population";
+    return PA_ERR_ARG;
+  }
+  H->lattice_dir = dir ? dir : "";
+  H->lattice_prec = precision > 0 ? precision : 11;
   return PA_OK;
 }
 

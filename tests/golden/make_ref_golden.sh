@@ -29,4 +29,8 @@ for p in SSC MSC; do
   $B/PAising${p}_L64_curand -s 100 -o $T/d_$p > "$OUT/logs/cur_${p}_L64.log"
   cp $T/d_$p/PA_results_run_0.dat "$OUT/curand_${p}_L64_R20000_t100_d0.005_s100.dat"
 done
+# LatticePopStore build (SSC only): population text of every temperature of run 0
+$B/PAisingSSC_L16_inj_lattice -R 20 -t 5 -s 100 -d 0.25 -o $T/h_SSC > "$OUT/logs/inj_SSC_L16_lattice.log"
+mkdir -p "$OUT/inj_SSC_L16_R20_t5_d0.25_s100_lattice"
+cp $T/h_SSC/*.dat "$OUT/inj_SSC_L16_R20_t5_d0.25_s100_lattice/"
 rm -rf "$T"

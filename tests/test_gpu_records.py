@@ -70,3 +70,42 @@ def test_records_native_mhr_vs_exact(cuda, oracle):
     exact = np.array([-oracle.kaufman(16, b)[0] / 256 for b in m[:, 0]])
     assert np.max(np.abs(m[:, 3] - exact)) < 3e-4
     assert np.max(np.abs(rows[:, 6] - exact)) < 3e-4
+
+
+def test_lattice_dump_reference_bytes(cuda, tmp_path):
+    """The LatticePopStore build's per-temperature population text, byte for
+    byte, through the command-line driver's -S switch."""
+    import subprocess
+    from conftest import ROOT
+    exe = os.path.join(ROOT, "paising_gb300", "_lib", "paising")
+    r = subprocess.run([exe, "-R", "20", "-t", "5", "-s", "100", "-d", "0.25", "-L", "16", "-c", "ssc", "-m",
+                        "reference", "-w", "fp64", "-S", "-o", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    d = os.path.join(GOLDEN, "ref", "inj_SSC_L16_R20_t5_d0.25_s100_lattice")
+    for i in range(1, 5):
+        assert open(tmp_path / f"PA_lattice_{i}.dat").read() == open(os.path.join(d, f"PA_lattice_{i}.dat")).read()
+
+
+def test_lattice_dump_msc_matches_population(cuda, tmp_path):
+    """MSC lattice dumps (an extension): the last temperature's text lists the
+    final population's active replicas, group-major."""
+    L, R = 16, 40
+    with pa.Engine(L=L, R=R, sweeps=3, dbeta=0.25, seed=5, coding="msc") as e:
+        e.set_lattice_dump(str(tmp_path))
+        e.run()
+        pop = e.population()
+        n = e.num_rows()
+    text = open(tmp_path / f"PA_lattice_{n - 1}.dat").read().strip().split("\n")
+    reps = [l for l in text[1:] if l.startswith("P=")]
+    assert len(reps) == int(text[0].split("R=")[1].rstrip(";"))
+    # replica 0 of the text = group 0, bit 0: rebuild its lattice rows from the words
+    h, W = L * L // 2, L // 2
+    s = np.where((pop[0] >> 0) & 1, 1, -1)
+    rows = []
+    for y in range(L):
+        row = []
+        for i in range(W):
+            a, b = s[y * W + i], s[h + y * W + i]
+            row += [a, b] if y % 2 == 0 else [b, a]
+        rows.append("{" + ",".join(str(v) for v in row) + "}")
+    assert reps[0] == "P={" + ",".join(rows) + "};"
