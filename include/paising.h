@@ -125,6 +125,26 @@ PA_API int pa_create_batch(const pa_config* cfgs, int n, pa_handle** out);
  * PAisingMSC.cu:640-814). */
 PA_API int pa_run(pa_handle* h);
 
+/* A run stepped from the host, for hosts that interleave their own work or
+ * checkpoint long anneals: pa_run_begin sets up the run and its initial
+ * population (temperature 0), pa_run_steps advances up to max_steps
+ * temperatures (*done = 1 once every population has finished its schedule),
+ * pa_run_end collects the rows like pa_run.  The same launches as the plain
+ * mode; handles with one run (runs = 1, or a native batch).  No counterpart
+ * in the reference, whose main() loop runs to the end. */
+PA_API int pa_run_begin(pa_handle* h);
+PA_API int pa_run_steps(pa_handle* h, int max_steps, int* done);
+PA_API int pa_run_end(pa_handle* h);
+
+/* Between the steps of a stepped run: the complete state of every
+ * population (spins, energies, schedule, rows so far, stream positions,
+ * MHR histogram, ancestors) to a binary file, and back into a handle created
+ * with the same configurations, which then continues with pa_run_steps and
+ * pa_run_end exactly as the original would have.  Runs that store their
+ * energies are not checkpointed. */
+PA_API int pa_checkpoint(pa_handle* h, const char* path);
+PA_API int pa_restore(pa_handle* h, const char* path);
+
 /* Autotuner of the MSC one-CTA sweep: for every lattice size of the handle,
  * times one sweep launch of its populations (freshly initialised, at the
  * first temperature) with 1, 2, 4 and 8 groups stacked per work unit where

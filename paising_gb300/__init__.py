@@ -74,6 +74,11 @@ _SIGS = {
     "pa_get_energies": ([_vp, _i, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_family_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_set_lattice_dump": ([_vp, ctypes.c_char_p, _i], _i),
+    "pa_run_begin": ([_vp], _i),
+    "pa_run_steps": ([_vp, _i, ctypes.POINTER(_i)], _i),
+    "pa_run_end": ([_vp], _i),
+    "pa_checkpoint": ([_vp, ctypes.c_char_p], _i),
+    "pa_restore": ([_vp, ctypes.c_char_p], _i),
     "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
@@ -195,6 +200,28 @@ class Engine:
         out = np.zeros((n.value, 4))
         _check(lib().pa_get_mhr_rows(self._h, set_index, out.ctypes.data, n.value, ctypes.byref(n)), self._h)
         return out
+
+    def run_begin(self) -> None:
+        """Start a host-stepped run (initial population, temperature 0)."""
+        _check(lib().pa_run_begin(self._h), self._h)
+
+    def run_steps(self, n: int) -> bool:
+        """Advance up to n temperatures; True once the schedule is complete."""
+        d = ctypes.c_int()
+        _check(lib().pa_run_steps(self._h, int(n), ctypes.byref(d)), self._h)
+        return bool(d.value)
+
+    def run_end(self) -> None:
+        """Collect the rows of a stepped run (as run())."""
+        _check(lib().pa_run_end(self._h), self._h)
+
+    def checkpoint(self, path: str) -> None:
+        """Complete state of a stepped run to a file (between steps)."""
+        _check(lib().pa_checkpoint(self._h, path.encode()), self._h)
+
+    def restore(self, path: str) -> None:
+        """Continue a checkpointed run in this handle (same configuration)."""
+        _check(lib().pa_restore(self._h, path.encode()), self._h)
 
     def set_lattice_dump(self, directory: str | None, precision: int = 11) -> None:
         """Per-temperature population text files of the first run

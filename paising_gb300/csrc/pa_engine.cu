@@ -231,6 +231,8 @@ struct pa_handle {
   std::string lattice_dir;  // pa_set_lattice_dump: per-temperature population text of the first run
   int lattice_prec = 11;
   bool lattice_failed = false;
+  int step_run = -1;  // stepped run in progress (pa_run_begin .. pa_run_end): its index, else -1
+  int step_i = 0;     // temperatures done in it
   std::vector<std::vector<double>> fam;  // per set: rows of (families, rho_t, S_f)
   std::vector<std::vector<double>> mhr;                    // per set: rows of (beta, E/N, C/N, betaF/N)
   std::vector<std::vector<std::vector<int32_t>>> energies;  // per set, per temperature: energies
@@ -432,27 +434,104 @@ struct pa_handle {
       }
       return e == cudaSuccess ? drain(r) : e;
     }
-    e = enqueue_init();
+    e = plain_begin(r);
+    bool done = false;
+    for (int i = 1; e == cudaSuccess && !done; ++i) e = plain_step(r, i, lattices, &done);
+    return e;
+  }
+
+  // Host-stepped pieces of run r (plain mode and the stepping entry points):
+  // the set-up and initial population ...
+  cudaError_t plain_begin(int r) {
+    drained.assign(npop, -1);
+    cudaError_t e = enqueue_init();
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e == cudaSuccess) e = drain(r);
-    for (int i = 1; i <= max_steps && e == cudaSuccess; ++i) {
-      e = enqueue_step();
-      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-      // the host reads every step's result, like the reference's host loop
-      for (int k = 0; k < npop && e == cudaSuccess; ++k) {
-        if (i >= pops[k].cap) continue;
-        double row[kRowCols];
-        e = cudaMemcpy(row, pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
-        if (e == cudaSuccess && lattices) e = dump_lattice(k, i, row[0]);
+    return e;
+  }
+
+  // ... and temperature i; *done once every population is through its schedule
+  cudaError_t plain_step(int r, int i, bool lattices, bool* done) {
+    cudaError_t e = enqueue_step();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    // the host reads every step's result, like the reference's host loop
+    for (int k = 0; k < npop && e == cudaSuccess; ++k) {
+      if (i >= pops[k].cap) continue;
+      double row[kRowCols];
+      e = cudaMemcpy(row, pops[k].h.rows + (size_t)i * kRowCols, sizeof(row), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && lattices) e = dump_lattice(k, i, row[0]);
+    }
+    if (e == cudaSuccess) e = drain(r);
+    *done = i >= max_steps;
+    if (adaptive && e == cudaSuccess) e = all_done(done);
+    return e;
+  }
+
+  // After run r: its rows, statistics and status into result sets r*npop + k.
+  int collect_run(int r) {
+    int status = PA_OK;
+    std::vector<PopDev> back(npop);
+    cudaError_t e = cudaMemcpyAsync(back.data(), d_pops, sizeof(PopDev) * npop, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    for (int k = 0; k < npop && e == cudaSuccess; ++k) {
+      // rows of the schedule the run followed (adaptive: as long as the device made it)
+      const PopHost& P = pops[k];
+      const int nrows = std::min(back[k].nsteps + 1, P.cap);
+      std::vector<double>& dst = rows[(size_t)r * npop + P.user_index];
+      dst.assign((size_t)nrows * kRowCols, 0.0);
+      e = cudaMemcpyAsync(dst.data(), P.h.rows, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "run");
+    for (int k = 0; k < npop; ++k) {
+      if (back[k].error) {
+        switch (back[k].error) {
+          case kErrExtinct:
+            status = PA_ERR_EXTINCT;
+            err = "resampling produced an empty population";
+            break;
+          case kErrTooManySteps:
+            status = PA_ERR_TOO_MANY_STEPS;
+            err = "number of temperature steps exceeds nBmax=10000 (raise R or lower min_overlap)";
+            break;
+          default:
+            status = PA_ERR_CAPACITY;
+            err = "population exceeded its buffer capacity (raise pa_config.capacity)";
+        }
       }
-      if (e == cudaSuccess) e = drain(r);
-      if (adaptive && e == cudaSuccess) {
-        bool done = false;
-        e = all_done(&done);
-        if (done) break;
+      const PopHost& P = pops[k];
+      const std::vector<double>& rw = rows[(size_t)r * npop + P.user_index];
+      for (size_t i = 1; i < rw.size() / kRowCols; ++i)
+        attempts += (double)P.cfg.sweeps * (double)P.h.N * rw[i * kRowCols + 8];
+      if (P.h.mhr_hist && !back[k].error) {
+        std::vector<unsigned long long> hist((size_t)P.h.N + 1);
+        e = cudaMemcpy(hist.data(), P.h.mhr_hist, sizeof(unsigned long long) * hist.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "MHR histogram");
+        mhr[(size_t)r * npop + P.user_index] = mhr_analysis(P.h.N, rw, hist);
+      }
+      if (P.h.family && !back[k].error) {
+        std::vector<double>& f = fam[(size_t)r * npop + P.user_index];
+        f.assign(rw.size() / kRowCols * 3, 0.0);
+        e = cudaMemcpy(f.data(), P.h.fam_rows, sizeof(double) * f.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "family statistics");
       }
     }
-    return e;
+    if (status == PA_OK) {
+      sets_done = (r + 1) * npop;
+      ++runs_done;
+    }
+    return status;
+  }
+
+  // Result containers for a new pa_run (or stepped run).
+  void reset_results() {
+    rows.assign((size_t)npop * seq_runs, {});
+    mhr.assign((size_t)npop * seq_runs, {});
+    energies.assign((size_t)npop * seq_runs, {});
+    fam.assign((size_t)npop * seq_runs, {});
+    sets_done = 0;
+    attempts = 0;
+    ran = true;
   }
 
   // Persistent sweep grid for the populations' current geometry and, in
@@ -878,17 +957,14 @@ int pa_num_sets(const pa_handle* H, int* n) {
 
 int pa_run(pa_handle* H) {
   if (!H) return PA_ERR_ARG;
-  H->rows.assign((size_t)H->npop * H->seq_runs, {});
-  H->mhr.assign((size_t)H->npop * H->seq_runs, {});
-  H->energies.assign((size_t)H->npop * H->seq_runs, {});
-  H->fam.assign((size_t)H->npop * H->seq_runs, {});
-  H->sets_done = 0;
-  H->attempts = 0;
-  H->ran = true;
+  if (H->step_run >= 0) {
+    H->err = "a stepped run is in progress (pa_run_end first)";
+    return PA_ERR_STATE;
+  }
+  H->reset_results();
   cudaError_t e = cudaEventRecord(H->ev0, H->stream);
   if (e != cudaSuccess) return H->cuda_fail(e, "event");
   int status = PA_OK;
-  std::vector<PopDev> back(H->npop);
   for (int r = 0; r < H->seq_runs && status == PA_OK; ++r) {
     if (H->adaptive) {
       e = H->set_adaptive(H->runs_done == 0);
@@ -901,56 +977,8 @@ int pa_run(pa_handle* H) {
       H->err = "cannot append to the lattice files in " + H->lattice_dir;
       return PA_ERR_ARG;
     }
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(back.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost, H->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
-      // rows of the schedule the run followed (adaptive: as long as the device made it)
-      const PopHost& P = H->pops[k];
-      const int nrows = std::min(back[k].nsteps + 1, P.cap);
-      std::vector<double>& dst = H->rows[(size_t)r * H->npop + P.user_index];
-      dst.assign((size_t)nrows * kRowCols, 0.0);
-      e = cudaMemcpyAsync(dst.data(), P.h.rows, dst.size() * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
-    if (e != cudaSuccess) return H->cuda_fail(e, "run");
-    for (int k = 0; k < H->npop; ++k) {
-      if (back[k].error) {
-        switch (back[k].error) {
-          case kErrExtinct:
-            status = PA_ERR_EXTINCT;
-            H->err = "resampling produced an empty population";
-            break;
-          case kErrTooManySteps:
-            status = PA_ERR_TOO_MANY_STEPS;
-            H->err = "number of temperature steps exceeds nBmax=10000 (raise R or lower min_overlap)";
-            break;
-          default:
-            status = PA_ERR_CAPACITY;
-            H->err = "population exceeded its buffer capacity (raise pa_config.capacity)";
-        }
-      }
-      const PopHost& P = H->pops[k];
-      const std::vector<double>& rw = H->rows[(size_t)r * H->npop + P.user_index];
-      for (size_t i = 1; i < rw.size() / kRowCols; ++i)
-        H->attempts += (double)P.cfg.sweeps * (double)P.h.N * rw[i * kRowCols + 8];
-      if (P.h.mhr_hist && !back[k].error) {
-        std::vector<unsigned long long> hist((size_t)P.h.N + 1);
-        e = cudaMemcpy(hist.data(), P.h.mhr_hist, sizeof(unsigned long long) * hist.size(), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return H->cuda_fail(e, "MHR histogram");
-        H->mhr[(size_t)r * H->npop + P.user_index] = mhr_analysis(P.h.N, rw, hist);
-      }
-      if (P.h.family && !back[k].error) {
-        std::vector<double>& f = H->fam[(size_t)r * H->npop + P.user_index];
-        f.assign(rw.size() / kRowCols * 3, 0.0);
-        e = cudaMemcpy(f.data(), P.h.fam_rows, sizeof(double) * f.size(), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return H->cuda_fail(e, "family statistics");
-      }
-    }
-    if (status == PA_OK) {
-      H->sets_done = (r + 1) * H->npop;
-      ++H->runs_done;
-    }
+    status = H->collect_run(r);
+    if (status == PA_ERR_CUDA) return status;
   }
   e = cudaEventRecord(H->ev1, H->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(H->ev1);
@@ -959,6 +987,198 @@ int pa_run(pa_handle* H) {
   if (e != cudaSuccess) return H->cuda_fail(e, "timing");
   H->ms = ms;
   return status;
+}
+
+int pa_run_begin(pa_handle* H) {
+  if (!H) return PA_ERR_ARG;
+  if (H->step_run >= 0 || H->seq_runs != 1) {
+    H->err = H->seq_runs != 1 ? "stepped runs need one run per handle (runs = 1 or a native batch)"
+                              : "a stepped run is already in progress";
+    return PA_ERR_STATE;
+  }
+  H->reset_results();
+  cudaError_t e = H->adaptive ? H->set_adaptive(H->runs_done == 0) : cudaSuccess;
+  if (e == cudaSuccess) e = H->plain_begin(0);
+  if (e != cudaSuccess) return H->cuda_fail(e, "run begin");
+  H->step_run = 0;
+  H->step_i = 0;
+  return PA_OK;
+}
+
+int pa_run_steps(pa_handle* H, int max_steps, int* done) {
+  if (!H || max_steps < 0) return PA_ERR_ARG;
+  if (H->step_run < 0) {
+    H->err = "no stepped run in progress (pa_run_begin first)";
+    return PA_ERR_STATE;
+  }
+  bool fin = false;
+  cudaError_t e = H->all_done(&fin);
+  const bool lattices = !H->lattice_dir.empty() && H->runs_done == 0;
+  for (int k = 0; k < max_steps && e == cudaSuccess && !fin; ++k) e = H->plain_step(0, ++H->step_i, lattices, &fin);
+  if (e != cudaSuccess) return H->cuda_fail(e, "run steps");
+  if (H->lattice_failed) {
+    H->err = "cannot append to the lattice files in " + H->lattice_dir;
+    return PA_ERR_ARG;
+  }
+  if (done) *done = fin ? 1 : 0;
+  return PA_OK;
+}
+
+int pa_run_end(pa_handle* H) {
+  if (!H) return PA_ERR_ARG;
+  if (H->step_run < 0) return PA_ERR_STATE;
+  const int status = H->collect_run(0);
+  H->step_run = -1;
+  return status;
+}
+
+// ---------------------------------------------------------------- checkpoint
+// File: "PAGB300C", version, population count, coding, temperatures done,
+// runs completed; per population (device order) its shape, its PopDev and
+// the contents of the device buffers that carry state between temperatures.
+namespace {
+constexpr char kCkptMagic[8] = {'P', 'A', 'G', 'B', '3', '0', '0', 'C'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptPop {
+  int L, R, Rcap, rgcap, cap, gpt, coding, rec, family;
+};
+
+// (device pointer, bytes) of every stateful buffer of population st (the
+// current half of the double buffers)
+std::vector<std::pair<void*, size_t>> state_buffers(const PopDev& st, const PopHost& P) {
+  const size_t units = st.coding == PA_CODING_MSC ? (size_t)st.rgcap * kMsb : (size_t)st.Rcap;
+  std::vector<std::pair<void*, size_t>> b;
+  b.push_back({st.spins[st.parity], population_bytes(st.coding, st.L, st.R_cur)});
+  if (st.coding == PA_CODING_MSC) b.push_back({st.active[st.parity], units});
+  b.push_back({st.E, units * sizeof(int32_t)});
+  b.push_back({st.M, units * sizeof(int32_t)});
+  b.push_back({st.rows, (size_t)P.cap * kRowCols * sizeof(double)});
+  b.push_back({st.betas, (size_t)P.cap * sizeof(double)});
+  b.push_back({st.thr, (size_t)P.cap * kThrPerStep * sizeof(uint32_t)});
+  if (st.mhr_hist) b.push_back({st.mhr_hist, ((size_t)st.N + 1) * sizeof(unsigned long long)});
+  if (st.family) {
+    b.push_back({st.anc[st.parity], units * sizeof(int32_t)});
+    b.push_back({st.fam_rows, (size_t)P.cap * 3 * sizeof(double)});
+  }
+  return b;
+}
+}  // namespace
+
+int pa_checkpoint(pa_handle* H, const char* path) {
+  if (!H || !path) return PA_ERR_ARG;
+  if (H->step_run < 0) {
+    H->err = "checkpoints are taken between the steps of a stepped run";
+    return PA_ERR_STATE;
+  }
+  for (const auto& P : H->pops)
+    if (P.h.rec & kRecEnergies) {
+      H->err = "a run that stores its energies cannot be checkpointed";
+      return PA_ERR_STATE;
+    }
+  std::vector<PopDev> st(H->npop);
+  cudaError_t e = cudaStreamSynchronize(H->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(st.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return H->cuda_fail(e, "checkpoint");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    H->err = std::string("cannot write ") + path;
+    return PA_ERR_ARG;
+  }
+  bool ok = std::fwrite(kCkptMagic, 1, 8, f) == 8;
+  const int32_t head[5] = {(int32_t)kCkptVersion, H->npop, H->coding, H->step_i, H->runs_done};
+  ok = ok && std::fwrite(head, sizeof(head), 1, f) == 1;
+  std::vector<uint8_t> buf;
+  for (int k = 0; k < H->npop && ok; ++k) {
+    const PopHost& P = H->pops[k];
+    const CkptPop cp{P.h.L, P.cfg.R, P.h.Rcap, P.h.rgcap, P.cap, P.h.gpt, P.h.coding, P.h.rec, P.h.family};
+    ok = std::fwrite(&cp, sizeof(cp), 1, f) == 1 && std::fwrite(&st[k], sizeof(PopDev), 1, f) == 1;
+    for (const auto& b : state_buffers(st[k], P)) {
+      if (!ok) break;
+      buf.resize(b.second);
+      e = cudaMemcpy(buf.data(), b.first, b.second, cudaMemcpyDeviceToHost);
+      const uint64_t n = b.second;
+      ok = e == cudaSuccess && std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(buf.data(), 1, n, f) == n;
+    }
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (e != cudaSuccess) return H->cuda_fail(e, "checkpoint");
+  if (!ok) {
+    H->err = std::string("cannot write ") + path;
+    return PA_ERR_ARG;
+  }
+  return PA_OK;
+}
+
+int pa_restore(pa_handle* H, const char* path) {
+  if (!H || !path) return PA_ERR_ARG;
+  if (H->step_run >= 0) {
+    H->err = "a stepped run is in progress";
+    return PA_ERR_STATE;
+  }
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    H->err = std::string("cannot read ") + path;
+    return PA_ERR_ARG;
+  }
+  auto bad = [&](const char* m) {
+    std::fclose(f);
+    H->err = std::string(path) + ": " + m;
+    return PA_ERR_ARG;
+  };
+  char magic[8];
+  int32_t head[5];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kCkptMagic, 8) != 0) return bad("not a checkpoint");
+  if (std::fread(head, sizeof(head), 1, f) != 1 || head[0] != (int32_t)kCkptVersion) return bad("unknown version");
+  if (head[1] != H->npop || head[2] != H->coding) return bad("written by a handle of another configuration");
+  std::vector<PopDev> cur(H->npop), saved(H->npop);
+  cudaError_t e = cudaMemcpy(cur.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    std::fclose(f);
+    return H->cuda_fail(e, "restore");
+  }
+  std::vector<uint8_t> buf;
+  for (int k = 0; k < H->npop; ++k) {
+    const PopHost& P = H->pops[k];
+    CkptPop cp;
+    if (std::fread(&cp, sizeof(cp), 1, f) != 1 || std::fread(&saved[k], sizeof(PopDev), 1, f) != 1)
+      return bad("truncated");
+    if (cp.L != P.h.L || cp.R != P.cfg.R || cp.Rcap != P.h.Rcap || cp.rgcap != P.h.rgcap || cp.cap != P.cap ||
+        cp.gpt != P.h.gpt || cp.coding != P.h.coding || cp.rec != P.h.rec || cp.family != P.h.family)
+      return bad("written by a handle of another configuration");
+    // the saved scalars with this handle's buffers
+    PopDev m = saved[k];
+    std::memcpy(m.spins, cur[k].spins, sizeof(m.spins));
+    std::memcpy(m.active, cur[k].active, sizeof(m.active));
+    std::memcpy(m.anc, cur[k].anc, sizeof(m.anc));
+    m.E = cur[k].E; m.M = cur[k].M; m.roff = cur[k].roff; m.offs = cur[k].offs; m.src = cur[k].src;
+    m.blk_tot = cur[k].blk_tot; m.blk_off = cur[k].blk_off; m.qpart_d = cur[k].qpart_d; m.qpart_f = cur[k].qpart_f;
+    m.rows = cur[k].rows; m.betas = cur[k].betas; m.thr = cur[k].thr; m.init_src = cur[k].init_src;
+    m.hist = cur[k].hist; m.mhr_hist = cur[k].mhr_hist; m.elog = cur[k].elog; m.alog = cur[k].alog;
+    m.nlog = cur[k].nlog; m.fam_cnt = cur[k].fam_cnt; m.fam_rows = cur[k].fam_rows; m.fam_part = cur[k].fam_part;
+    m.ticket = 0;
+    for (const auto& b : state_buffers(m, P)) {
+      uint64_t n = 0;
+      if (std::fread(&n, sizeof(n), 1, f) != 1 || n != b.second) return bad("truncated or mismatched buffer");
+      buf.resize(n);
+      if (std::fread(buf.data(), 1, n, f) != n) return bad("truncated");
+      e = cudaMemcpy(b.first, buf.data(), n, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        std::fclose(f);
+        return H->cuda_fail(e, "restore");
+      }
+    }
+    cur[k] = m;
+  }
+  std::fclose(f);
+  e = cudaMemcpy(H->d_pops, cur.data(), sizeof(PopDev) * H->npop, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return H->cuda_fail(e, "restore");
+  H->reset_results();
+  H->runs_done = head[4];
+  H->drained.assign(H->npop, -1);
+  H->step_run = 0;
+  H->step_i = head[3];
+  return PA_OK;
 }
 
 int pa_autotune(pa_handle* H, int* tiles, int n) {
