@@ -342,51 +342,117 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 // (PAisingMSC.cu:413-414).  Here every new word gathers its 32 bits:
 // bit k of new group j comes from old replica src[k*rg_new + j].
 //
-// A block takes work items (new group j, chunk of kResChunk sites): the 32
-// source rows and bit positions of group j are resolved once into shared
-// memory, after which every site's 32 loads are independent of each other
-// (many in flight per thread) and coalesced across the warp.  Items run in
-// site-chunk-major order over consecutive groups, whose sources are
-// neighbouring replicas, so the old rows being read stay in L2.
-constexpr int kResChunk = 1024;
+// Work unit of one warp: 32 consecutive new groups (lane g builds group
+// j0 + g) x a strip of 32 sites.  Lane g resolves the sources of its 32 bits
+// into row pointers and rotations held in registers, four bits at a time,
+// and gathers its 32 output words with loads at immediate offsets.  The 32
+// lanes' sources are 32 consecutive new replicas, i.e. neighbouring old
+// replicas in one or two old groups, so a load instruction touches one or two
+// old words: the gather costs about one warp load per output word, and no L2
+// traffic beyond the old rows themselves.  Units of all populations of the
+// batch come from one queue (msc_resample_plan_kernel) and are taken by
+// persistent warps, so uneven populations finish together.
 constexpr int kResampleThreads = 256;
+constexpr int kSub = 8;  // sites gathered per pass over the 32 source bits
 
-__global__ void __launch_bounds__(kResampleThreads) msc_resample_kernel(PopDev* pops) {
-  __shared__ uint32_t s_off[kMsb], s_rot[kMsb];  // source word offset; rotation moving its bit to bit k
-  __shared__ uint32_t s_valid;
-  PopDev* st = pops + blockIdx.y;
-  if (!pop_stepping(st)) return;
-  const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb;
-  const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1];
-  uint32_t* neu = (uint32_t*)st->spins[st->parity];
-  uint8_t* act = st->active[st->parity];
-  const uint32_t* src = st->src;
-  const int tid = threadIdx.x, nchunk = (N + kResChunk - 1) / kResChunk;
-  const int items = rgn * nchunk;
-  for (int it = blockIdx.x; it < items; it += gridDim.x) {
-    const int c = it / rgn, j = it - c * rgn;  // chunk-major: consecutive items, consecutive groups
-    __syncthreads();                           // the previous item's sources are no longer read
-    if (tid < kMsb) {
-      const int s = tid * rgn + j;
-      const bool v = s < Rn;
-      const uint32_t lin = v ? src[s] : 0u;  // an invalid bit reads old word 0 and is masked off
-      s_off[tid] = (lin >> 5) * (uint32_t)N;
-      s_rot[tid] = ((uint32_t)tid - (lin & 31u)) & 31u;
-      const uint32_t m = __ballot_sync(kFull, v);
-      if (tid == 0) s_valid = m;
-      if (c == 0) act[j * kMsb + tid] = v ? 1 : 0;
+// Sites per warp unit: 32, or 8 when a population would otherwise have too
+// few units to occupy the GPU (small lattices).
+__device__ __forceinline__ int res_strip(int N, int rgn) {
+  const int tiles = (rgn + 31) / 32;
+  return (long long)tiles * (N / 32) >= 8192 ? 32 : kSub;
+}
+
+__global__ void __launch_bounds__(1024) msc_resample_plan_kernel(BatchDev* b) {
+  __shared__ uint32_t s_u[33];
+  const int p = threadIdx.x, np = b->npop;
+  uint32_t units = 0;
+  if (p < np) {
+    const PopDev* st = b->pops + p;
+    if (st->coding == kMSC && pop_stepping(st)) {
+      const int rgn = (st->R_cur + kMsb - 1) / kMsb, S = res_strip(st->N, rgn);
+      units = (uint32_t)(((rgn + 31) / 32) * ((st->N + S - 1) / S));
     }
-    __syncthreads();
-    const uint32_t vmask = s_valid;
-    const int t1 = min(N, (c + 1) * kResChunk);
-    for (int t = c * kResChunk + tid; t < t1; t += blockDim.x) {
-      uint32_t w = 0;
-#pragma unroll 16
-      for (int k = 0; k < kMsb; ++k) {
-        const uint32_t v = __ldg(old + s_off[k] + t);
-        w |= __funnelshift_l(v, v, s_rot[k]) & (1u << k);  // source bit rotated into bit k
+  }
+  uint32_t total;
+  const uint32_t ex = block_exscan(units, s_u, &total);
+  if (p < np) b->res_prefix[p] = (int)ex;
+  if (p == 0) {
+    b->res_prefix[np] = (int)total;
+    b->res_next = 0;
+  }
+}
+
+template <bool kFull>
+__device__ __forceinline__ void gather_sub(const uint32_t* const (&p)[4], const uint32_t (&rot)[4],
+                                           const uint32_t (&msk)[4], int nv, uint32_t (&w)[kSub]) {
+#pragma unroll
+  for (int t = 0; t < kSub; ++t) {
+    const int tc = kFull ? t : min(t, nv - 1);  // partial: repeat the last site (not stored)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t v = __ldg(p[q] + tc);
+      w[t] |= __funnelshift_l(v, v, rot[q]) & msk[q];  // source bit rotated into bit k
+    }
+  }
+}
+
+constexpr int kResampleBlocksPerSM = 3;  // 80 registers, no spills
+
+__global__ void __launch_bounds__(kResampleThreads, kResampleBlocksPerSM) msc_resample_kernel(BatchDev* b) {
+  const int lane = threadIdx.x & 31;
+  const int total = b->res_prefix[b->npop];
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = (int)atomicAdd(&b->res_next, 1u);
+    u = __shfl_sync(kFull, u, 0);
+    if (u >= total) break;
+    int lo = 0, hi = b->npop;  // population of unit u
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (b->res_prefix[mid] <= u) lo = mid;
+      else hi = mid;
+    }
+    const PopDev* st = b->pops + lo;
+    const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb, S = res_strip(N, rgn);
+    const int nstrip = (N + S - 1) / S;
+    const int loc = u - b->res_prefix[lo], tile = loc / nstrip, strip = loc - tile * nstrip;
+    const int j = tile * 32 + lane, t0 = strip * S, nt = min(S, N - t0);
+    const bool jv = j < rgn;
+    const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1];
+    const uint32_t* src = st->src;
+    if (strip == 0 && jv) {
+      uint8_t* act = st->active[st->parity];
+#pragma unroll 4
+      for (int k = 0; k < kMsb; ++k) act[j * kMsb + k] = (k * rgn + j) < Rn ? 1 : 0;
+    }
+    uint32_t* dst = (uint32_t*)st->spins[st->parity] + (size_t)j * N + t0;
+#pragma unroll 1
+    for (int tc = 0; tc < nt; tc += kSub) {
+      const int nv = min(kSub, nt - tc);  // a multiple of 4: N and t0 are
+      uint32_t w[kSub];
+#pragma unroll
+      for (int t = 0; t < kSub; ++t) w[t] = 0u;
+#pragma unroll 1
+      for (int k0 = 0; k0 < kMsb; k0 += 4) {
+        const uint32_t* p[4];
+        uint32_t rot[4], msk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int k = k0 + q, s = k * rgn + j;
+          const bool v = jv && s < Rn;
+          const uint32_t lin = v ? src[s] : 0u;  // an invalid bit reads old word 0 and is masked off
+          p[q] = old + (size_t)(lin >> 5) * N + t0 + tc;
+          rot[q] = ((uint32_t)k - (lin & 31u)) & 31u;
+          msk[q] = v ? 1u << k : 0u;
+        }
+        if (nv == kSub) gather_sub<true>(p, rot, msk, nv, w);
+        else gather_sub<false>(p, rot, msk, nv, w);
       }
-      neu[(size_t)j * N + t] = w & vmask;
+      if (jv) {
+        uint4* d4 = reinterpret_cast<uint4*>(dst + tc);
+        d4[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        if (nv > 4) d4[1] = make_uint4(w[4], w[5], w[6], w[7]);
+      }
     }
   }
 }
@@ -476,12 +542,14 @@ cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_msc_resample(PopDev* pops, int npop, cudaStream_t s) {
+cudaError_t launch_msc_resample(BatchDev* b, cudaStream_t s) {
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int x = (nsm * 8 + npop - 1) / npop;
-  msc_resample_kernel<<<dim3(x < 16 ? 16 : x, npop), 256, 0, s>>>(pops);
+  msc_resample_plan_kernel<<<1, 1024, 0, s>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  msc_resample_kernel<<<nsm * kResampleBlocksPerSM, kResampleThreads, 0, s>>>(b);  // persistent warps
   return cudaGetLastError();
 }
 

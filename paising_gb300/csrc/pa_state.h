@@ -107,6 +107,9 @@ struct BatchDev {
   unsigned int work_next;
   PopDev* pops;
   int unit_prefix[kMaxPop + 1];
+  // the MSC resampling gather's work list: units of 32 new groups x 32 sites
+  unsigned int res_next;
+  int res_prefix[kMaxPop + 1];
 };
 
 // A population takes part in the current temperature step.
