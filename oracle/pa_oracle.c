@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls
  * this file; it is built into oracle/_build/libpaoracle.so and used by the
- * tests, by __graft_entry__.smoke() as the checker, and by bench.py's
- * cpu_baseline leg.
+ * tests, by __graft_entry__.smoke() to verify the engine's results, and by
+ * bench.py's cpu_baseline leg.
  *
  * It restates, stage by stage and in the reference's own draw order, the two
  * reference programs:

@@ -1,8 +1,8 @@
 """ctypes bindings of the oracle library oracle/_build/libpaoracle.so.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's cpu_baseline / reference legs.  The product
-package never imports this module.
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+verify the engine's results and by bench.py's cpu_baseline / reference legs.
+The product package never imports this module.
 
 Every function restates one stage of the reference (see pa_oracle.c for the
 file:line of each) on numpy arrays in the reference's own layouts.

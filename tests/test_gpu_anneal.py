@@ -79,7 +79,7 @@ def test_native_free_energy_vs_kaufman_L16(cuda, oracle, coding):
 @pytest.mark.slow
 @pytest.mark.parametrize("coding", ["msc", "ssc"])
 def test_native_free_energy_vs_kaufman_C2(cuda, oracle, coding):
-    """The spec bar at L=64, R=20000, 100 sweeps, dbeta=0.005:
+    """The accuracy target at L=64, R=20000, 100 sweeps, dbeta=0.005:
     |betaF/N - exact| <= 1e-4 at every beta, native stream, FP32 weights."""
     rows, _ = run(L=64, R=20000, sweeps=100, seed=2026, coding=coding)
     r = rows[0]
