@@ -169,8 +169,9 @@ def run_ours(a):
         eng.run()
     nsteps = eng.num_rows() - 1
     # one launch sequence serves all P populations: 5 kernels to initialise,
-    # 7 per temperature (q, copy numbers, scatter, resample, plan, sweep, finish)
-    launches_per_run = 5 + 7 * nsteps
+    # 8 per temperature (q, copy numbers, scatter, gather plan, gather, sweep
+    # plan, sweep, finish)
+    launches_per_run = 5 + 8 * nsteps
 
     def barrier():
         if dist:

@@ -313,7 +313,7 @@ struct pa_handle {
     if ((e = launch("copy_numbers", [&] { return launch_copy_numbers(d_pops, npop, rblocks, stream); })) != cudaSuccess)
       return e;
     if ((e = launch("scatter", [&] { return launch_scatter(d_pops, npop, rblocks, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_batch, d_pops, npop, coding, stream); });
+    e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_batch, coding, stream); });
     if (e != cudaSuccess) return e;
     if (family && (e = launch("family_resample", [&] { return launch_family_resample(d_pops, npop, rblocks, stream); })) !=
                       cudaSuccess)

@@ -581,8 +581,8 @@ cudaError_t launch_init(PopDev* pops, int npop, int coding, cudaStream_t s) {
   return coding == kMSC ? launch_msc_init(pops, npop, s) : launch_ssc_init(pops, npop, s);
 }
 
-cudaError_t launch_resample(BatchDev* b, PopDev* pops, int npop, int coding, cudaStream_t s) {
-  return coding == kMSC ? launch_msc_resample(b, s) : launch_ssc_resample(pops, npop, s);
+cudaError_t launch_resample(BatchDev* b, int coding, cudaStream_t s) {
+  return coding == kMSC ? launch_msc_resample(b, s) : launch_ssc_resample(b, s);
 }
 
 cudaError_t launch_q(PopDev* pops, int npop, int blocks, cudaStream_t s) {

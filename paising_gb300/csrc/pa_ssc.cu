@@ -306,17 +306,105 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 
 // -------------------------------------------------------------- resample
 // Gather form of resampleKer: new replica s copies old replica src[s].
-__global__ void ssc_resample_kernel(PopDev* pops) {
-  PopDev* st = pops + blockIdx.y;
-  if (!pop_stepping(st)) return;
-  const int N = st->N, Rn = st->R_cur;
-  const uint4* old = (const uint4*)st->spins[st->parity ^ 1];
-  uint4* neu = (uint4*)st->spins[st->parity];
-  const int nv = N >> 4;
-  for (int s = blockIdx.x; s < Rn; s += gridDim.x) {
-    const uint4* a = old + (size_t)st->src[s] * nv;
-    uint4* c = neu + (size_t)s * nv;
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) c[v] = a[v];
+//
+// Work unit: up to kSscUnitVecs 16-byte vectors of one population's new
+// buffer -- whole replicas (floor(kSscUnitVecs / nv) of them) when a replica
+// has at most kSscUnitVecs vectors, else one kSscUnitVecs part of a replica.
+// Units of all populations of the batch come from one queue
+// (ssc_resample_plan_kernel) and are taken by persistent CTAs, so a batch of
+// uneven populations keeps every SM copying until the last unit; each thread
+// issues all its loads of a unit before its stores.
+constexpr int kSscResThreads = 256;
+constexpr int kSscVecsPerThread = 8;
+constexpr int kSscUnitVecs = kSscResThreads * kSscVecsPerThread;  // 32 KB
+constexpr int kSscResBlocksPerSM = 4;  // 64 registers
+
+__host__ __device__ __forceinline__ long long ssc_units(int nv, int Rn) {
+  if (nv > kSscUnitVecs) return (long long)Rn * ((nv + kSscUnitVecs - 1) / kSscUnitVecs);
+  const int rpu = kSscUnitVecs / nv;
+  return (Rn + rpu - 1) / rpu;
+}
+
+__global__ void __launch_bounds__(1024) ssc_resample_plan_kernel(BatchDev* b) {
+  __shared__ uint32_t s_u[33];
+  const int p = threadIdx.x, np = b->npop;
+  uint32_t units = 0;
+  if (p < np) {
+    const PopDev* st = b->pops + p;
+    if (st->coding == kSSC && pop_stepping(st)) units = (uint32_t)ssc_units(st->N >> 4, st->R_cur);
+  }
+  uint32_t total;
+  const uint32_t ex = block_exscan(units, s_u, &total);
+  if (p < np) b->res_prefix[p] = (int)ex;
+  if (p == 0) {
+    b->res_prefix[np] = (int)total;
+    b->res_next = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kSscResThreads, kSscResBlocksPerSM) ssc_resample_kernel(BatchDev* b) {
+  __shared__ int s_u[2];  // this unit and the next one (taken ahead by thread 0)
+  const int tid = threadIdx.x, total = b->res_prefix[b->npop];
+  if (tid == 0) s_u[0] = (int)atomicAdd(&b->res_next, 1u);
+  __syncthreads();
+  for (int it = 0;; ++it) {
+    const int u = s_u[it & 1];
+    if (u >= total) break;  // block-uniform
+    if (tid == 0) s_u[(it + 1) & 1] = (int)atomicAdd(&b->res_next, 1u);
+    int lo = 0, hi = b->npop;  // population of unit u
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (b->res_prefix[mid] <= u) lo = mid;
+      else hi = mid;
+    }
+    const PopDev* st = b->pops + lo;
+    const int nv = st->N >> 4, Rn = st->R_cur, loc = u - b->res_prefix[lo];
+    const uint4* old = (const uint4*)st->spins[st->parity ^ 1];
+    uint4* neu = (uint4*)st->spins[st->parity];
+    const uint32_t* src = st->src;
+    // the unit as replicas [s0, s0 + ns) x vectors [j0, j0 + nj) of each
+    int s0, ns, j0, nj;
+    if (nv > kSscUnitVecs) {
+      const int upr = (nv + kSscUnitVecs - 1) / kSscUnitVecs, part = loc % upr;
+      s0 = loc / upr;
+      ns = 1;
+      j0 = part * kSscUnitVecs;
+      nj = min(kSscUnitVecs, nv - j0);
+    } else {
+      const int rpu = kSscUnitVecs / nv;
+      s0 = loc * rpu;
+      ns = min(rpu, Rn - s0);
+      j0 = 0;
+      nj = nv;
+    }
+    const int n = ns * nj;                     // vectors in the unit (<= kSscUnitVecs)
+    const uint32_t inv = 0xffffffffu / (uint32_t)nj + 1u;  // n / nj by __umulhi: n * nj < 2^32
+    // vector i of the unit is vector j0 + i % nj of new replica s0 + i / nj
+    auto at = [&](int i, int& s) {
+      const int q = ns == 1 ? 0 : (int)__umulhi((uint32_t)i, inv);
+      s = s0 + q;
+      return j0 + i - q * nj;
+    };
+    uint4 r[kSscVecsPerThread];
+#pragma unroll
+    for (int k = 0; k < kSscVecsPerThread; ++k) {
+      const int i = tid + k * kSscResThreads;
+      if (i < n) {
+        int s;
+        const int j = at(i, s);
+        r[k] = __ldg(old + (size_t)src[s] * nv + j);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kSscVecsPerThread; ++k) {
+      const int i = tid + k * kSscResThreads;
+      if (i < n) {
+        int s;
+        const int j = at(i, s);
+        neu[(size_t)s * nv + j] = r[k];
+      }
+    }
+    __syncthreads();  // s_u[(it + 1) & 1] is visible; s_u[it & 1] may be overwritten
   }
 }
 
@@ -365,12 +453,14 @@ cudaError_t launch_ssc_init(PopDev* pops, int npop, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ssc_resample(PopDev* pops, int npop, cudaStream_t s) {
+cudaError_t launch_ssc_resample(BatchDev* b, cudaStream_t s) {
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int x = (nsm * 8 + npop - 1) / npop;
-  ssc_resample_kernel<<<dim3(x < 16 ? 16 : x, npop), 128, 0, s>>>(pops);
+  ssc_resample_plan_kernel<<<1, 1024, 0, s>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  ssc_resample_kernel<<<nsm * kSscResBlocksPerSM, kSscResThreads, 0, s>>>(b);  // persistent CTAs
   return cudaGetLastError();
 }
 

@@ -246,7 +246,7 @@ int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_n
   h.src = const_cast<uint32_t*>(src);
   int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  return finish(launch_resample(S.b, S.st, 1, kSSC, s), s, "ssc_resample");
+  return finish(launch_resample(S.b, kSSC, s), s, "ssc_resample");
 }
 
 int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R_new, uint32_t* new_words,
@@ -265,7 +265,7 @@ int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R
   h.src = const_cast<uint32_t*>(src);
   int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  return finish(launch_resample(S.b, S.st, 1, kMSC, s), s, "msc_resample");
+  return finish(launch_resample(S.b, kMSC, s), s, "msc_resample");
 }
 
 }  // extern "C"

@@ -131,8 +131,11 @@ def test_resample_plan_fp32_close_to_fp64(cuda, st, oracle, coding):
     assert diff <= 2
 
 
-@pytest.mark.parametrize("L,R", [(16, 50), (64, 30)])
+@pytest.mark.parametrize("L,R", [(16, 50), (64, 30), (8, 700), (24, 130), (128, 9), (192, 7), (256, 5)])
 def test_ssc_resample_gather(cuda, st, oracle, L, R):
+    """Work units of whole replicas (L <= 128, the last one partial, e.g. L=24:
+    56 replicas of 36 vectors) and of replica parts (L=192: 2048 + 256
+    vectors, L=256: 2 x 2048) copy exactly what resampleKer copies."""
     torch = cuda
     old = oracle.ssc_init(L, R, 4, 0)
     rng = np.random.default_rng(1)
