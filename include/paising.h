@@ -145,16 +145,34 @@ PA_API int pa_run_end(pa_handle* h);
 PA_API int pa_checkpoint(pa_handle* h, const char* path);
 PA_API int pa_restore(pa_handle* h, const char* path);
 
-/* Autotuner of the MSC one-CTA sweep: for every lattice size of the handle,
- * times one sweep launch of its populations (freshly initialised, at the
- * first temperature) with 1, 2, 4 and 8 groups stacked per work unit where
- * valid, keeps the fastest per spin-flip attempt and rebuilds the launch plan
- * (and graph).  Must precede the first pa_run; the runs that follow start
- * from the configured state exactly as without it.  tiles[k] (k < n, may be
- * null with n = 0) receives population k's choice.  Results are unchanged by
- * the choice under the reference stream.  No counterpart in the reference,
- * whose launch shapes are compile-time constants. */
+/* Autotuner of the sweep's tile shape and spins per word.  It times one
+ * sweep launch of the handle's populations (freshly initialised, at the first
+ * temperature) per candidate, keeps the fastest per spin-flip attempt and
+ * rebuilds the launch plan (and graph):
+ *   MSC, one CTA per work unit: for every lattice size, 1, 2, 4 or 8 groups
+ *     of 32 replicas stacked per work unit, where valid.  Results are
+ *     unchanged by the choice (draws are keyed by group and site).
+ *   SSC, native stream, every L in {64, 128, 256} and sweep_variant 0: the
+ *     int8 sweep (4 sites of a replica per 32-bit word) or the bit-plane sweep
+ *     (32 sites per word) for the whole batch.  The two forms draw different
+ *     native streams (both with acceptance probability exactly T/2^32), so
+ *     the choice changes the trajectory, not the statistics.
+ * Must precede the first pa_run; the runs that follow start from the
+ * configured state exactly as without it.  tiles[k] (k < n, may be null with
+ * n = 0) receives population k's work-unit size (groups per tile for MSC,
+ * replicas per tile for SSC); pa_sweep_form reports the whole form.  No
+ * counterpart in the reference, whose launch shapes and MSbits are
+ * compile-time constants (PAisingMSC.cu:34). */
 PA_API int pa_autotune(pa_handle* h, int* tiles, int n);
+
+/* The sweep form population `index` is annealed with. */
+typedef struct pa_sweep_form_t {
+  int spins_per_word;    /* spins held by one 32-bit word: SSC 4 (int8) or 32 (bit planes); MSC 32 */
+  int replicas_per_word; /* SSC 1; MSC 32 (bit k = replica k of the group) */
+  int tile;              /* work unit: MSC groups per tile, SSC replicas per tile */
+  int cluster_ctas;      /* CTAs sweeping one MSC group together (1, 2 or 4); SSC 1 */
+} pa_sweep_form_t;
+PA_API int pa_sweep_form(const pa_handle* h, int index, pa_sweep_form_t* out);
 
 /* Number of result sets a pa_run produces: one per population per
  * sequential run (PA_results_run_<set>.dat). */

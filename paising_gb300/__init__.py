@@ -63,6 +63,11 @@ class KernelTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 24), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
 
 
+class SweepForm(ctypes.Structure):
+    _fields_ = [("spins_per_word", ctypes.c_int), ("replicas_per_word", ctypes.c_int), ("tile", ctypes.c_int),
+                ("cluster_ctas", ctypes.c_int)]
+
+
 _vp, _i, _u64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_double
 _SIGS = {
     "pa_abi_version": ([], _i),
@@ -70,6 +75,7 @@ _SIGS = {
     "pa_create": ([ctypes.POINTER(Config), ctypes.POINTER(_vp)], _i),
     "pa_run": ([_vp], _i),
     "pa_autotune": ([_vp, _vp, _i], _i),
+    "pa_sweep_form": ([_vp, _i, ctypes.POINTER(SweepForm)], _i),
     "pa_get_mhr_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_energies": ([_vp, _i, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_family_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
@@ -246,12 +252,20 @@ class Engine:
         return out
 
     def autotune(self) -> list[int]:
-        """Time the MSC tile sizes and keep the fastest (pa_autotune); returns
-        the groups per work unit chosen for each population."""
+        """Time the sweep forms and keep the fastest (pa_autotune): MSC groups
+        per work unit, SSC int8 or bit-plane sweep.  Returns each population's
+        work-unit size (sweep_form() gives the whole form)."""
         n = len(self.configs)
         arr = (ctypes.c_int * n)()
         _check(lib().pa_autotune(self._h, arr, n), self._h)
         return list(arr)
+
+    def sweep_form(self, index: int = 0) -> dict:
+        """{spins_per_word, replicas_per_word, tile, cluster_ctas} of population
+        `index` (pa_sweep_form)."""
+        f = SweepForm()
+        _check(lib().pa_sweep_form(self._h, index, ctypes.byref(f)), self._h)
+        return {k: getattr(f, k) for k, _ in SweepForm._fields_}
 
     def num_rows(self) -> int:
         n = ctypes.c_int()

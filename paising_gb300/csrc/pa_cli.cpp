@@ -8,7 +8,7 @@
 // (resampling weights), -g 0|1 (host-stepped or graph), -D device, -a (the
 // adaptive temperature step of the reference's AdaptiveStep build, with its
 // output directory ./data%s_L%d_R%d_EqSw%d/, PAisingSSC.cu:406-410), -T (time
-// the MSC tile sizes before the run, pa_autotune), -H (multi-histogram
+// the tile sizes and SSC spins per word before the run, pa_autotune), -H (multi-histogram
 // reweighting, the MHR build: PA_MHR_results_run_<r>.dat), -E (energies of
 // every temperature, the EnergiesPopStore build: PA_energies_<i>.dat), -F
 // (family statistics, PA_family_run_<r>.dat; not in the reference), -S (the
@@ -45,7 +45,7 @@ static void usage(const char* prog) {
       " -g 0|1             ( 1: one CUDA graph per run (default), 0: host steps each temperature )\n"
       " -D device          ( CUDA device ordinal )\n"
       " -a                 ( adaptive temperature step, MinOverlap 0.85, MaxOverlap 0.87 )\n"
-      " -T                 ( autotune the MSC sweep's tile sizes before the run )\n"
+      " -T                 ( autotune the sweep's tile sizes and SSC spins per word before the run )\n"
       " -H                 ( multi-histogram reweighting: PA_MHR_results_run_<r>.dat )\n"
       " -E                 ( store the energies of every temperature: PA_energies_<i>.dat )\n"
       " -F                 ( family statistics of every temperature: PA_family_run_<r>.dat )\n"

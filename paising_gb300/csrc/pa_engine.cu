@@ -573,15 +573,18 @@ struct pa_handle {
 
   // Device time per spin-flip attempt of one sweep launch over the
   // populations flagged in `part` (the others are marked finished), with
-  // geometry `geo` for them; the population state is the one left on the
-  // device by the caller (an initialised population at step 1).
-  cudaError_t time_sweep(const std::vector<PopDev>& state, const std::vector<char>& part, const SweepGeom& geo,
-                         double* ns_per_attempt) {
+  // geometry geo[k] for population k (SSC: `bits` selects the bit-plane
+  // sweep); the population state is the one left on the device by the caller
+  // (an initialised population at step 1).
+  cudaError_t time_sweep(const std::vector<PopDev>& state, const std::vector<char>& part,
+                         const std::vector<SweepGeom>& geo, bool bits, double* ns_per_attempt) {
     std::vector<PopDev> hp = state;
     double attempts = 0;
+    int smem = 0;
     for (int k = 0; k < npop; ++k) {
       if (part[k]) {
-        geom_to_pop(geo, &hp[k]);
+        geom_to_pop(geo[k], &hp[k]);
+        smem = std::max(smem, geo[k].smem);
         if (pop_stepping(&hp[k])) attempts += (double)pops[k].cfg.sweeps * hp[k].N * (double)hp[k].R_cur;
       } else {
         hp[k].step = hp[k].nsteps + 1;
@@ -589,12 +592,14 @@ struct pa_handle {
     }
     cudaError_t e = upload_pops(hp);
     SweepLaunch sl{};
-    if (e == cudaSuccess) e = sweep_setup(coding, rng_mode, geo.smem, &sl);
+    if (e == cudaSuccess) e = bits ? ssc_bits_setup(smem, &sl) : sweep_setup(coding, rng_mode, smem, &sl);
     float best = 0.f;
     for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {  // the first launch warms up
       e = launch_plan(d_batch, npop, 0, stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
-      if (e == cudaSuccess) e = launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sl, stream);
+      if (e == cudaSuccess)
+        e = bits ? launch_ssc_bits_sweep(d_batch, 0, stream_seed, sl, stream)
+                 : launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sl, stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
       if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
       float ms = 0.f;
@@ -1187,37 +1192,66 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
     H->err = "pa_autotune must precede the first pa_run";
     return PA_ERR_STATE;
   }
-  if (H->coding == PA_CODING_MSC && H->cs == 1) {
+  const bool msc_tiles = H->coding == PA_CODING_MSC && H->cs == 1;
+  // SSC, native stream: int8 (4 sites per word) or bit planes (32 sites per
+  // word) for the whole batch, when every population allows both and asks
+  // for neither
+  bool ssc_forms = H->coding == PA_CODING_SSC && H->rng_mode == PA_RNG_NATIVE;
+  for (const auto& P : H->pops) {
+    SweepGeom gb;
+    if (P.cfg.sweep_variant != 0 || !ssc_bits_geom(P.cfg.L, &gb)) ssc_forms = false;
+  }
+  if (msc_tiles || ssc_forms) {
     // an initialised population (step 1, random spins) to sweep
     cudaError_t e = H->enqueue_init();
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     std::vector<PopDev> state(H->npop);
     if (e == cudaSuccess) e = cudaMemcpy(state.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
-    std::vector<int> done(H->npop, 0);
-    for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
-      if (done[k]) continue;
-      const int L = H->pops[k].cfg.L;
-      std::vector<char> part(H->npop, 0);
-      for (int j = 0; j < H->npop; ++j) part[j] = H->pops[j].cfg.L == L;
-      int best_G = 1;
-      double best = 0;
-      for (int G = 1; G <= 8 && e == cudaSuccess; G *= 2) {
-        SweepGeom g;
-        if (!msc_geom(L, &g, G)) continue;
-        double t = 0;
-        e = H->time_sweep(state, part, g, &t);
-        if (e == cudaSuccess && t > 0 && (best == 0 || t < best)) {
-          best = t;
-          best_G = G;
+    if (msc_tiles) {  // groups per tile, per lattice size
+      std::vector<int> done(H->npop, 0);
+      for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+        if (done[k]) continue;
+        const int L = H->pops[k].cfg.L;
+        std::vector<char> part(H->npop, 0);
+        for (int j = 0; j < H->npop; ++j) part[j] = H->pops[j].cfg.L == L;
+        int best_G = 1;
+        double best = 0;
+        for (int G = 1; G <= 8 && e == cudaSuccess; G *= 2) {
+          SweepGeom g;
+          if (!msc_geom(L, &g, G)) continue;
+          double t = 0;
+          e = H->time_sweep(state, part, std::vector<SweepGeom>(H->npop, g), false, &t);
+          if (e == cudaSuccess && t > 0 && (best == 0 || t < best)) {
+            best = t;
+            best_G = G;
+          }
         }
+        for (int j = 0; j < H->npop; ++j)
+          if (part[j]) {
+            done[j] = 1;
+            PopHost& P = H->pops[j];
+            msc_geom(L, &P.geom, best_G);
+            geom_to_pop(P.geom, &P.h);
+          }
       }
-      for (int j = 0; j < H->npop; ++j)
-        if (part[j]) {
-          done[j] = 1;
-          PopHost& P = H->pops[j];
-          msc_geom(L, &P.geom, best_G);
+    } else {  // SSC sweep form of the batch
+      std::vector<char> all(H->npop, 1);
+      std::vector<SweepGeom> g8(H->npop), gb(H->npop);
+      for (int k = 0; k < H->npop; ++k) {
+        ssc_geom(H->pops[k].cfg.L, &g8[k]);
+        ssc_bits_geom(H->pops[k].cfg.L, &gb[k]);
+      }
+      double t8 = 0, tb = 0;
+      if (e == cudaSuccess) e = H->time_sweep(state, all, g8, false, &t8);
+      if (e == cudaSuccess) e = H->time_sweep(state, all, gb, true, &tb);
+      if (e == cudaSuccess) {
+        H->ssc_bits = tb > 0 && (t8 <= 0 || tb <= t8);
+        for (int k = 0; k < H->npop; ++k) {
+          PopHost& P = H->pops[k];
+          P.geom = H->ssc_bits ? gb[k] : g8[k];
           geom_to_pop(P.geom, &P.h);
         }
+      }
     }
     // the run starts from the configured state again (stream positions included)
     std::vector<PopDev> hp(H->npop);
@@ -1229,6 +1263,20 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
   for (int k = 0; k < H->npop; ++k)
     if (H->pops[k].user_index < n) tiles[H->pops[k].user_index] = H->pops[k].geom.G;
   return PA_OK;
+}
+
+int pa_sweep_form(const pa_handle* H, int index, pa_sweep_form_t* out) {
+  if (!H || !out) return PA_ERR_ARG;
+  for (const auto& P : H->pops)
+    if (P.user_index == index) {
+      const bool msc = P.cfg.coding == PA_CODING_MSC;
+      out->spins_per_word = msc ? kMsb : (H->ssc_bits ? 32 : 4);
+      out->replicas_per_word = msc ? kMsb : 1;
+      out->tile = P.geom.G;
+      out->cluster_ctas = msc ? H->cs : 1;
+      return PA_OK;
+    }
+  return PA_ERR_ARG;
 }
 
 int pa_num_rows(const pa_handle* H, int* n) {

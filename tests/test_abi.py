@@ -70,6 +70,8 @@ def test_stage_argument_checks(engine_lib):
     assert engine_lib.pa_ssc_sweep(None, 64, 10, 1, 0.4, 0, 1, 0, 1, None, None, None) == 1
     assert engine_lib.pa_msc_sweep(None, None, 64, 1, 1, 0.4, 0, 1, 0, 1, None, None, None) == 1
     assert engine_lib.pa_resample_plan(None, None, 0, 10, 10, 10, 0, 0.1, 0, 0, 1, 0, None, None, None, None, None) == 1
+    assert engine_lib.pa_sweep_form(None, 0, None) == 1
+    assert engine_lib.pa_autotune(None, None, 0) == 1
 
 
 def test_cli_argument_errors():

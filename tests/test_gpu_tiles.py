@@ -94,3 +94,48 @@ def test_autotune_batch(cuda, oracle):
         for k, p in enumerate(pops):
             ref, _ = oracle.anneal("msc", p["L"], p["R"], p["sweeps"], p["dbeta"], 1.0, 1, p["seed"])
             compare_rows(e.rows(k), ref[0], rtol=1e-9)
+
+
+def test_autotune_ssc_spins_per_word(cuda):
+    """SSC with the native stream at L in {64, 128}: the autotuner times the
+    int8 sweep (4 sites per word) against the bit-plane sweep (32 sites per
+    word) on the batch and keeps the faster.  At these sizes (1250 bit-plane
+    tiles) that is the bit-plane sweep, 4-5x faster, which the engine also uses
+    untuned: the tuned run equals the untuned one bit for bit."""
+    pops = [dict(L=64, R=20000, sweeps=2, dbeta=0.25, seed=21), dict(L=128, R=5000, sweeps=2, dbeta=0.25, seed=22)]
+
+    def go(tune, **kw):
+        with pa.Engine.batch([dict(p, **kw) for p in pops], coding="ssc") as e:
+            tiles = e.autotune() if tune else None
+            forms = [e.sweep_form(k) for k in range(len(pops))]
+            e.run()
+            return tiles, forms, [e.rows(k) for k in range(len(pops))]
+
+    tiles, forms, tuned = go(True)
+    assert tiles == [16, 4]  # replicas per 1024-word tile
+    assert all(f["spins_per_word"] == 32 and f["replicas_per_word"] == 1 and f["cluster_ctas"] == 1 for f in forms)
+    _, _, plain = go(False)
+    for a, b in zip(tuned, plain):
+        assert np.array_equal(a, b)
+    # the other form draws another native stream (its physics is checked
+    # against the exact solution in the SSC tests)
+    _, forms8, int8 = go(False, sweep_variant=1)
+    assert forms8[0]["spins_per_word"] == 4
+    assert not np.array_equal(int8[0], plain[0])
+
+
+def test_sweep_form_reports(cuda):
+    """pa_sweep_form: SSC int8 where bit planes do not apply (L=32, or the
+    reference stream), MSC 32 replicas per word with its tile and cluster."""
+    with pa.Engine(L=32, R=100, coding="ssc") as e:
+        e.autotune()  # nothing to choose: L=32 has no bit-plane form
+        assert e.sweep_form() == dict(spins_per_word=4, replicas_per_word=1, tile=1, cluster_ctas=1)
+    with pa.Engine(L=64, R=100, coding="ssc", rng="reference") as e:
+        assert e.sweep_form()["spins_per_word"] == 4
+    with pa.Engine(L=16, R=1000, coding="msc", tile_groups=4) as e:
+        assert e.sweep_form() == dict(spins_per_word=32, replicas_per_word=32, tile=4, cluster_ctas=1)
+    with pa.Engine(L=256, R=64, coding="msc") as e:
+        assert e.sweep_form()["cluster_ctas"] == 2
+    with pa.Engine(L=16, R=100, coding="msc") as e:
+        with pytest.raises(pa.PaisingError):
+            e.sweep_form(1)
