@@ -123,15 +123,37 @@ def load_profile_traffic(kernel: str, workload: str):
 
 
 def dist_init():
+    """(rank, local rank, world size, torch.distributed or None) of a
+    torchrun launch; one rank per GPU (NCCL), gloo where no GPU is present."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws == 1:
         return 0, 0, 1, None
     import torch
     import torch.distributed as dist
     rank, lrank = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(lrank)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(lrank)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, lrank, ws, dist
+
+
+def rank_seed(rank: int) -> int:
+    """Seed of the populations rank `rank` anneals: the ranks run independent
+    replicas of the workload (no data-parallel exchange on this path)."""
+    return 1000 + 97 * rank
+
+
+def reduce_over_ranks(dist, device, elapsed: float, attempts: float):
+    """Whole-job figures of a multi-rank run: the slowest rank's time and the
+    attempts of all ranks (MAX and SUM all-reduces; identity on one rank)."""
+    if not dist:
+        return elapsed, attempts
+    import torch
+    t = torch.tensor([elapsed, attempts], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return mx[0].item(), t[1].item()
 
 
 # ------------------------------------------------------------- our engine
@@ -162,7 +184,7 @@ def run_ours(a):
     torch.cuda.set_device(dev)
     P = a.populations
     eng = pa.Engine(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=P,
-                    seed=1000 + 97 * rank, coding=a.coding, rng="native", weights="fp32", graph=bool(a.graph),
+                    seed=rank_seed(rank), coding=a.coding, rng="native", weights="fp32", graph=bool(a.graph),
                     device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")  # > L2 (129 MB)
     for _ in range(a.warmup):
@@ -189,15 +211,7 @@ def run_ours(a):
             ms_steps.append(ms)
             att_steps.append(att)
         barrier()
-    tot_ms, tot_att = sum(ms_steps), sum(att_steps)
-    if dist:
-        t = torch.tensor([tot_ms, tot_att], dtype=torch.float64, device=f"cuda:{dev}")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        tot_ms_max, tot_att_all = mx[0].item(), t[1].item()
-    else:
-        tot_ms_max, tot_att_all = tot_ms, tot_att
+    tot_ms_max, tot_att_all = reduce_over_ranks(dist, f"cuda:{dev}", sum(ms_steps), sum(att_steps))
     value = tot_att_all / (tot_ms_max * 1e6)
 
     # end to end through the C ABI with host buffers: every step uploads the
@@ -225,13 +239,7 @@ def run_ours(a):
         e2e_att += eng.timing()[1]
         rows_bytes = sum(r.nbytes for r in rows)
     eng.set_population(None)
-    e2e_tot = sum(e2e_s)
-    if dist:
-        t = torch.tensor([e2e_tot, e2e_att], dtype=torch.float64, device=f"cuda:{dev}")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e_tot, e2e_att = mx[0].item(), t[1].item()
+    e2e_tot, e2e_att = reduce_over_ranks(dist, f"cuda:{dev}", sum(e2e_s), e2e_att)
     e2e_value = e2e_att / (e2e_tot * 1e9)
 
     out = None
