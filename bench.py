@@ -341,9 +341,9 @@ def profile_leg(a, eng, pa) -> dict:
     # algorithmic INT32 operations per spin-flip attempt: MSC ~5 (bitsliced
     # neighbour count and acceptance mask shared by 32 replicas), SSC ~33 (a
     # 32-bit Philox word, ~25 operations, plus the update of one site).  The
-    # native SSC sweep at L = 64, 128, 256 runs on bit planes (32 sites of one
-    # replica per word) and so does the bitsliced work of the MSC figure.
-    ssc_bits = a.coding == "ssc" and a.L in (64, 128, 256)
+    # native SSC sweep on bit planes (32 sites per word) does the bitsliced
+    # work of the MSC figure.
+    ssc_bits = a.coding == "ssc" and eng.sweep_form(0)["spins_per_word"] == 32
     ops_per_attempt = 5.0 if a.coding == "msc" or ssc_bits else 33.0
     achieved = attempts_per_launch * ops_per_attempt / (avg_ms * 1e-3) / 1e12
     peaks = pa.probe_int_issue(eng.config.device)

@@ -71,9 +71,15 @@ typedef struct pa_config {
   int device;        /* CUDA device ordinal */
   double capacity;   /* replica buffer = ceil(capacity * R) + 256; 0 selects 1.25 */
   int sweep_variant; /* MSC sweep kernel: 0 automatic, 1 one CTA per group, 2 or 4: a thread-block
-                        cluster of that many CTAs per group (needed for L > 128) */
+                        cluster of that many CTAs per group (needed for L > 128).  SSC: 0 automatic
+                        (native stream: bit planes, 32 sites per word, where L packs into words at
+                        least 3/4 full -- L = 8, 16, 24, 32, 48, 56, 64, 96, 112, 128, 144, 168, 192,
+                        224, 240, 256 -- else int8), 1 int8 */
   int tile_groups;   /* MSC groups stacked into one work unit of the one-CTA sweep: 0 automatic,
-                        1, 2, 4 or 8 (more than 1 needs L % 4 == 0 and at most 44 KB per tile) */
+                        1, 2, 4 or 8 (more than 1 needs L % 4 == 0 and at most 44 KB per tile).
+                        SSC bit planes (native stream): replicas per tile, 0 automatic, else the
+                        largest tile for L (pa_sweep_form) or a power-of-two fraction of it; the
+                        whole batch then runs on bit planes */
   int adaptive;      /* 1: adaptive temperature step, the reference's AdaptiveStep build
                         (PAisingSSC.cu:23,306-334,644-660): after every temperature the next step is
                         the largest (grown by 1.1x, else bisected) whose energy-histogram overlap lies
@@ -152,11 +158,12 @@ PA_API int pa_restore(pa_handle* h, const char* path);
  *   MSC, one CTA per work unit: for every lattice size, 1, 2, 4 or 8 groups
  *     of 32 replicas stacked per work unit, where valid.  Results are
  *     unchanged by the choice (draws are keyed by group and site).
- *   SSC, native stream, every L in {64, 128, 256} and sweep_variant 0: the
- *     int8 sweep (4 sites of a replica per 32-bit word) or the bit-plane sweep
- *     (32 sites per word) for the whole batch.  The two forms draw different
- *     native streams (both with acceptance probability exactly T/2^32), so
- *     the choice changes the trajectory, not the statistics.
+ *   SSC, native stream, every L with a bit-plane layout and sweep_variant 0:
+ *     for every lattice size the bit-plane tile (replicas per work unit), then
+ *     for the whole batch the int8 sweep (4 sites of a replica per 32-bit
+ *     word) or the bit-plane sweep (32 sites per word).  The forms and tiles
+ *     draw different native streams (all with acceptance probability exactly
+ *     T/2^32), so the choice changes the trajectory, not the statistics.
  * Must precede the first pa_run; the runs that follow start from the
  * configured state exactly as without it.  tiles[k] (k < n, may be null with
  * n = 0) receives population k's work-unit size (groups per tile for MSC,
@@ -294,6 +301,16 @@ PA_API int pa_ssc_init(int8_t* spins, int L, int R, uint64_t seed, uint64_t iseq
  * Metropolis sweeps at inverse temperature beta, then E and M per replica. */
 PA_API int pa_ssc_sweep(int8_t* spins, int L, int R, int sweeps, double beta, int rng_mode, uint64_t seed,
                  uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream);
+
+/* The same sweeps on bit planes (native stream only; no counterpart in the
+ * reference): the population is packed to one bit per site in shared memory
+ * (a sublattice row as words of up to 32 sites, or several replicas' rows per
+ * word when a row has at most 16 sites), swept with the bitsliced adder and
+ * the digit-serial acceptance, and unpacked.  Each site flips with
+ * probability exactly min(1, T/2^32) like pa_ssc_sweep's native stream, from
+ * another stream.  PA_ERR_ARG where L has no bit-plane layout. */
+PA_API int pa_ssc_sweep_bits(int8_t* spins, int L, int R, int sweeps, double beta, uint64_t seed, int step,
+                             int32_t* E, int32_t* M, void* stream);
 
 /* ReplicaInit (PAisingMSC.cu:169-188): ceil(R/32) groups, active bits. */
 PA_API int pa_msc_init(uint32_t* words, uint8_t* active, int L, int R, uint64_t seed, uint64_t iseq, void* stream);

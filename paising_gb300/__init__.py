@@ -102,6 +102,7 @@ _SIGS = {
     "pa_probe_int_issue": ([_i, _vp], _i),
     "pa_ssc_init": ([_vp, _i, _i, _u64, _u64, _vp], _i),
     "pa_ssc_sweep": ([_vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
+    "pa_ssc_sweep_bits": ([_vp, _i, _i, _i, _d, _u64, _i, _vp, _vp, _vp], _i),
     "pa_msc_init": ([_vp, _vp, _i, _i, _u64, _u64, _vp], _i),
     "pa_msc_sweep": ([_vp, _vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
     "pa_resample_plan": ([_vp, _vp, _i, _i, _i, _i, _d, _d, _d, _i, _u64, _u64, _vp, _vp, _vp, _vp, _vp], _i),

@@ -643,11 +643,18 @@ int validate(const pa_config& c) {
   if (c.sweep_variant != 0 && c.sweep_variant != 1 && c.sweep_variant != 2 && c.sweep_variant != 4)
     return bad("sweep_variant must be 0, 1, 2 or 4");
   if (c.coding == PA_CODING_SSC && c.sweep_variant > 1) return bad("cluster sweeps exist for MSC only");
-  if (c.tile_groups != 0 && c.tile_groups != 1 && c.tile_groups != 2 && c.tile_groups != 4 && c.tile_groups != 8)
-    return bad("tile_groups must be 0, 1, 2, 4 or 8");
-  if (c.tile_groups > 1 && (c.coding != PA_CODING_MSC || msc_variant(c.sweep_variant, c.L) > 1))
-    return bad("tiles of several groups exist for the one-CTA MSC sweep only");
   SweepGeom g;
+  if (c.coding == PA_CODING_SSC && c.tile_groups != 0) {
+    // replicas per tile of the bit-plane sweep
+    if (c.rng_mode != PA_RNG_NATIVE || c.sweep_variant == 1 || !ssc_bits_geom(c.L, &g, c.tile_groups))
+      return bad("SSC tile_groups: replicas per bit-plane tile (native stream), the largest tile for L or a "
+                 "power-of-two fraction of it");
+  } else {
+    if (c.tile_groups != 0 && c.tile_groups != 1 && c.tile_groups != 2 && c.tile_groups != 4 && c.tile_groups != 8)
+      return bad("tile_groups must be 0, 1, 2, 4 or 8");
+    if (c.tile_groups > 1 && msc_variant(c.sweep_variant, c.L) > 1)
+      return bad("tiles of several groups exist for the one-CTA MSC sweep only");
+  }
   if (c.coding == PA_CODING_MSC) {
     const int cs = msc_variant(c.sweep_variant, c.L);
     if (cs == 1 && c.tile_groups > 1 && !msc_geom(c.L, &g, c.tile_groups))
@@ -704,12 +711,24 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
       batch_groups += (c.R + kMsb - 1) / kMsb;
     }
-  // SSC with the native stream: bit-plane sweep when every lattice allows it
-  // (sweep_variant 1 keeps the int8 sweep)
+  // SSC with the native stream: bit-plane sweep when every lattice packs
+  // into words at least 3/4 full (sweep_variant 1 keeps the int8 sweep;
+  // pa_autotune may also choose a sparser bit-plane layout by timing)
   H->ssc_bits = H->coding == PA_CODING_SSC && H->rng_mode == PA_RNG_NATIVE;
+  long long batch_replicas = 0;  // work of the bit-plane sweep: bounds its tile sizes
+  bool ssc_tiles = false;        // a population asks for a bit-plane tile size
   for (const auto& c : cfgs) {
-    SweepGeom gb;
-    if (c.sweep_variant == 1 || !ssc_bits_geom(c.L, &gb)) H->ssc_bits = false;
+    if (c.sweep_variant == 1 || ssc_bits_fill(c.L) < 0.75) H->ssc_bits = false;
+    batch_replicas += c.R;
+    ssc_tiles = ssc_tiles || (c.coding == PA_CODING_SSC && c.tile_groups > 0);
+  }
+  if (ssc_tiles) {  // every population of the batch then needs a bit-plane layout
+    H->ssc_bits = true;
+    for (const auto& c : cfgs) {
+      SweepGeom gb;
+      if (c.sweep_variant == 1 || !ssc_bits_geom(c.L, &gb)) return fail(PA_ERR_ARG, "SSC tile_groups needs every "
+                                                                      "population of the batch on bit planes");
+    }
   }
   H->pops.resize(cfgs.size());
   for (size_t k = 0; k < cfgs.size(); ++k) {
@@ -718,7 +737,9 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     P.user_index = (int)k;
     if (P.cfg.capacity <= 0) P.cfg.capacity = 1.25;
     bool okg;
-    if (P.cfg.coding == PA_CODING_SSC) okg = H->ssc_bits ? ssc_bits_geom(P.cfg.L, &P.geom) : ssc_geom(P.cfg.L, &P.geom);
+    if (P.cfg.coding == PA_CODING_SSC)
+      okg = H->ssc_bits ? ssc_bits_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_replicas, slots)
+                        : ssc_geom(P.cfg.L, &P.geom);
     else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_groups, slots);
     else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
     if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +
@@ -1234,12 +1255,34 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
             geom_to_pop(P.geom, &P.h);
           }
       }
-    } else {  // SSC sweep form of the batch
+    } else {  // SSC: bit-plane replicas per tile for every lattice size, then the form of the batch
       std::vector<char> all(H->npop, 1);
       std::vector<SweepGeom> g8(H->npop), gb(H->npop);
-      for (int k = 0; k < H->npop; ++k) {
-        ssc_geom(H->pops[k].cfg.L, &g8[k]);
-        ssc_bits_geom(H->pops[k].cfg.L, &gb[k]);
+      for (int k = 0; k < H->npop; ++k) ssc_geom(H->pops[k].cfg.L, &g8[k]);
+      std::vector<int> done(H->npop, 0);
+      for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+        if (done[k]) continue;
+        const int L = H->pops[k].cfg.L;
+        std::vector<char> part(H->npop, 0);
+        for (int j = 0; j < H->npop; ++j) part[j] = H->pops[j].cfg.L == L;
+        SweepGeom best_g;
+        ssc_bits_geom(L, &best_g);  // the largest tile
+        double best = 0;
+        for (int t = best_g.G; t >= 1 && e == cudaSuccess; t /= 2) {
+          SweepGeom g;
+          if (!ssc_bits_geom(L, &g, t)) continue;
+          double tt = 0;
+          e = H->time_sweep(state, part, std::vector<SweepGeom>(H->npop, g), true, &tt);
+          if (e == cudaSuccess && tt > 0 && (best == 0 || tt < best)) {
+            best = tt;
+            best_g = g;
+          }
+        }
+        for (int j = 0; j < H->npop; ++j)
+          if (part[j]) {
+            done[j] = 1;
+            gb[j] = best_g;
+          }
       }
       double t8 = 0, tb = 0;
       if (e == cudaSuccess) e = H->time_sweep(state, all, g8, false, &t8);

@@ -25,6 +25,8 @@ struct SweepGeom {
   int kconst;  // (N/2)/128 when 128 divides N/2 (draws per reference thread per half sweep), else 0
   int smem;    // dynamic shared memory bytes for one work unit
   int G = 1;   // MSC groups per work unit: G lattices stacked as G*L rows of one sweep
+              // (SSC bit planes: replicas per work unit)
+  int seg = 0; // SSC bit planes: sites of a sublattice row per word segment
 };
 
 // ceil(2^32 / d) for 2 <= d < 2^16: then __umulhi(n, recip32(d)) == n / d
@@ -79,9 +81,17 @@ cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_ssc_resample(BatchDev* b, cudaStream_t s);
 cudaError_t launch_msc_resample(BatchDev* b, cudaStream_t s);
 
-// SSC populations swept on bit planes (native stream, L = 64, 128, 256):
-// tiles of G replicas packed to one bit per site in shared memory.
-bool ssc_bits_geom(int L, SweepGeom* g);
+// SSC populations swept on bit planes (native stream): tiles of G replicas
+// packed to one bit per site in shared memory, a sublattice row as Wr words
+// of `seg` sites (several replicas' rows per word when a row is at most 16
+// sites).  False where L has no such layout.  Replicas per tile: `tile` if
+// given (a power-of-two fraction of the largest tile, else false), else by a
+// cost model from the batch's replicas and resident CTAs (`slots`), else the
+// largest tile (about 1024 words per plane).
+bool ssc_bits_geom(int L, SweepGeom* g, int tile = 0, long long replicas = 0, int slots = 0);
+// Fraction of the bits of the packed words that hold sites (1 at L = 16, 32,
+// 64, 128, 256; 0.75 at L = 24, 48, 96; 0 where no bit-plane layout exists).
+double ssc_bits_fill(int L);
 cudaError_t ssc_bits_setup(int smem, SweepLaunch* out);
 cudaError_t launch_ssc_bits_sweep(BatchDev* b, int energy_only, unsigned long long seed, const SweepLaunch& sl,
                                   cudaStream_t s);

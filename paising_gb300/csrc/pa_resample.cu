@@ -557,6 +557,7 @@ void geom_to_pop(const SweepGeom& g, PopDev* h) {
   h->npass = g.npass;
   h->kconst = g.kconst;
   h->gpt = g.G;
+  h->seg = g.seg;
   h->invL = recip32(g.L);
   h->invWr = recip32(g.Wr);
 }

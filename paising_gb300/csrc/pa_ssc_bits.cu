@@ -1,24 +1,31 @@
 // pa_ssc_bits.cu -- single-spin-coded populations swept on bit planes
-// (native stream, L = 64, 128 or 256).
+// (native stream).
 //
 // The population stays in the SSC layout in HBM (one int8 +-1 per site,
 // sublattice A then B, site (x, y) at idx = y*L/2 + x/2, PAisingSSC.cu:169).
-// A CTA loads a tile of G replicas and packs every sublattice row of each
-// into L/64 words, bit i = site i of the row (1 == +1): "multi-site coding",
-// 32 sites of one replica per word.  In a checkerboard half-sweep the sites of
-// one sublattice are independent, so a row word is updated at once: its four
-// neighbour words are the other sublattice's rows y-1, y, y+1 and row y
-// shifted by one site (towards x-1 or x+1 by row parity, as in
-// PAisingSSC.cu:170,182), their anti-parallel counts come from the bitsliced
-// adder, and the 32 Metropolis decisions from the digit-serial acceptance of
+// A CTA loads a tile of replicas and packs every sublattice row (S = L/2
+// sites) into bits, 1 == +1: "multi-site coding".  A row takes Wq words of
+// `seg` sites each (seg a multiple of 4, at most 32); when a row fits one
+// word, floor(32/seg) rows of different replicas share it as segments (L=16:
+// 4 replicas x 8 sites, L=32: 2 x 16, L=48: one 24-site segment).  In a
+// checkerboard half-sweep the sites of one sublattice are independent, so a
+// word is updated at once: its four neighbour words are the other
+// sublattice's rows y-1, y, y+1 and row y shifted by one site towards x-1 or
+// x+1 by row parity (PAisingSSC.cu:170,182) -- periodically inside each
+// segment, or across the row's words -- their anti-parallel counts come from
+// the bitsliced adder, and the decisions from the digit-serial acceptance of
 // the multi-spin-coded sweep (accept_native): each site flips with
 // probability exactly min(1, T/2^32), T = ceil(2^32 e^{-beta dE}), the
-// thresholds of the int8 sweep.  The energy and magnetisation of each replica
-// are population counts of the planes.  The tile is unpacked and written
-// back once per temperature.
+// thresholds of the int8 sweep.  Bits outside the segments stay 0.  The
+// energy and magnetisation of each replica are population counts of its
+// segments.  The tile is unpacked and written back once per temperature.
 //
-// Work per tile and half-sweep: G * L * L/64 row words = 1024, four per
-// thread, decided together (kKB = 4).
+// Work per tile and half-sweep: about 1024 words, four per thread, decided
+// together (kKB = 4).
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
 #include "pa_kernels.h"
 #include "pa_msc_core.cuh"
 
@@ -29,54 +36,196 @@ using namespace msc;
 namespace {
 
 constexpr uint32_t kLsb4 = 0x01010101u;
+constexpr int kTileWords = 1024;    // words of one plane of a tile (4 per thread)
+constexpr int kMaxBitsTile = 256;   // replicas per tile (one counter each)
 
 // bits j of the 4 bytes of w (+1 -> 1, -1 -> 0), j = byte index
 __device__ __forceinline__ uint32_t pack4(uint32_t w) {
   const uint32_t plus = ~(w >> 1) & kLsb4;  // +1 = 0x01, -1 = 0xFF
   return (plus * 0x01020408u) >> 24;        // byte j's bit 0 to bit j
 }
-__device__ __forceinline__ uint32_t pack16(uint4 v) {
-  return pack4(v.x) | (pack4(v.y) << 4) | (pack4(v.z) << 8) | (pack4(v.w) << 12);
-}
 // 4 bits to 4 bytes: bit j set -> +1 (0x01), clear -> -1 (0xFF)
 __device__ __forceinline__ uint32_t unpack4(uint32_t n) {
   const uint32_t ones = (n * 0x00204081u) & kLsb4;
   return 0xFFFFFFFFu ^ (ones * 0xFEu);
 }
-__device__ __forceinline__ uint4 unpack16(uint32_t bits) {
-  return make_uint4(unpack4(bits & 0xFu), unpack4((bits >> 4) & 0xFu), unpack4((bits >> 8) & 0xFu),
-                    unpack4((bits >> 12) & 0xFu));
+// seg int8 spins at p (4-byte aligned) <-> bits 0..seg-1
+__device__ __forceinline__ uint32_t pack_seg(const uint8_t* p, int seg) {
+  uint32_t b = 0;
+  for (int i = 0; i < seg; i += 4) b |= pack4(*reinterpret_cast<const uint32_t*>(p + i)) << i;
+  return b;
+}
+__device__ __forceinline__ void unpack_seg(uint32_t b, uint8_t* p, int seg) {
+  for (int i = 0; i < seg; i += 4) *reinterpret_cast<uint32_t*>(p + i) = unpack4((b >> i) & 0xFu);
 }
 
-constexpr int kMaxBitsTile = 16;
+// Parameters of the population a CTA is sweeping (shared memory).
+struct BitsParams {
+  int L, N, h, S;          // lattice side, sites, sites per sublattice, sites per sublattice row
+  int Wq, seg, segs, wpp;  // words per row, sites per segment, segments per word, words per plane of a word group
+  int GW, G, R;            // word groups (of segs replicas) per tile, replicas per tile, replicas
+  uint32_t invWpp, invWq;  // ceil(2^32 / wpp), ceil(2^32 / Wq) (Wq > 1)
+  uint32_t M0, ML, V;      // first site of every segment, last site of every segment, all segment bits
+  int step, sweeps;
+  uint32_t tag, T4, T8;
+  uint8_t* spins;
+  int32_t* E;
+  int32_t* M;
+};
+
+// Row layout of L: Wq words of seg sites, segs = segments per word.
+__host__ __device__ inline bool bits_layout(int L, int* Wq, int* seg, int* segs) {
+  if (L < 8 || L % 8 != 0 || L > 256) return false;
+  const int S = L / 2;
+  for (int w = (S + 31) / 32; w <= 8; ++w)
+    if (S % w == 0 && (S / w) % 4 == 0) {
+      *Wq = w;
+      *seg = S / w;
+      *segs = w == 1 ? 32 / *seg : 1;
+      return true;
+    }
+  return false;
+}
+
+__device__ __forceinline__ uint32_t recip32_dev(uint32_t d) {
+  return (uint32_t)((0x100000000ull + d - 1) / d);
+}
+
+// word `it` of a plane of the tile -> word group g, word wr of the group,
+// row y, word c of the row
+__device__ __forceinline__ void bits_split(const BitsParams& P, int it, int& g, int& wr, int& y, int& c) {
+  g = (int)__umulhi((uint32_t)it, P.invWpp);
+  wr = it - g * P.wpp;
+  y = P.Wq == 1 ? wr : (int)__umulhi((uint32_t)wr, P.invWq);
+  c = wr - y * P.Wq;
+}
+
+// the other horizontal neighbour of the sites of word c of row `row` (word
+// offset) of plane o: sites i-1 (left) or i+1, periodic inside the row
+__device__ __forceinline__ uint32_t bits_side(const BitsParams& P, const uint32_t* o, int row, int c, uint32_t ctr,
+                                              bool left) {
+  const int Wq = P.Wq, seg = P.seg;
+  if (Wq == 1)
+    return left ? (((ctr << 1) & ~P.M0) | ((ctr >> (seg - 1)) & P.M0)) & P.V
+                : (((ctr >> 1) & ~P.ML) | ((ctr << (seg - 1)) & P.ML)) & P.V;
+  if (left) return ((ctr << 1) | (o[row + (c == 0 ? Wq - 1 : c - 1)] >> (seg - 1))) & P.V;
+  return (ctr >> 1) | ((o[row + (c + 1 == Wq ? 0 : c + 1)] & 1u) << (seg - 1));
+}
+
+// replicas of tile ti present, and the words of one plane they occupy
+__device__ __forceinline__ int bits_present(const BitsParams& P, int ti) { return min(P.G, P.R - ti * P.G); }
+__device__ __forceinline__ int bits_items(const BitsParams& P, int ti) {
+  return (bits_present(P, ti) + P.segs - 1) / P.segs * P.wpp;
+}
+
+// int8 replicas of tile ti -> bit planes (to_smem), or back
+__device__ __noinline__ void bits_move(const BitsParams& P, uint32_t* pl, int ti, bool to_smem) {
+  const int r0 = ti * P.G, gc = bits_present(P, ti), items = bits_items(P, ti);
+  for (int it = threadIdx.x; it < 2 * items; it += blockDim.x) {
+    const int X = it >= items ? 1 : 0;
+    int g, wr, y, c;
+    bits_split(P, it - X * items, g, wr, y, c);
+    uint32_t* word = pl + (X * P.GW + g) * P.wpp + wr;
+    uint32_t w = to_smem ? 0u : *word;
+    for (int j = 0; j < P.segs; ++j) {
+      const int rep = g * P.segs + j;
+      if (rep >= gc) break;
+      uint8_t* sp = P.spins + (size_t)(r0 + rep) * P.N + X * P.h + y * P.S + c * P.seg;
+      if (to_smem) w |= pack_seg(sp, P.seg) << (j * P.seg);
+      else unpack_seg(w >> (j * P.seg), sp, P.seg);
+    }
+    if (to_smem) *word = w;
+  }
+}
+
+// anti-parallel bonds (each seen from its A end) and +1 sites of every
+// replica of tile ti
+__device__ __noinline__ void bits_count(const BitsParams& P, const uint32_t* pl, int ti, int* s_anti, int* s_plus) {
+  const int gc = bits_present(P, ti), items = bits_items(P, ti), L = P.L, Wq = P.Wq;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int g, wr, y, c;
+    bits_split(P, it, g, wr, y, c);
+    const uint32_t* A = pl + g * P.wpp;
+    const uint32_t* B = pl + (P.GW + g) * P.wpp;
+    const uint32_t a = A[wr], ctr = B[wr];
+    const uint32_t up = B[(y == 0 ? L - 1 : y - 1) * Wq + c], dn = B[(y + 1 == L ? 0 : y + 1) * Wq + c];
+    const uint32_t side = bits_side(P, B, y * Wq, c, ctr, (y & 1) == 0);
+    const uint32_t x1 = a ^ ctr, x2 = a ^ side, x3 = a ^ up, x4 = a ^ dn;
+    if (P.segs == 1) {
+      atomicAdd(&s_anti[g], __popc(x1) + __popc(x2) + __popc(x3) + __popc(x4));
+      atomicAdd(&s_plus[g], __popc(a) + __popc(ctr));
+    } else {
+      const uint32_t m = (1u << P.seg) - 1u;  // seg <= 16 here
+      for (int j = 0; j < P.segs; ++j) {
+        const int rep = g * P.segs + j;
+        if (rep >= gc) break;
+        const uint32_t mj = m << (j * P.seg);
+        atomicAdd(&s_anti[rep], __popc(x1 & mj) + __popc(x2 & mj) + __popc(x3 & mj) + __popc(x4 & mj));
+        atomicAdd(&s_plus[rep], __popc(a & mj) + __popc(ctr & mj));
+      }
+    }
+  }
+}
 
 }  // namespace
 
-bool ssc_bits_geom(int L, SweepGeom* g) {
-  if (L != 64 && L != 128 && L != 256) return false;
+bool ssc_bits_geom(int L, SweepGeom* g, int tile, long long replicas, int slots) {
+  int Wq, seg, segs;
+  if (!bits_layout(L, &Wq, &seg, &segs)) return false;
+  const int wpp = L * Wq;
+  int GWmax = kTileWords / wpp;
+  if (GWmax < 1) GWmax = 1;
+  if (GWmax * segs > kMaxBitsTile) GWmax = kMaxBitsTile / segs;
+  int GW = GWmax;
+  if (tile > 0) {  // replicas per tile asked for: a power-of-two fraction of the largest tile
+    bool ok = false;
+    for (int w = GWmax; w >= 1 && !ok; w /= 2) ok = w * segs == tile;
+    if (!ok) return false;
+    GW = tile / segs;
+  } else if (replicas > 0 && slots > 0) {
+    // waves of tiles over the resident CTAs times the words a thread updates
+    // per half-sweep (threads with no word skip the acceptance); ties keep
+    // the larger tile
+    double best = 0;
+    for (int w = GWmax; w >= 1; w /= 2) {
+      const double tiles = std::ceil((double)replicas / (w * segs));
+      const double c = std::max(1.0, tiles / slots) * ((w * wpp + kSweepThreads - 1) / kSweepThreads);
+      if (w == GWmax || c < best - 1e-9) {
+        best = c;
+        GW = w;
+      }
+    }
+  }
   g->L = L;
   g->N = L * L;
   g->half = g->N / 2;
-  g->Wr = L / 64;                // words per sublattice row
-  const int wpp = L * g->Wr;     // words per sublattice plane
-  g->G = 1024 / wpp;             // replicas per tile: 1024 row words per half-sweep
+  g->Wr = Wq;
+  g->seg = seg;
+  g->G = GW * segs;  // replicas per tile
   g->T = kSweepThreads;
   g->rpp = 0;
-  g->npass = g->G * wpp / kSweepThreads;  // row words per thread per half-sweep (4)
+  g->npass = (GW * wpp + kSweepThreads - 1) / kSweepThreads;  // words per thread per half-sweep
   g->kconst = 0;
-  g->smem = g->G * 2 * wpp * 4;
-  return g->G >= 1 && g->G <= kMaxBitsTile;
+  g->smem = GW * 2 * wpp * 4;
+  return true;
+}
+
+double ssc_bits_fill(int L) {
+  int Wq, seg, segs;
+  if (!bits_layout(L, &Wq, &seg, &segs)) return 0.0;
+  return (double)(L / 2) * (Wq == 1 ? segs : 1) / (32.0 * Wq);
 }
 
 __global__ void __launch_bounds__(kSweepThreads, 4)
     ssc_sweep_bits_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
-  extern __shared__ __align__(16) uint32_t pl[];  // [X][g][y][c]: plane X of replica g, row y, word c
+  extern __shared__ __align__(16) uint32_t pl[];  // [X][word group][y][c]: plane X, row y, word c
   __shared__ int s_unit, s_pop;
   __shared__ uint2 s_dig[kMsb];
   __shared__ int s_anti[kMaxBitsTile], s_plus[kMaxBitsTile];
-  __shared__ UnitParams P;
-  __shared__ BitStats stats;  // lane g accumulates the replicas in slot g of its tiles
+  __shared__ BitsParams P;
+  __shared__ BitStats stats;  // lane k accumulates the replicas k, k+32, ... of its tiles
 
+  static_assert(kMaxBitsTile == kSweepThreads, "one counter per thread to clear");
   const int tid = threadIdx.x;
   const int total = b->unit_prefix[b->npop];
   const PhiloxKeys keys(stream_seed);
@@ -93,19 +242,31 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       s_unit = loc;
       if (p >= 0 && p != cur) {
         const PopDev* st = b->pops + p;
-        P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.Wr = st->Wr; P.G = st->gpt;
-        P.rg = st->R_cur;  // replicas
+        P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.S = st->L >> 1;
+        P.Wq = st->Wr; P.seg = st->seg; P.segs = P.Wq == 1 ? 32 / P.seg : 1;
+        P.wpp = P.L * P.Wq;
+        P.G = st->gpt;
+        P.GW = P.G / P.segs;
+        P.R = st->R_cur;
+        P.invWpp = recip32_dev((uint32_t)P.wpp);
+        P.invWq = P.Wq > 1 ? recip32_dev((uint32_t)P.Wq) : 0u;
+        uint32_t m0 = 0;
+        for (int j = 0; j < P.segs; ++j) m0 |= 1u << (j * P.seg);
+        P.M0 = m0;
+        P.ML = m0 << (P.seg - 1);
+        P.V = P.segs * P.seg == 32 ? 0xffffffffu : (1u << (P.segs * P.seg)) - 1u;
         P.step = st->step;
         P.sweeps = energy_only ? 0 : st->sweeps;
         P.tag = kTagSscSweep | (uint32_t)st->pop_id;
         P.T4 = st->thr[(size_t)st->step * kThrPerStep + 10];
         P.T8 = st->thr[(size_t)st->step * kThrPerStep + 11];
-        P.words = (uint32_t*)st->spins[st->parity];
+        P.spins = (uint8_t*)st->spins[st->parity];
         P.E = st->E;
         P.M = st->M;
       }
     }
-    if (tid < kMaxBitsTile) { s_anti[tid] = 0; s_plus[tid] = 0; }
+    s_anti[tid] = 0;
+    s_plus[tid] = 0;
     __syncthreads();
     const int p = s_pop, ti = s_unit;
     if (p < 0) break;
@@ -117,96 +278,81 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         s_dig[tid] = make_uint2(d8, d4 ^ d8);
       }
     }
-    const int L = P.L, N = P.N, h = P.h, Wq = P.Wr, G = P.G;
-    const int wpp = L * Wq, lwpp = 31 - __clz(wpp), lwq = 31 - __clz(Wq);
-    const int r0 = ti * G, gc = min(G, P.rg - r0);
-    const uint8_t* spins = (const uint8_t*)P.words;
-
-    // pack: one row word (32 bytes of int8 spins) per item
-    for (int it = tid; it < gc * 2 * wpp; it += blockDim.x) {
-      const int g = it >> (lwpp + 1), X = (it >> lwpp) & 1, w = it & (wpp - 1);
-      const uint4* src = (const uint4*)(spins + (size_t)(r0 + g) * N + (size_t)X * h + (size_t)w * 32);
-      pl[(X * G + g) * wpp + w] = pack16(src[0]) | (pack16(src[1]) << 16);
-    }
+    bits_move(P, pl, ti, true);
     __syncthreads();
 
-    const int items = gc * wpp;  // row words of one plane present in the tile
+    // one half-sweep over the words of plane `self`; kForm 0: one 32-site word
+    // per row (L = 64, rotations only), 1: any other layout
+    {
+    const int L = P.L, Wq = P.Wq, seg = P.seg, wpp = P.wpp, GW = P.GW, items = bits_items(P, ti);
+    auto half_sweep = [&](auto form_c, uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
+      constexpr int kForm = decltype(form_c)::value;
+#pragma unroll 1
+      for (int q0 = 0; q0 * kSweepThreads < items; q0 += kKB) {
+        uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+        uint32_t vm = 0;
+#pragma unroll
+        for (int k = 0; k < kKB; ++k) {
+          const int it = tid + (q0 + k) * kSweepThreads;
+          const bool valid = it < items;
+          const int itc = valid ? it : 0;
+          const int g = (int)__umulhi((uint32_t)itc, P.invWpp), wr = itc - g * wpp;
+          int y = wr, c = 0;
+          if (kForm == 1 && Wq > 1) {
+            y = (int)__umulhi((uint32_t)wr, P.invWq);
+            c = wr - y * Wq;
+          }
+          const int base = g * wpp;
+          const int rowu = (y == 0 ? L - 1 : y - 1) * Wq, rowd = (y + 1 == L ? 0 : y + 1) * Wq;
+          const uint32_t s = self[base + wr];
+          const uint32_t ctr = oth[base + wr], up = oth[base + rowu + c], dn = oth[base + rowd + c];
+          const bool left = (hf == 0) == ((y & 1) == 0);
+          const uint32_t side = kForm == 0 ? (left ? __funnelshift_l(ctr, ctr, 1) : __funnelshift_r(ctr, ctr, 1))
+                                           : bits_side(P, oth + base, y * Wq, c, ctr, left);
+          uint32_t s0, s1, s2;
+          adder4(s ^ ctr, s ^ side, s ^ up, s ^ dn, s0, s1, s2);
+          const uint32_t v = kForm == 0 ? 0xffffffffu : P.V;
+          av[k] = s0;
+          ac[k] = (s1 | s2) & v;
+          un[k] = valid ? ~(s1 | s2) & v : 0u;
+          vm |= valid ? 1u << k : 0u;
+          site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)wr;  // word number in the population
+        }
+        const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u + (uint32_t)(q0 / kKB);
+        // slots holding words lead (it grows with k): no Philox work for the rest
+        accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, __popc(vm));
+#pragma unroll
+        for (int k = 0; k < kKB; ++k)
+          if (vm >> k & 1u) self[site[k] - (uint32_t)(ti * GW) * (uint32_t)wpp] ^= ac[k];
+      }
+    };
+    const bool full_word = Wq == 1 && seg == 32;  // block-uniform
     const int sweeps = P.sweeps;
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
       for (int hf = 0; hf < 2; ++hf) {
-        uint32_t* self = pl + hf * G * wpp;
-        const uint32_t* oth = pl + (1 - hf) * G * wpp;
+        uint32_t* self = pl + hf * GW * wpp;
+        const uint32_t* oth = pl + (1 - hf) * GW * wpp;
         const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
-#pragma unroll 1
-        for (int q0 = 0; q0 * kSweepThreads < G * wpp; q0 += kKB) {
-          uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
-          uint32_t vm = 0;
-#pragma unroll
-          for (int k = 0; k < kKB; ++k) {
-            const int it = tid + (q0 + k) * kSweepThreads;
-            const bool valid = it < items;
-            const int itc = valid ? it : 0;
-            const int g = itc >> lwpp, wr = itc & (wpp - 1), y = wr >> lwq, c = wr & (Wq - 1);
-            const int base = g * wpp, row = y * Wq;
-            const int rowu = (y == 0 ? L - 1 : y - 1) * Wq, rowd = (y + 1 == L ? 0 : y + 1) * Wq;
-            const uint32_t s = self[base + wr];
-            const uint32_t ctr = oth[base + wr], up = oth[base + rowu + c], dn = oth[base + rowd + c];
-            // the other horizontal neighbour: site i-1 or i+1 of the same row
-            const bool left = (hf == 0) == ((y & 1) == 0);
-            uint32_t side;
-            if (left) side = __funnelshift_l(oth[base + row + (c == 0 ? Wq - 1 : c - 1)], ctr, 1);
-            else side = __funnelshift_r(ctr, oth[base + row + (c + 1 == Wq ? 0 : c + 1)], 1);
-            uint32_t s0, s1, s2;
-            adder4(s ^ ctr, s ^ side, s ^ up, s ^ dn, s0, s1, s2);
-            av[k] = s0;
-            ac[k] = s1 | s2;
-            un[k] = valid ? ~(s1 | s2) : 0u;
-            vm |= valid ? 1u << k : 0u;
-            site[k] = (uint32_t)(r0 + g) * (uint32_t)wpp + (uint32_t)wr;
-          }
-          const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u + (uint32_t)(q0 / kKB);
-          accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, kKB);
-#pragma unroll
-          for (int k = 0; k < kKB; ++k)
-            if (vm >> k & 1u) {
-              const int it = tid + (q0 + k) * kSweepThreads;
-              self[(it >> lwpp) * wpp + (it & (wpp - 1))] ^= ac[k];
-            }
-        }
+        if (full_word) half_sweep(std::integral_constant<int, 0>(), self, oth, hf, c1);
+        else half_sweep(std::integral_constant<int, 1>(), self, oth, hf, c1);
         __syncthreads();
       }
     }
 
-    // energy (every bond seen once from its A end: E = -2N + 2 #anti-parallel)
-    // and magnetisation (M = 2 #plus - N) of each replica of the tile
-    for (int it = tid; it < items; it += blockDim.x) {
-      const int g = it >> lwpp, wr = it & (wpp - 1), y = wr >> lwq, c = wr & (Wq - 1);
-      const int base = g * wpp, row = y * Wq;
-      const uint32_t* A = pl;
-      const uint32_t* B = pl + G * wpp;
-      const uint32_t a = A[base + wr], ctr = B[base + wr];
-      const uint32_t up = B[base + (y == 0 ? L - 1 : y - 1) * Wq + c], dn = B[base + (y + 1 == L ? 0 : y + 1) * Wq + c];
-      const uint32_t side = (y & 1) == 0 ? __funnelshift_l(B[base + row + (c == 0 ? Wq - 1 : c - 1)], ctr, 1)
-                                         : __funnelshift_r(ctr, B[base + row + (c + 1 == Wq ? 0 : c + 1)], 1);
-      atomicAdd(&s_anti[g], __popc(a ^ ctr) + __popc(a ^ side) + __popc(a ^ up) + __popc(a ^ dn));
-      atomicAdd(&s_plus[g], __popc(a) + __popc(ctr));
     }
-    // unpack and write the tile back
-    uint8_t* dst = (uint8_t*)P.words;
-    for (int it = tid; it < gc * 2 * wpp; it += blockDim.x) {
-      const int g = it >> (lwpp + 1), X = (it >> lwpp) & 1, w = it & (wpp - 1);
-      const uint32_t bits = pl[(X * G + g) * wpp + w];
-      uint4* o = (uint4*)(dst + (size_t)(r0 + g) * N + (size_t)X * h + (size_t)w * 32);
-      o[0] = unpack16(bits & 0xFFFFu);
-      o[1] = unpack16(bits >> 16);
-    }
+
+    bits_count(P, pl, ti, s_anti, s_plus);
+    bits_move(P, pl, ti, false);
     __syncthreads();
-    if (tid < gc) {
-      const int E = -2 * N + 2 * s_anti[tid], Mg = 2 * s_plus[tid] - N;
-      P.E[r0 + tid] = E;
-      P.M[r0 + tid] = Mg;
-      stats.add(tid, E, Mg);
+    {
+      const int r0 = ti * P.G, gc = bits_present(P, ti), N = P.N;
+      for (int j = tid; j < gc; j += blockDim.x) {
+        P.E[r0 + j] = -2 * N + 2 * s_anti[j];
+        P.M[r0 + j] = 2 * s_plus[j] - N;
+      }
+      if (tid < kMsb)
+        for (int j = tid; j < gc; j += kMsb) stats.add(tid, -2 * N + 2 * s_anti[j], 2 * s_plus[j] - N);
     }
   }
   if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);

@@ -90,13 +90,14 @@ int finish(cudaError_t e, cudaStream_t s, const char* what) {
   return e == cudaSuccess ? PA_OK : stage_fail(e, what);
 }
 
+// bits: the SSC bit-plane sweep (native stream only)
 int sweep_stage(int coding, void* spins, uint8_t* active, int L, int units, int sweeps, double beta, int rng_mode,
-                uint64_t seed, uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream) {
+                uint64_t seed, uint64_t iseq, int step, int32_t* E, int32_t* M, void* stream, bool bits = false) {
   cudaStream_t s = (cudaStream_t)stream;
   SweepGeom g;
-  if (coding == kMSC ? !msc_geom(L, &g) : !ssc_geom(L, &g)) return PA_ERR_ARG;
+  if (bits ? !ssc_bits_geom(L, &g) : coding == kMSC ? !msc_geom(L, &g) : !ssc_geom(L, &g)) return PA_ERR_ARG;
   SweepLaunch sl;
-  cudaError_t e = sweep_setup(coding, rng_mode, g.smem, &sl);
+  cudaError_t e = bits ? ssc_bits_setup(g.smem, &sl) : sweep_setup(coding, rng_mode, g.smem, &sl);
   if (e != cudaSuccess) return stage_fail(e, "sweep setup");
   Scratch S;
   if ((e = S.alloc()) != cudaSuccess) return stage_fail(e, "scratch");
@@ -117,10 +118,12 @@ int sweep_stage(int coding, void* spins, uint8_t* active, int L, int units, int 
   uint32_t t[2 * kThrPerStep];
   fill_thr(0.0, t);
   fill_thr(beta, t + kThrPerStep);
+  if (bits) geom_to_pop(g, &h);
   int rc = upload(S, h, b, t, s);
   if (rc) return rc;
   e = launch_plan(S.b, 1, 0, s);
-  if (e == cudaSuccess) e = launch_sweep(S.b, coding, rng_mode, 0, seed, sl, s);
+  if (e == cudaSuccess)
+    e = bits ? launch_ssc_bits_sweep(S.b, 0, seed, sl, s) : launch_sweep(S.b, coding, rng_mode, 0, seed, sl, s);
   return finish(e, s, "sweep");
 }
 
@@ -151,6 +154,13 @@ int pa_ssc_sweep(int8_t* spins, int L, int R, int sweeps, double beta, int rng_m
   if (!spins || !E || !M || R < 1 || sweeps < 0 || step < 0 || !ssc_geom(L, &g)) return PA_ERR_ARG;
   if (rng_mode != PA_RNG_NATIVE && rng_mode != PA_RNG_REFERENCE) return PA_ERR_ARG;
   return sweep_stage(kSSC, spins, nullptr, L, R, sweeps, beta, rng_mode, seed, iseq, step, E, M, stream);
+}
+
+int pa_ssc_sweep_bits(int8_t* spins, int L, int R, int sweeps, double beta, uint64_t seed, int step, int32_t* E,
+                      int32_t* M, void* stream) {
+  SweepGeom g;
+  if (!spins || !E || !M || R < 1 || sweeps < 0 || step < 0 || !ssc_bits_geom(L, &g)) return PA_ERR_ARG;
+  return sweep_stage(kSSC, spins, nullptr, L, R, sweeps, beta, PA_RNG_NATIVE, seed, 0, step, E, M, stream, true);
 }
 
 int pa_msc_init(uint32_t* words, uint8_t* active, int L, int R, uint64_t seed, uint64_t iseq, void* stream) {

@@ -26,7 +26,8 @@ constexpr int kSweepThreads = 256;
 
 struct PopDev {
   // ------------------------------------------------ configuration (constant)
-  int L, N, coding, Rinit, Rcap, rgcap, sweeps, rng_mode, weights, pop_id, nsteps, pad0;
+  int L, N, coding, Rinit, Rcap, rgcap, sweeps, rng_mode, weights, pop_id, nsteps;
+  int seg;  // SSC bit-plane sweep: sites per word segment (SweepGeom::seg)
   // sweep thread layout (see SweepGeom): words per row, rows per pass,
   // worker threads, passes, reference draws per thread per half sweep,
   // MSC groups per work unit (tile), and the reciprocals of L and Wr used

@@ -12,7 +12,7 @@ import torch
 
 from . import SSC, MSC, PaisingError, lib
 
-__all__ = ["ssc_init", "ssc_sweep", "msc_init", "msc_sweep", "resample_plan", "ssc_resample", "msc_resample"]
+__all__ = ["ssc_init", "ssc_sweep", "ssc_sweep_bits", "msc_init", "msc_sweep", "resample_plan", "ssc_resample", "msc_resample"]
 
 
 def _ptr(t: torch.Tensor | None):
@@ -46,6 +46,16 @@ def ssc_sweep(spins: torch.Tensor, L: int, sweeps: int, beta: float, rng: int, s
     E = torch.empty(R, dtype=torch.int32, device=spins.device)
     M = torch.empty(R, dtype=torch.int32, device=spins.device)
     _check(lib().pa_ssc_sweep(_ptr(spins), L, R, sweeps, beta, rng, seed, iseq, step, _ptr(E), _ptr(M), _stream()))
+    return E, M
+
+
+def ssc_sweep_bits(spins: torch.Tensor, L: int, sweeps: int, beta: float, seed: int, step: int = 1):
+    """The bit-plane sweep (native stream) in place on spins [R, N] int8;
+    returns (E, M) int32 tensors."""
+    R = spins.shape[0]
+    E = torch.empty(R, dtype=torch.int32, device=spins.device)
+    M = torch.empty(R, dtype=torch.int32, device=spins.device)
+    _check(lib().pa_ssc_sweep_bits(_ptr(spins), L, R, sweeps, beta, seed, step, _ptr(E), _ptr(M), _stream()))
     return E, M
 
 

@@ -42,6 +42,13 @@ def cuda():
     return torch
 
 
+@pytest.fixture(scope="module")
+def st(cuda):
+    """The stage-level entry points (paising_gb300.stages)."""
+    from paising_gb300 import stages
+    return stages
+
+
 def compare_rows(got: np.ndarray, ref: np.ndarray, rtol: float = 1e-9, exact_R: bool = True):
     """Rows of a results file: the population size column exactly, the rest to
     rtol (relative, with an absolute floor for values that are ~0)."""

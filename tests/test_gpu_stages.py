@@ -9,12 +9,6 @@ import paising_gb300 as pa
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def st(cuda):
-    from paising_gb300 import stages
-    return stages
-
-
 def msc_words_np(t):
     return t.cpu().numpy().view(np.uint32)
 

@@ -64,7 +64,9 @@ def test_tiles_native_free_energy_vs_kaufman_L16(cuda, oracle, tile):
 
 def test_tiles_rejected_where_invalid(cuda):
     for kw in (dict(L=10, tile_groups=2), dict(L=128, tile_groups=2), dict(L=64, tile_groups=3),
-               dict(L=64, coding="ssc", tile_groups=2)):
+               dict(L=64, coding="ssc", tile_groups=3), dict(L=64, coding="ssc", tile_groups=32),
+               dict(L=64, coding="ssc", tile_groups=2, rng="reference"),
+               dict(L=64, coding="ssc", tile_groups=2, sweep_variant=1), dict(L=104, coding="ssc", tile_groups=1)):
         with pytest.raises(pa.PaisingError):
             pa.Engine(**{"coding": "msc", "R": 1000, **kw})
 
@@ -98,38 +100,54 @@ def test_autotune_batch(cuda, oracle):
 
 def test_autotune_ssc_spins_per_word(cuda):
     """SSC with the native stream at L in {64, 128}: the autotuner times the
-    int8 sweep (4 sites per word) against the bit-plane sweep (32 sites per
-    word) on the batch and keeps the faster.  At these sizes (1250 bit-plane
-    tiles) that is the bit-plane sweep, 4-5x faster, which the engine also uses
-    untuned: the tuned run equals the untuned one bit for bit."""
+    bit-plane tile sizes of every lattice size, then the int8 sweep (4 sites
+    per word) against the bit-plane sweep (32 sites per word) on the batch,
+    and keeps the faster -- at these sizes the bit planes, 4-5x faster.  The
+    run equals an untuned run configured with the same tiles bit for bit."""
     pops = [dict(L=64, R=20000, sweeps=2, dbeta=0.25, seed=21), dict(L=128, R=5000, sweeps=2, dbeta=0.25, seed=22)]
 
-    def go(tune, **kw):
-        with pa.Engine.batch([dict(p, **kw) for p in pops], coding="ssc") as e:
+    def go(tune, per_pop=None, **kw):
+        cfg = [dict(p, **kw, **(per_pop[k] if per_pop else {})) for k, p in enumerate(pops)]
+        with pa.Engine.batch(cfg, coding="ssc") as e:
             tiles = e.autotune() if tune else None
             forms = [e.sweep_form(k) for k in range(len(pops))]
             e.run()
             return tiles, forms, [e.rows(k) for k in range(len(pops))]
 
     tiles, forms, tuned = go(True)
-    assert tiles == [16, 4]  # replicas per 1024-word tile
+    assert tiles[0] in (16, 8, 4, 2, 1) and tiles[1] in (4, 2, 1)  # power-of-two fractions of the largest tile
     assert all(f["spins_per_word"] == 32 and f["replicas_per_word"] == 1 and f["cluster_ctas"] == 1 for f in forms)
-    _, _, plain = go(False)
-    for a, b in zip(tuned, plain):
+    assert [f["tile"] for f in forms] == tiles
+    _, forms_c, fixed = go(False, per_pop=[dict(tile_groups=t) for t in tiles])
+    assert [f["tile"] for f in forms_c] == tiles
+    for a, b in zip(tuned, fixed):
         assert np.array_equal(a, b)
     # the other form draws another native stream (its physics is checked
     # against the exact solution in the SSC tests)
     _, forms8, int8 = go(False, sweep_variant=1)
     assert forms8[0]["spins_per_word"] == 4
-    assert not np.array_equal(int8[0], plain[0])
+    assert not np.array_equal(int8[0], fixed[0])
+
+
+def test_ssc_tiles_need_bit_planes_everywhere(cuda):
+    """An SSC batch asking for a bit-plane tile runs wholly on bit planes, so
+    every lattice size needs a layout (L=104 has none)."""
+    with pytest.raises(pa.PaisingError):
+        pa.Engine.batch([dict(L=64, R=100, tile_groups=4), dict(L=104, R=100)], coding="ssc")
+    with pa.Engine.batch([dict(L=64, R=100, tile_groups=4), dict(L=40, R=100)], coding="ssc") as e:
+        assert e.sweep_form(0)["tile"] == 4 and e.sweep_form(1)["spins_per_word"] == 32  # L=40: 20-site words
 
 
 def test_sweep_form_reports(cuda):
-    """pa_sweep_form: SSC int8 where bit planes do not apply (L=32, or the
+    """pa_sweep_form: SSC int8 where bit planes do not apply (L=104, or the
     reference stream), MSC 32 replicas per word with its tile and cluster."""
-    with pa.Engine(L=32, R=100, coding="ssc") as e:
-        e.autotune()  # nothing to choose: L=32 has no bit-plane form
+    with pa.Engine(L=104, R=100, coding="ssc") as e:
+        e.autotune()  # nothing to choose: 52-site rows have no bit-plane layout
         assert e.sweep_form() == dict(spins_per_word=4, replicas_per_word=1, tile=1, cluster_ctas=1)
+    with pa.Engine(L=16, R=100, coding="ssc", tile_groups=256) as e:  # 4 replicas' 8-site rows per word
+        assert e.sweep_form() == dict(spins_per_word=32, replicas_per_word=1, tile=256, cluster_ctas=1)
+    with pa.Engine(L=16, R=100, coding="ssc") as e:  # the cost model: smaller tiles for few replicas
+        assert e.sweep_form()["tile"] in (128, 64, 32, 16, 8, 4)
     with pa.Engine(L=64, R=100, coding="ssc", rng="reference") as e:
         assert e.sweep_form()["spins_per_word"] == 4
     with pa.Engine(L=16, R=1000, coding="msc", tile_groups=4) as e:
