@@ -71,6 +71,69 @@ __global__ void msc_init_kernel(PopDev* pops) {
 //   (accept_native); each replica's acceptance probability is exactly
 //   T/2^32, as in the reference.  The stream is keyed by stream_seed (one
 //   per batch; populations differ in counter word 3).
+// Tile gi0 (gc groups present) <-> HBM: group gi0+g's sublattice X goes to
+// lat + X*G*h + g*h (for G = 1 simply the group's N words; G > 1 implies
+// h % 4 == 0).  Out of line: keeps the sweep loop's registers free.
+__device__ __noinline__ void msc_move_tile(const UnitParams& P, uint32_t* lat, int gi0, int gc, bool to_smem) {
+  const int N = P.N, h = P.h, G = P.G;
+  uint4* lat4 = (uint4*)lat;
+  uint4* g4 = (uint4*)(P.words + (size_t)gi0 * N);
+  if (G == 1) {
+    for (int v = threadIdx.x; v < (N >> 2); v += blockDim.x) {
+      if (to_smem) lat4[v] = g4[v];
+      else g4[v] = lat4[v];
+    }
+    return;
+  }
+  const int h4 = h >> 2, n4 = N >> 2;
+  for (int v = threadIdx.x; v < 2 * gc * h4; v += blockDim.x) {
+    const int X = v >= gc * h4 ? 1 : 0, r = v - X * gc * h4;
+    const int g = (int)__umulhi((uint32_t)r, P.invH4), i = r - g * h4;
+    uint4* s = lat4 + X * G * h4 + g * h4 + i;
+    uint4* d = g4 + (size_t)g * n4 + X * h4 + i;
+    if (to_smem) *s = *d;
+    else *d = *s;
+  }
+}
+
+// Energy and magnetisation per replica bit of the tile: the left and up
+// bond of every A and B site (PAisingMSC.cu:272-294), counted per bit with
+// warp ballots into cntE / cntM [group of the tile][bit].  Each warp works
+// inside one group (kSweepThreads/32/G warps per group), so a ballot never
+// mixes groups.
+__device__ __noinline__ void msc_count(const UnitParams& P, const uint32_t* lat, int gc, int* cntE, int* cntM) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int L = P.L, Wr = P.Wr, h = P.h, G = P.G, wpg = (kSweepThreads / 32) / G;
+  const int w = tid >> 5, g = w / wpg, ws = w - g * wpg;
+  int cE = 0, cM = 0;  // lane k accumulates bit k
+  if (g >= gc) return;  // warp-uniform
+  const uint32_t* A = lat + g * h;
+  const uint32_t* B = lat + G * h + g * h;
+  for (int j0 = ws * 32; j0 < h; j0 += wpg * 32) {
+    const int j = j0 + lane;
+    uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
+    if (j < h) {
+      const int y = (int)__umulhi((uint32_t)j, P.invWr), x = j - y * Wr;
+      const int iL = y * Wr + (x == 0 ? Wr - 1 : x - 1), iU = (y + 1 == L ? 0 : y + 1) * Wr + x;
+      sA = A[j];
+      sB = B[j];
+      uint32_t Ai2, Bi2;
+      if (y & 1) { Ai2 = sB; Bi2 = A[iL]; }
+      else { Ai2 = B[iL]; Bi2 = sA; }
+      adder4(sA ^ Ai2, sA ^ B[iU], sB ^ Bi2, sB ^ A[iU], s0, s1, s2);
+    }
+#pragma unroll 4
+    for (int k = 0; k < kMsb; ++k) {
+      const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
+                    4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
+      const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
+      if (lane == k) { cE += e; cM += m; }
+    }
+  }
+  atomicAdd(&cntE[g * kMsb + lane], cE);
+  atomicAdd(&cntM[g * kMsb + lane], cM);
+}
+
 static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the tile, bit) in the epilogue");
 template <int MODE>
 __global__ void __launch_bounds__(kSweepThreads, 4)
@@ -144,30 +207,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
     }
     const int N = P.N, h = P.h, G = P.G, gi0 = ti * G;
     const int gc = min(G, P.rg - gi0);  // groups present in this tile
-    uint32_t* words = P.words;
-    // tile <-> HBM: group gi0+g's sublattice X goes to lat + X*G*h + g*h
-    // (for G = 1 simply the group's N words; G > 1 implies h % 4 == 0)
-    auto move_tile = [&](bool to_smem) {
-      uint4* lat4 = (uint4*)lat;
-      uint4* g4 = (uint4*)(words + (size_t)gi0 * N);
-      if (G == 1) {
-        for (int v = tid; v < (N >> 2); v += blockDim.x) {
-          if (to_smem) lat4[v] = g4[v];
-          else g4[v] = lat4[v];
-        }
-        return;
-      }
-      const int h4 = h >> 2, n4 = N >> 2;
-      for (int v = tid; v < 2 * gc * h4; v += blockDim.x) {
-        const int X = v >= gc * h4 ? 1 : 0, r = v - X * gc * h4;
-        const int g = (int)__umulhi((uint32_t)r, P.invH4), i = r - g * h4;
-        uint4* s = lat4 + X * G * h4 + g * h4 + i;
-        uint4* d = g4 + (size_t)g * n4 + X * h4 + i;
-        if (to_smem) *s = *d;
-        else *d = *s;
-      }
-    };
-    move_tile(true);
+    msc_move_tile(P, lat, gi0, gc, true);
     __syncthreads();
 
     // stacked row v of the tile -> group g, row y in the group, smem offsets
@@ -281,44 +321,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       }
     }
 
-    // energy and magnetisation per replica bit: the left and up bond of every
-    // A and B site (PAisingMSC.cu:272-294), counted per bit with warp ballots.
-    // Each warp works inside one group (kSweepThreads/32/G warps per group),
-    // so a ballot never mixes groups.
-    {
-      const int L = P.L, Wr = P.Wr, wpg = (kSweepThreads / 32) / G;
-      const int w = tid >> 5, g = w / wpg, ws = w - g * wpg;
-      int cE = 0, cM = 0;  // lane k accumulates bit k
-      if (g < gc) {        // warp-uniform
-        const uint32_t* A = lat + g * h;
-        const uint32_t* B = lat + G * h + g * h;
-        for (int j0 = ws * 32; j0 < h; j0 += wpg * 32) {
-          const int j = j0 + lane;
-          uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
-          if (j < h) {
-            const int y = (int)__umulhi((uint32_t)j, P.invWr), x = j - y * Wr;
-            const int iL = y * Wr + (x == 0 ? Wr - 1 : x - 1), iU = (y + 1 == L ? 0 : y + 1) * Wr + x;
-            sA = A[j];
-            sB = B[j];
-            uint32_t Ai2, Bi2;
-            if (y & 1) { Ai2 = sB; Bi2 = A[iL]; }
-            else { Ai2 = B[iL]; Bi2 = sA; }
-            adder4(sA ^ Ai2, sA ^ B[iU], sB ^ Bi2, sB ^ A[iU], s0, s1, s2);
-          }
-#pragma unroll 4
-          for (int k = 0; k < kMsb; ++k) {
-            const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) +
-                          2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
-                          4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
-            const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
-            if (lane == k) { cE += e; cM += m; }
-          }
-        }
-        atomicAdd(&s_cntE[g * kMsb + lane], cE);
-        atomicAdd(&s_cntM[g * kMsb + lane], cM);
-      }
-    }
-    move_tile(false);
+    msc_count(P, lat, gc, s_cntE, s_cntM);
+    msc_move_tile(P, lat, gi0, gc, false);
     __syncthreads();
     if (tid < gc * kMsb) {
       const int gi = gi0 + (tid >> 5);
