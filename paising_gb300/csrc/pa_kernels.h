@@ -85,9 +85,10 @@ cudaError_t launch_msc_resample(BatchDev* b, cudaStream_t s);
 // packed to one bit per site in shared memory, a sublattice row as Wr words
 // of `seg` sites (several replicas' rows per word when a row is at most 16
 // sites).  False where L has no such layout.  Replicas per tile: `tile` if
-// given (a power-of-two fraction of the largest tile, else false), else by a
-// cost model from the batch's replicas and resident CTAs (`slots`), else the
-// largest tile (about 1024 words per plane).
+// given (the largest tile for L halved k times, else false), else the
+// largest such tile that still leaves a tile for each of `slots` resident
+// CTAs given the batch's replicas, else the largest tile (about 1024 words
+// per plane).
 bool ssc_bits_geom(int L, SweepGeom* g, int tile = 0, long long replicas = 0, int slots = 0);
 // Fraction of the bits of the packed words that hold sites (1 at L = 16, 32,
 // 64, 128, 256; 0.75 at L = 24, 48, 96; 0 where no bit-plane layout exists).

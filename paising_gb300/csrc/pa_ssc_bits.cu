@@ -22,8 +22,6 @@
 //
 // Work per tile and half-sweep: about 1024 words, four per thread, decided
 // together (kKB = 4).
-#include <algorithm>
-#include <cmath>
 #include <type_traits>
 
 #include "pa_kernels.h"
@@ -183,18 +181,18 @@ bool ssc_bits_geom(int L, SweepGeom* g, int tile, long long replicas, int slots)
     if (!ok) return false;
     GW = tile / segs;
   } else if (replicas > 0 && slots > 0) {
-    // waves of tiles over the resident CTAs times the words a thread updates
-    // per half-sweep (threads with no word skip the acceptance); ties keep
-    // the larger tile
-    double best = 0;
-    for (int w = GWmax; w >= 1; w /= 2) {
-      const double tiles = std::ceil((double)replicas / (w * segs));
-      const double c = std::max(1.0, tiles / slots) * ((w * wpp + kSweepThreads - 1) / kSweepThreads);
-      if (w == GWmax || c < best - 1e-9) {
-        best = c;
+    // the largest tile that still leaves a tile for every resident CTA:
+    // smaller tiles give a thread fewer than four words and so lose the
+    // acceptance's sharing of undecided bits across them (at a full GPU L=64
+    // tiles of 8 replicas ran 1.7x slower than 16); fewer tiles than CTAs
+    // leave SMs idle (one L=16 population of 20000: 256 replicas per tile
+    // 370 attempts/ns, 32 per tile 503)
+    GW = 1;
+    for (int w = GWmax; w >= 1; w /= 2)
+      if ((replicas + (long long)w * segs - 1) / ((long long)w * segs) >= slots) {
         GW = w;
+        break;
       }
-    }
   }
   g->L = L;
   g->N = L * L;

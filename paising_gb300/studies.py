@@ -1,7 +1,7 @@
 """Reproducible studies on the GPU engine (run on a CUDA host):
 
     python -m paising_gb300.studies precision   [--out FILE]
-    python -m paising_gb300.studies batch       [--out FILE]
+    python -m paising_gb300.studies batch       [--coding msc|ssc] [--out FILE]
     python -m paising_gb300.studies large       [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
@@ -12,7 +12,8 @@ precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     evaluated inside this module.
 batch: 64 populations with L drawn from {16,32,48,64,96,128}, R uniform in
     [1000, 20000], dbeta from {0.0025, 0.005, 0.01}, beta_final 1, 20 sweeps
-    (seed 2026), annealed as one batch and as 64 sequential plain runs.
+    (seed 2026), annealed as one batch and as 64 sequential plain runs, MSC
+    or SSC (native stream: bit planes at every one of these sizes).
 """
 from __future__ import annotations
 
@@ -112,13 +113,13 @@ def precision(seed: int = 31) -> dict:
     return out
 
 
-def batch(seed: int = 2026) -> dict:
+def batch(seed: int = 2026, coding: str = "msc") -> dict:
     rng = np.random.default_rng(seed)
     pops = [dict(L=int(rng.choice([16, 32, 48, 64, 96, 128])), R=int(rng.integers(1000, 20001)),
                  dbeta=float(rng.choice([0.0025, 0.005, 0.01])), sweeps=20, seed=seed + k) for k in range(64)]
-    res = {"populations": pops}
+    res = {"coding": coding, "populations": pops}
     for form, tune in (("batched", True), ("batched_model_tiles", False)):
-        with pa.Engine.batch(pops, coding="msc") as e:
+        with pa.Engine.batch(pops, coding=coding) as e:
             t0 = time.perf_counter()
             tiles = e.autotune() if tune else None
             tune_s = time.perf_counter() - t0
@@ -127,14 +128,16 @@ def batch(seed: int = 2026) -> dict:
             e.run()
             wall = time.perf_counter() - t0
             ms, att = e.timing()
-        res[form] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6)}
+            spw = e.sweep_form(0)["spins_per_word"]
+        res[form] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6),
+                     "spins_per_word": spw}
         if tune:
             res[form]["autotune_s"] = tune_s
             res[form]["tiles_by_L"] = {str(p["L"]): t for p, t in zip(pops, tiles)}
     tot_ms = tot_att = 0.0
     t0 = time.perf_counter()
     for p in pops:
-        with pa.Engine(coding="msc", **p) as e:
+        with pa.Engine(coding=coding, **p) as e:
             e.run()
             m, a = e.timing()
             tot_ms += m
@@ -175,8 +178,9 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("study", choices=["precision", "batch", "large"])
     ap.add_argument("--out", default=None)
+    ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
-    r = {"precision": precision, "batch": batch, "large": large}[a.study]()
+    r = batch(coding=a.coding) if a.study == "batch" else {"precision": precision, "large": large}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0
