@@ -25,6 +25,63 @@ namespace pa {
 
 using namespace msc;
 
+// This CTA's stripe (rows row0 .. row0+LR-1) of both sublattices of group
+// gi <-> shared memory, below a halo row of Wr words each (stripe X at
+// lat + X*SH + Wr).  Out of line: keeps the sweep loop's registers free.
+__device__ __noinline__ void cluster_move_stripe(const UnitParams& P, uint32_t* lat, int gi, int row0, int LR, int SH,
+                                                 bool to_smem) {
+  const int Wr = P.Wr, SW = LR * Wr;
+  uint4* ga = (uint4*)(P.words + (size_t)gi * P.N + (size_t)row0 * Wr);
+  uint4* gb = (uint4*)(P.words + (size_t)gi * P.N + P.h + (size_t)row0 * Wr);
+  uint4* la = (uint4*)(lat + Wr);
+  uint4* lb = (uint4*)(lat + SH + Wr);
+  for (int v = threadIdx.x; v < (SW >> 2); v += blockDim.x) {
+    if (to_smem) {
+      la[v] = ga[v];
+      lb[v] = gb[v];
+    } else {
+      ga[v] = la[v];
+      gb[v] = lb[v];
+    }
+  }
+}
+
+// Energy and magnetisation counts of this stripe per replica bit: left and
+// up bond of every A and B site (PAisingMSC.cu:272-294), the up neighbours
+// of the last row taken from the lower halos; lane k of every warp adds bit
+// k's counts to cntE / cntM.
+__device__ __noinline__ void cluster_count(const UnitParams& P, const uint32_t* lat, int row0, int LR, int SH, int tx,
+                                           int txl, int rsub, bool worker, int* cntE, int* cntM) {
+  const int Wr = P.Wr, rpp = P.rpp, npass = P.npass, lane = threadIdx.x & 31;
+  const uint32_t* A = lat + Wr;
+  const uint32_t* Bs = lat + SH + Wr;
+  int cE = 0, cM = 0;
+  for (int pass = 0; pass < npass; ++pass) {
+    const int lr = rsub + pass * rpp;
+    const bool valid = worker && lr < LR;
+    uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
+    if (valid) {
+      const int ty = row0 + lr, row = lr * Wr;
+      sA = A[row + tx];
+      sB = Bs[row + tx];
+      uint32_t Ai2, Bi2;
+      if (ty & 1) { Ai2 = sB; Bi2 = A[row + txl]; }
+      else { Ai2 = Bs[row + txl]; Bi2 = sA; }
+      const uint32_t Ai4 = Bs[row + Wr + tx], Bi4 = A[row + Wr + tx];
+      adder4(sA ^ Ai2, sA ^ Ai4, sB ^ Bi2, sB ^ Bi4, s0, s1, s2);
+    }
+#pragma unroll 4
+    for (int k = 0; k < kMsb; ++k) {
+      const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
+                    4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
+      const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
+      if (lane == k) { cE += e; cM += m; }
+    }
+  }
+  atomicAdd(&cntE[lane], cE);
+  atomicAdd(&cntM[lane], cM);
+}
+
 template <int MODE, int CS, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
     msc_sweep_cluster_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
@@ -38,7 +95,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int prev = (rank + CS - 1) % CS, next = (rank + 1) % CS;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x;
   const int total = b->unit_prefix[b->npop];
   const PhiloxKeys keys(stream_seed);
   int cur = -1;
@@ -97,17 +154,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
     // stripe of a sublattice in shared memory: halo row, LR rows, halo row
     const int h = P.h, Wr = P.Wr, L = P.L, LR = L / CS, SW = LR * Wr, SH = SW + 2 * Wr;
     const int row0 = rank * LR;
-    uint32_t* words = P.words;
-    {  // load this CTA's stripe of both sublattices
-      const uint4* ga = (const uint4*)(words + (size_t)gi * P.N + (size_t)row0 * Wr);
-      const uint4* gb = (const uint4*)(words + (size_t)gi * P.N + h + (size_t)row0 * Wr);
-      uint4* la = (uint4*)(lat + Wr);
-      uint4* lb = (uint4*)(lat + SH + Wr);
-      for (int v = tid; v < (SW >> 2); v += blockDim.x) {
-        la[v] = ga[v];
-        lb[v] = gb[v];
-      }
-    }
+    cluster_move_stripe(P, lat, gi, row0, LR, SH, true);
     cluster.sync();
     // halo rows of sublattice X (0: A, 1: B): the last row of the previous
     // stripe and the first row of the next one
@@ -200,46 +247,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
     fetch_halo(0);
     fetch_halo(1);
     __syncthreads();
-    int cE = 0, cM = 0;
-    {
-      const uint32_t* A = lat + Wr;
-      const uint32_t* Bs = lat + SH + Wr;
-      const int rpp = P.rpp, npass = P.npass;
-      for (int pass = 0; pass < npass; ++pass) {
-        const int lr = rsub + pass * rpp;
-        const bool valid = worker && lr < LR;
-        uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
-        if (valid) {
-          const int ty = row0 + lr, row = lr * Wr;
-          sA = A[row + tx];
-          sB = Bs[row + tx];
-          uint32_t Ai2, Bi2;
-          if (ty & 1) { Ai2 = sB; Bi2 = A[row + txl]; }
-          else { Ai2 = Bs[row + txl]; Bi2 = sA; }
-          const uint32_t Ai4 = Bs[row + Wr + tx], Bi4 = A[row + Wr + tx];
-          adder4(sA ^ Ai2, sA ^ Ai4, sB ^ Bi2, sB ^ Bi4, s0, s1, s2);
-        }
-#pragma unroll 4
-        for (int k = 0; k < kMsb; ++k) {
-          const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
-                        4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
-          const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
-          if (lane == k) { cE += e; cM += m; }
-        }
-      }
-    }
-    atomicAdd(&s_cntE[lane], cE);
-    atomicAdd(&s_cntM[lane], cM);
-    {  // write the stripe back
-      uint4* ga = (uint4*)(words + (size_t)gi * P.N + (size_t)row0 * Wr);
-      uint4* gb = (uint4*)(words + (size_t)gi * P.N + h + (size_t)row0 * Wr);
-      const uint4* la = (const uint4*)(lat + Wr);
-      const uint4* lb = (const uint4*)(lat + SH + Wr);
-      for (int v = tid; v < (SW >> 2); v += blockDim.x) {
-        ga[v] = la[v];
-        gb[v] = lb[v];
-      }
-    }
+    cluster_count(P, lat, row0, LR, SH, tx, txl, rsub, worker, s_cntE, s_cntM);
+    cluster_move_stripe(P, lat, gi, row0, LR, SH, false);
     cluster.sync();  // all stripes' counts are complete
     if (rank == 0 && tid < kMsb) {
       int ce = 0, cm = 0;
