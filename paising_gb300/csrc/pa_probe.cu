@@ -18,7 +18,11 @@ namespace {
 
 constexpr int kProbeIters = 2048;
 
-__global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k, int mode) {
+// MODE 0: LOP3 only (ALU pipe), 1: IMAD only (FMA pipe), 2: LOP3 and IMAD
+// alternating (both integer pipes).  The mode is a template parameter so
+// that every mode compiles to straight chains of its own instructions.
+template <int MODE>
+__global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k) {
   uint32_t a[8];
   const uint32_t k2 = k * 3u + 1u;
 #pragma unroll
@@ -28,7 +32,7 @@ __global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k
   for (int it = 0; it < kProbeIters; ++it) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      if (mode == 0 || (mode == 2 && i < 4))
+      if (MODE == 0 || (MODE == 2 && (i & 1) == 0))
         asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[i]) : "r"(k), "r"(k2));
       else
         asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[i]) : "r"(k), "r"(k2));
@@ -61,7 +65,10 @@ int pa_probe_int_issue(int device, double* lane_ops_per_s) {
     float best = 1e30f;
     for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
       cudaEventRecord(e0);
-      int_issue_probe<<<blocks, threads>>>(buf, 0x9E3779B9u + rep, mode);
+      const uint32_t k = 0x9E3779B9u + rep;
+      if (mode == 0) int_issue_probe<0><<<blocks, threads>>>(buf, k);
+      else if (mode == 1) int_issue_probe<1><<<blocks, threads>>>(buf, k);
+      else int_issue_probe<2><<<blocks, threads>>>(buf, k);
       cudaEventRecord(e1);
       e = cudaEventSynchronize(e1);
       float ms = 0.f;
