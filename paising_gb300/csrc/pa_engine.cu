@@ -640,6 +640,9 @@ int validate(const pa_config& c) {
   if (c.R < 1 || c.sweeps < 0 || c.runs < 1 || !(c.dbeta > 0) || !(c.beta_final > 0))
     return bad("R, sweeps, runs, dbeta, beta_final out of range");
   if (c.capacity != 0 && c.capacity < 1.0) return bad("capacity must be >= 1");
+  // replica indices and slot counts are 32-bit on the device
+  if ((c.capacity > 0 ? c.capacity : 1.25) * (double)c.R + 256.0 > 2147483647.0 - kMsb)
+    return bad("R * capacity must stay below 2^31 replica slots");
   if (c.sweep_variant != 0 && c.sweep_variant != 1 && c.sweep_variant != 2 && c.sweep_variant != 4)
     return bad("sweep_variant must be 0, 1, 2 or 4");
   if (c.coding == PA_CODING_SSC && c.sweep_variant > 1) return bad("cluster sweeps exist for MSC only");

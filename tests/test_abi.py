@@ -50,6 +50,7 @@ def test_status_strings_and_defaults(engine_lib):
 @pytest.mark.parametrize("kw", [dict(L=12, coding="ssc"), dict(L=7, coding="msc"), dict(R=0), dict(sweeps=-1),
                                 dict(dbeta=0.0), dict(capacity=0.5), dict(L=264, coding="msc"),
                                 dict(L=256, coding="msc", sweep_variant=1), dict(L=64, coding="ssc", sweep_variant=2),
+                                dict(R=2_000_000_000), dict(R=1_000_000_000, capacity=2.5),
                                 dict(L=64, coding="msc", sweep_variant=3), dict(L=10, coding="msc", sweep_variant=2)])
 def test_create_rejects_bad_arguments(engine_lib, kw):
     import paising_gb300 as pa

@@ -163,3 +163,14 @@ def test_cli_reference_C1(cuda, tmp_path, coding):
     for a, b in zip(mine[:50], theirs[:50]):  # beta, E/N and R print identically
         fa, fb = a.split(), b.split()
         assert fa[0] == fb[0] and fa[1] == fb[1] and fa[8] == fb[8]
+
+
+def test_failed_allocation_is_reported(cuda):
+    """A population far larger than the device (about 80 TB of spins): the
+    allocation fails, pa_create returns PA_ERR_CUDA with a message and frees
+    what it had allocated, and the device stays usable."""
+    with pytest.raises(pa.PaisingError) as ei:
+        pa.Engine(L=256, R=1_000_000_000, coding="ssc")
+    assert ei.value.status == 2
+    rows, _ = run(L=16, R=200, sweeps=2, dbeta=0.25, seed=1, coding="msc")
+    assert rows[0].shape[0] == 5

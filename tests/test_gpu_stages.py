@@ -195,3 +195,36 @@ def test_native_acceptance_probability(cuda, st, oracle, coding, beta):
     prob = np.where(na >= 2, 1.0, np.where(na == 1, p[1], p[0]))
     mean, var = prob.sum(), (prob * (1 - prob)).sum()
     assert abs(flips - mean) < 5 * np.sqrt(var), (flips, mean, np.sqrt(var))
+
+
+def test_resample_plan_capacity_and_extinction(cuda, st, oracle):
+    """The error paths of the resampling plan: a population that would
+    outgrow its buffer raises the capacity error instead of writing past the
+    buffer (the copy-number kernel publishes the flag, the scatter then
+    writes nothing), and an empty new population the extinction error; the
+    call returns the status.  With exactly enough room the plan succeeds."""
+    torch = cuda
+    L, R = 16, 1000
+    _, E, _ = _energies(oracle, "ssc", L, R, 21, 0.3)
+    Et = torch.from_numpy(E).cuda()
+    b0, b1, Emean, iseq = 0.3, 0.305, float(E.mean()), 555
+    dB = b1 - b0
+    lnQ = -dB * Emean + np.log(oracle.ssc_q(E, dB, Emean)) - np.log(R)
+
+    def plan(Rinit, Rcap, seed):
+        return st.resample_plan(Et, None, pa.SSC, R, Rinit, Rcap, b0, b1, Emean, pa.WEIGHTS_FP64, seed, iseq)
+
+    Rn = oracle.ssc_copy_numbers(E, R, lnQ, dB, 21, iseq)[1]
+    assert plan(R, Rn, 21)[5] == Rn
+    with pytest.raises(pa.PaisingError) as ei:
+        plan(R, Rn - 1, 21)
+    assert ei.value.status == 3
+    # R_init = 1: about one copy expected in all, so some seeds draw none
+    n_new = {s: oracle.ssc_copy_numbers(E, 1, lnQ, dB, s, iseq)[1] for s in range(1, 40)}
+    dead = [s for s, n in n_new.items() if n == 0]
+    alive = [s for s, n in n_new.items() if n > 0]
+    assert dead and alive
+    with pytest.raises(pa.PaisingError) as ei:
+        plan(1, 2 * R, dead[0])
+    assert ei.value.status == 4
+    assert plan(1, 2 * R, alive[0])[5] == n_new[alive[0]]
