@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 site[k] = base + (uint32_t)sidx;  // = group * h + word in the group
               }
               const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
-              accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0);
+              accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0, P.T4, P.T8);
 #pragma unroll
               for (int k = 0; k < kKB; ++k)
                 if (vm >> k & 1u) self[site[k] - base] ^= ac[k];

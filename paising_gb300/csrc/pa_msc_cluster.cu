@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
             }
             const uint32_t chain =
                 (((uint32_t)gi * CS + (uint32_t)rank) * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
-            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0);
+            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0, P.T4, P.T8);
 #pragma unroll
             for (int k = 0; k < kKB; ++k)
               if (ix[k] >= 0) self[ix[k]] ^= ac[k];

@@ -42,21 +42,50 @@ __device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, ui
   und -= dec;
 }
 
-// Remaining digits (from digit 4 on) of one 32-bit comparison word, drawing
-// fresh Philox blocks (counter (c0, c1 | sub0 + c, step, tag)) until every
-// bit of every lane is decided.  Returns the bits decided "less".
-__device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub0,
-                                                  uint32_t step, uint32_t tag, const PhiloxKeys& K,
-                                                  const uint2* dig) {
+// The last undecided bits of a comparison word: their first 8 digits equal
+// T's, so U < T/2^32 is decided by the remaining 24 digits at once,
+// U mod 2^24 < T mod 2^24, with one fresh 32-bit word w per bit (its top 24
+// bits are U's remaining digits).  Takes the lowest undecided bit; a no-op
+// when none is left.
+__device__ __forceinline__ void finish_bit(uint32_t w, uint32_t am, uint32_t t4, uint32_t t8, uint32_t& und,
+                                           uint32_t& lt) {
+  const uint32_t b = und & (0u - und);
+  const uint32_t t = (am & b) ? t4 : t8;
+  lt |= (w >> 8) < t ? b : 0u;
+  und ^= b;
+}
+
+// Tag of the words that finish single bits (finish_bit): the sweep's tag with
+// bit 29 flipped ('M' -> 'm', 'S' -> 's'), a stream of its own.
+constexpr uint32_t kFinishTagFlip = 0x20u << 24;
+
+// Remaining digits (from digit 4 on) of one 32-bit comparison word: digits
+// 4..7 of every bit from one Philox block (counter (c0, c1 | sub, step,
+// tag)); the few bits still undecided after them (1/16 of those entering)
+// are finished one at a time by finish_bit, four per Philox block (counter
+// (c0, c1 | (fsub + k), step, tag ^ kFinishTagFlip), k = 0..7, enough for all
+// 32 bits).  Returns the bits decided "less".
+__device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub,
+                                                  uint32_t fsub, uint32_t step, uint32_t tag, const PhiloxKeys& K,
+                                                  const uint2* dig, uint32_t T4, uint32_t T8) {
   uint32_t lt = 0;
+  if (!__any_sync(kFull, und != 0u)) return lt;
+  {
+    const U4 r = philox10k(c0, c1 | sub, step, tag, K);
+    digit_step(r.x, am, dig[4], und, lt);
+    digit_step(r.y, am, dig[5], und, lt);
+    digit_step(r.z, am, dig[6], und, lt);
+    digit_step(r.w, am, dig[7], und, lt);
+  }
+  const uint32_t t4 = T4 & 0xFFFFFFu, t8 = T8 & 0xFFFFFFu, ftag = tag ^ kFinishTagFlip;
 #pragma unroll 1
-  for (int c = 0; c < 7; ++c) {
+  for (uint32_t k = 0; k < 8u; ++k) {
     if (!__any_sync(kFull, und != 0u)) break;
-    const U4 r = philox10k(c0, c1 | (sub0 + c), step, tag, K);
-    digit_step(r.x, am, dig[4 + 4 * c], und, lt);
-    digit_step(r.y, am, dig[5 + 4 * c], und, lt);
-    digit_step(r.z, am, dig[6 + 4 * c], und, lt);
-    digit_step(r.w, am, dig[7 + 4 * c], und, lt);
+    const U4 r = philox10k(c0, c1 | (fsub + k), step, ftag, K);
+    finish_bit(r.x, am, t4, t8, und, lt);
+    finish_bit(r.y, am, t4, t8, und, lt);
+    finish_bit(r.z, am, t4, t8, und, lt);
+    finish_bit(r.w, am, t4, t8, und, lt);
   }
   return lt;
 }
@@ -76,7 +105,7 @@ __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uin
 __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t (&und)[kKB], uint32_t (&acc)[kKB],
                                               const uint32_t (&site)[kKB], uint32_t chain_c0, uint32_t c1,
                                               uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig,
-                                              int nvalid) {
+                                              int nvalid, uint32_t T4, uint32_t T8) {
   // independent Philox chains of the kKB sites, interleaved by the compiler
   const uint2 d0 = dig[0], d1 = dig[1], d2 = dig[2], d3 = dig[3];
   auto head = [&](int k) {
@@ -110,13 +139,14 @@ __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t
       ovf |= 1u << k;
     }
   }
-  const uint32_t lt = finish_digits(m, am, chain_c0, c1, 1u, step, tag, K, dig);
+  const uint32_t lt = finish_digits(m, am, chain_c0, c1, 1u, 0u, step, tag, K, dig, T4, T8);
   acc[0] |= lt & und[0];
 #pragma unroll
   for (int k = 1; k < kKB; ++k) {
     if (!(ovf >> k & 1u)) acc[k] |= __funnelshift_r(lt, lt, rot[k]) & und[k];
     if (__any_sync(kFull, ovf >> k & 1u))
-      acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, step, tag, K, dig);
+      acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, 8u, step, tag, K,
+                              dig, T4, T8);
   }
 }
 

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         }
         const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u + (uint32_t)(q0 / kKB);
         // slots holding words lead (it grows with k): no Philox work for the rest
-        accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, __popc(vm));
+        accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, __popc(vm), P.T4, P.T8);
 #pragma unroll
         for (int k = 0; k < kKB; ++k)
           if (vm >> k & 1u) self[site[k] - (uint32_t)(ti * GW) * (uint32_t)wpp] ^= ac[k];
