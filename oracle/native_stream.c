@@ -1,0 +1,190 @@
+/*
+ * native_stream.c -- CPU restatement of the engine's NATIVE random stream and
+ * of the multi-spin-coded sweep that consumes it.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls
+ * this file; it is built into oracle/_build/libpaoracle.so beside the
+ * restatement of the reference (pa_oracle.c) and used by tests/ to check the
+ * engine's production sweep bit for bit.
+ *
+ * The reference has no counterpart: its MSC sweep draws one cuRAND word per
+ * word-site and expands it to 32 numbers with an LCG (PAisingMSC.cu:220-225).
+ * The engine's native stream instead decides every replica's Metropolis test
+ * U < T/2^32 (T = ceil(2^32 e^{-4 beta}) or ceil(2^32 e^{-8 beta}), the
+ * reference's thresholds, PAisingMSC.cu:674-675) exactly, from fresh
+ * Philox4x32-10 bits.  This file restates that specification independently of
+ * the CUDA code (written from the description, in plain C):
+ *
+ *   key      = the stream seed (k0 = low word, k1 = high word)
+ *   counter  = (c0, c1 | sub, step, tag)   c1 = (2 sweep + half) << 4
+ *   head     : word-site k of a thread's batch of four: digits 0..3 of its 32
+ *              comparisons from block (site_k, c1 | 0): word j = digit j
+ *   merge    : the still-undecided bits of sites 1..3 are rotated left by the
+ *              smallest r that keeps them clear of the bits already merged
+ *              (site 0's at rotation 0); a site with no such r "overflows"
+ *   tail     : the merged word takes digits 4..7 from block (chain, c1 | 1);
+ *              an overflowing site from block (site_k, c1 | 8)
+ *   finish   : a bit still undecided after digit 7 is decided at once by
+ *              U mod 2^24 < T mod 2^24, U's remaining 24 digits being the top
+ *              24 bits of one fresh word: lowest bit first, four bits per
+ *              block (c0, c1 | (fsub + k), step, tag ^ 0x20000000), k = 0..7,
+ *              fsub = 0 for the merged word and 8 for an overflowing site
+ *
+ * A digit-serial comparison: digit j of U is bit i of word j for replica bit
+ * i; while the digits agree with T's the bit stays undecided; at the first
+ * difference it is decided, "less" iff T's digit is 1.
+ */
+#include <stdint.h>
+#include <string.h>
+
+#include "inj_stream.h"
+
+#define FINISH_TAG_FLIP 0x20000000u
+
+static inline uint32_t rotl32(uint32_t x, uint32_t r) { return r ? (x << r) | (x >> (32u - r)) : x; }
+static inline uint32_t rotr32(uint32_t x, uint32_t r) { return r ? (x >> r) | (x << (32u - r)) : x; }
+
+static inline void blk(uint64_t key, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t o[4]) {
+    const uint32_t k[2] = {(uint32_t)key, (uint32_t)(key >> 32)};
+    const uint32_t c[4] = {c0, c1, c2, c3};
+    inj_philox4x32_10(k, c, o);
+}
+
+/* one digit j (0 = most significant) for every bit in *und; bits of `a` use
+ * T4's digit, the others T8's */
+static inline void digit(uint32_t u, uint32_t a, uint32_t T4, uint32_t T8, int j, uint32_t* und, uint32_t* lt) {
+    const uint32_t d4 = (T4 >> (31 - j)) & 1u ? 0xFFFFFFFFu : 0u;
+    const uint32_t d8 = (T8 >> (31 - j)) & 1u ? 0xFFFFFFFFu : 0u;
+    const uint32_t t = (a & d4) | (~a & d8);
+    const uint32_t differ = *und & (t ^ u);
+    *lt |= differ & t;
+    *und &= ~differ;
+}
+
+/* digits 4.. of one word's undecided bits; returns the bits decided "less" */
+static uint32_t finish_word(uint32_t und, uint32_t a, uint32_t c0, uint32_t c1, uint32_t sub, uint32_t fsub,
+                            uint32_t step, uint32_t tag, uint64_t key, uint32_t T4, uint32_t T8) {
+    uint32_t lt = 0, o[4];
+    if (!und) return 0;
+    blk(key, c0, c1 | sub, step, tag, o);
+    for (int j = 0; j < 4; ++j) digit(o[j], a, T4, T8, 4 + j, &und, &lt);
+    for (uint32_t k = 0; k < 8 && und; ++k) {
+        blk(key, c0, c1 | (fsub + k), step, tag ^ FINISH_TAG_FLIP, o);
+        for (int n = 0; n < 4 && und; ++n) {
+            int i = 0;
+            while (!((und >> i) & 1u)) ++i;
+            const uint32_t t = ((a >> i) & 1u ? T4 : T8) & 0xFFFFFFu;
+            if ((o[n] >> 8) < t) lt |= 1u << i;
+            und &= ~(1u << i);
+        }
+    }
+    return lt;
+}
+
+/* Acceptance of nvalid (<= 4) word-sites of one thread batch.
+ *   a[k]   bits with one anti-parallel neighbour (threshold T4), else T8
+ *   und[k] bits that need a random decision
+ *   acc[k] in: bits accepted outright; out: all accepted bits */
+void or_native_accept4(const uint32_t a[4], const uint32_t und_in[4], uint32_t acc[4], const uint32_t site[4],
+                       int nvalid, uint32_t chain, uint32_t c1, uint32_t step, uint32_t tag, uint64_t key,
+                       uint32_t T4, uint32_t T8) {
+    uint32_t und[4], o[4];
+    for (int k = 0; k < 4; ++k) {
+        und[k] = k < nvalid ? und_in[k] : 0u;
+        if (!und[k]) continue;
+        blk(key, site[k], c1, step, tag, o);
+        for (int j = 0; j < 4; ++j) digit(o[j], a[k], T4, T8, j, &und[k], &acc[k]);
+    }
+    uint32_t m = und[0], am = a[0] & und[0], rot[4] = {0, 0, 0, 0}, ovf[4] = {0, 0, 0, 0};
+    for (int k = 1; k < 4; ++k) {
+        uint32_t r = 0;
+        while (r < 32u && (m & rotl32(und[k], r))) ++r;
+        if (r == 32u) {
+            ovf[k] = 1;
+            continue;
+        }
+        rot[k] = r;
+        m |= rotl32(und[k], r);
+        am |= rotl32(a[k] & und[k], r);
+    }
+    const uint32_t lt = finish_word(m, am, chain, c1, 1u, 0u, step, tag, key, T4, T8);
+    acc[0] |= lt & und[0];
+    for (int k = 1; k < 4; ++k)
+        acc[k] |= ovf[k] ? finish_word(und[k], a[k] & und[k], site[k], c1, 8u, 8u, step, tag, key, T4, T8)
+                         : rotr32(lt, rot[k]) & und[k];
+}
+
+/* Bitsliced count of anti-parallel neighbours (PAisingMSC.cu:207-218). */
+static inline void count4(uint32_t s, const uint32_t n[4], uint32_t* c0, uint32_t* c1, uint32_t* c2) {
+    uint32_t b0 = 0, b1 = 0, b2 = 0;
+    for (int k = 0; k < 4; ++k) {  /* ripple-add one input plane at a time */
+        const uint32_t x = s ^ n[k];
+        const uint32_t carry0 = b0 & x;
+        b0 ^= x;
+        const uint32_t carry1 = b1 & carry0;
+        b1 ^= carry0;
+        b2 |= carry1;
+    }
+    *c0 = b0;
+    *c1 = b1;
+    *c2 = b2;
+}
+
+/* `sweeps` native checkerboard sweeps of rg groups of 32 replicas at
+ * thresholds T4, T8, with the thread layout of the engine's one-CTA sweep
+ * over one group per work unit: `threads` threads, thread (rsub, tx) =
+ * (tid / (L/2), tid % (L/2)) updates word column tx of sublattice rows
+ * rsub + pass * rpp, rpp = min(threads / (L/2), L), four passes per batch;
+ * its batch number is chain = (group * threads + tid) * nbatch + pass / 4.
+ * Layout as the reference's MSC Replica (PAisingMSC.cu:84-92): group g at
+ * words + g*N, sublattice A then B, site (x, y) of a sublattice at
+ * y*L/2 + x/2; the horizontal neighbour of an A site in an even row is on
+ * its left (PAisingMSC.cu:203, 238). */
+void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                         uint32_t step, uint32_t tag, int threads) {
+    const int N = L * L, h = N / 2, Wr = L / 2;
+    int rpp = threads / Wr;
+    if (rpp > L) rpp = L;
+    const int npass = (L + rpp - 1) / rpp, nbatch = (npass + 3) / 4;
+#pragma omp parallel for schedule(static)
+    for (int g = 0; g < rg; ++g) {
+        uint32_t* A = words + (size_t)g * N;
+        uint32_t* B = A + h;
+        for (int sw = 0; sw < sweeps; ++sw)
+            for (int hf = 0; hf < 2; ++hf) {
+                uint32_t* self = hf ? B : A;
+                const uint32_t* oth = hf ? A : B;
+                const uint32_t c1 = (uint32_t)(sw * 2 + hf) << 4;
+                for (int tid = 0; tid < Wr * rpp; ++tid) {
+                    const int tx = tid % Wr, rsub = tid / Wr;
+                    for (int p0 = 0; p0 < npass; p0 += 4) {
+                        uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
+                        int idx[4] = {-1, -1, -1, -1};
+                        for (int k = 0; k < 4; ++k) {
+                            const int pass = p0 + k, y = rsub + pass * rpp;
+                            if (pass >= npass || y >= L) continue;
+                            const int i = y * Wr + tx;
+                            /* horizontal neighbour: left for A in even rows and
+                             * B in odd rows, else right */
+                            const int left = (hf == 0) == ((y & 1) == 0);
+                            const int xs = left ? (tx + Wr - 1) % Wr : (tx + 1) % Wr;
+                            const uint32_t n[4] = {oth[y * Wr + xs], oth[i], oth[((y + L - 1) % L) * Wr + tx],
+                                                   oth[((y + 1) % L) * Wr + tx]};
+                            uint32_t c0, cc1, cc2;
+                            count4(self[i], n, &c0, &cc1, &cc2);
+                            a[k] = c0;
+                            acc[k] = cc1 | cc2;  /* two or more anti-parallel: dE <= 0 */
+                            und[k] = ~(cc1 | cc2);
+                            site[k] = (uint32_t)g * (uint32_t)h + (uint32_t)i;
+                            idx[k] = i;
+                        }
+                        const uint32_t chain = ((uint32_t)g * (uint32_t)threads + (uint32_t)tid) * (uint32_t)nbatch +
+                                               (uint32_t)(p0 / 4);
+                        or_native_accept4(a, und, acc, site, npass - p0, chain, c1, step, tag, key, T4, T8);
+                        for (int k = 0; k < 4; ++k)
+                            if (idx[k] >= 0) self[idx[k]] ^= acc[k];
+                    }
+                }
+            }
+    }
+}

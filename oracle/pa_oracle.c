@@ -487,6 +487,23 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
                double* fam, double* attempts);
 
+/* The engine's native-stream MSC sweep (native_stream.c). */
+void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                         uint32_t step, uint32_t tag, int threads);
+
+/* Native-stream sweeps in place of checkKerALL's (MSC only): key, tag and
+ * thread count of or_msc_sweep_native; temperature i of run r is counter
+ * word i | r << 14. */
+typedef struct {
+    uint64_t key;
+    uint32_t tag;
+    int threads;
+} native_sweep_cfg;
+
+static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+                       int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
+                       double* fam, double* attempts, const native_sweep_cfg* nat);
+
 int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
               int max_steps, double* rows, int max_rows, double* attempts) {
     return or_anneal2(msc, L, Rinit, sweeps, dBinit, Bfin, runs, seed, max_steps, 0, 0.0, 0.0, rows, max_rows,
@@ -502,6 +519,24 @@ int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin,
 int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
                double* fam, double* attempts) {
+    return anneal_impl(msc, L, Rinit, sweeps, dBinit, Bfin, runs, seed, max_steps, adaptive, minov, maxov, rows,
+                       max_rows, fam, attempts, NULL);
+}
+
+/* or_anneal2 for MSC with the engine's native-stream sweeps (the
+ * initialisation and the copy-number draws stay in reference coordinates,
+ * as in the engine); runs are sequential and continue the subsequence
+ * counter. */
+int or_anneal_msc_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+                         uint64_t key, uint32_t tag, int threads, double* rows, int max_rows, double* attempts) {
+    const native_sweep_cfg nat = {key, tag, threads};
+    return anneal_impl(1, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
+                       attempts, &nat);
+}
+
+static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+                       int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
+                       double* fam, double* attempts, const native_sweep_cfg* nat) {
     int N = L * L;
     const int nBmax = 10000;
     double* B = (double*)calloc(nBmax, sizeof(double));
@@ -602,7 +637,11 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                 if (fr) family_stats(anc, act, rg * MSB, Rinit, Rn[i], fr + (size_t)i * 3);
                 uint32_t thr[2];
                 or_msc_thresholds(B[i], thr);
-                or_msc_sweep(wd, L, rg, sweeps, thr, seed, iseq);
+                if (nat)
+                    or_msc_sweep_native(wd, L, rg, sweeps, thr[0], thr[1], nat->key,
+                                        (uint32_t)i | ((uint32_t)r << 14), nat->tag, nat->threads);
+                else
+                    or_msc_sweep(wd, L, rg, sweeps, thr, seed, iseq);
                 iseq += (uint64_t)rg * EQT;
                 or_msc_energy(wd, L, rg, Ev, Mm);
                 double avg[5];

@@ -43,6 +43,9 @@ _SIGS = {
     "or_anneal": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _vp, _i, _vp], _i),
     "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
+    "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _vp, _i, _vp], _i),
+    "or_native_accept4": ([_vp, _vp, _vp, _vp, _i, _u32, _u32, _u32, _u32, _u64, _u32, _u32], None),
+    "or_msc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], None),
 }
 
 _lib = None
@@ -59,7 +62,7 @@ def lib() -> ctypes.CDLL:
     if _lib is None:
         if not os.path.exists(LIB_PATH) or any(
                 os.path.getmtime(os.path.join(HERE, f)) > os.path.getmtime(LIB_PATH)
-                for f in ("pa_oracle.c", "kaufman.c", "inj_stream.h")):
+                for f in ("pa_oracle.c", "native_stream.c", "kaufman.c", "inj_stream.h")):
             build()
         L = ctypes.CDLL(LIB_PATH)
         for n, (a, r) in _SIGS.items():
@@ -212,6 +215,32 @@ def msc_resample(old: np.ndarray, L: int, roff, offs, Rnew: int):
     return new, act
 
 
+# ------------------------------------------------- the engine's native stream
+# (native_stream.c: no counterpart in the reference; pins the engine's
+# production sweep bit for bit)
+NATIVE_TAG_MSC = 0x4D << 24     # 'M' in the top byte of counter word 3
+FINISH_TAG_FLIP = 0x20 << 24    # single-bit finishing words: 'M' -> 'm'
+
+
+def native_accept4(a, und, acc, site, nvalid, chain, c1, step, tag, key, T4, T8) -> np.ndarray:
+    """Accepted bits of a batch of four word-sites (uint32[4])."""
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    und = np.ascontiguousarray(und, dtype=np.uint32)
+    out = np.ascontiguousarray(acc, dtype=np.uint32).copy()
+    site = np.ascontiguousarray(site, dtype=np.uint32)
+    lib().or_native_accept4(_p(a), _p(und), _p(out), _p(site), nvalid, chain, c1, step, tag, key, T4, T8)
+    return out
+
+
+def msc_sweep_native(words: np.ndarray, L: int, sweeps: int, T4: int, T8: int, key: int, step: int, tag: int,
+                     threads: int = 256) -> np.ndarray:
+    """Native-stream MSC sweeps of the engine's one-CTA sweep (one group per
+    work unit) on a copy of words [rg][N]."""
+    w = np.ascontiguousarray(words, dtype=np.uint32).copy()
+    lib().or_msc_sweep_native(_p(w), L, w.shape[0], sweeps, T4, T8, key, step, tag, threads)
+    return w
+
+
 # ---------------------------------------------------------- full anneal
 def anneal(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005, beta_final: float = 1.0,
            runs: int = 1, seed: int = 1, max_steps: int = 0, adaptive: bool = False, min_overlap: float = 0.85,
@@ -239,6 +268,20 @@ def anneal_family(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005
     if n < 0:
         raise RuntimeError("oracle anneal failed")
     return rows[:, :n], (fam[:, :n] if family else None), att.value
+
+
+def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
+                      key: int, tag: int, threads: int = 256):
+    """Rows of `runs` sequential MSC runs whose sweeps use the engine's
+    native stream (one-CTA sweep, one group per work unit): runs x nrows x 10."""
+    maxr = int(beta_final / dbeta) + 8
+    rows = np.zeros((runs, maxr, 10))
+    att = ctypes.c_double()
+    n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, threads, _p(rows), maxr,
+                                   ctypes.byref(att))
+    if n < 0:
+        raise RuntimeError("oracle anneal failed")
+    return rows[:, :n]
 
 
 def kaufman(L: int, beta: float):

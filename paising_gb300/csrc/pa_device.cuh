@@ -99,6 +99,14 @@ __host__ __device__ __forceinline__ double ref_uniform(uint32_t h) {
 constexpr uint32_t kTagSscSweep = 0x53u << 24;
 constexpr uint32_t kTagMscSweep = 0x4Du << 24;
 
+// Counter word 2 of the native sweep streams: the temperature index (below
+// 2^14, since schedules end at nBmax = 10000) and, above it, the population's
+// run number, so that repeated runs of a handle draw fresh sweep randomness
+// (runs 2^18 apart share it).
+__device__ __forceinline__ uint32_t native_step_word(const PopDev* st) {
+  return (uint32_t)st->step | ((uint32_t)st->run << 14);
+}
+
 // -------------------------------------------------------------- reductions
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {

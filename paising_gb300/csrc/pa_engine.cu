@@ -791,6 +791,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
     h.rng_mode = c.rng_mode;
     h.weights = c.weights;
     h.pop_id = P.user_index;
+    h.run = -1;  // begin_run_kernel numbers the runs from 0
     h.nsteps = P.nsteps;
     h.seed = c.seed;
     h.bf0 = -N * std::log(2.0);

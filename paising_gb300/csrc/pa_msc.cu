@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         const PopDev* st = b->pops + p;
         P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.Wr = st->Wr; P.rpp = st->rpp; P.npass = st->npass;
         P.kconst = st->kconst;
-        P.step = st->step;
+        P.step = (int)native_step_word(st);
         P.sweeps = energy_only ? 0 : st->sweeps;
         P.nbatch = (st->npass + kKB - 1) / kKB;
         P.G = st->gpt > 0 ? st->gpt : 1;

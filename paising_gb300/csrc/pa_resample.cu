@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(1024) plan_kernel(BatchDev* b, int energy_only
 __global__ void begin_run_kernel(PopDev* pops) {
   PopDev* st = pops + blockIdx.x;
   st->step = 0;
+  st->run += 1;  // -1 at creation: the first run is run 0
   st->R_prev = st->R_cur = st->Rinit;
   st->parity = 0;
   st->error = 0;

@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
   int cur = -1;
   PopDev* st = nullptr;
   int L = 0, N = 0, h = 0, Wr = 1, hw = 0, rpp = 1, kconst = 0, step = 0, sweeps = 0;
+  uint32_t nstep = 0;  // counter word 2 of the native stream
   unsigned long long seed = 0, iseq = 0;
   // native stream key: one seed for the whole batch; populations differ in counter word 3
   const uint32_t k0 = (uint32_t)stream_seed, k1 = (uint32_t)(stream_seed >> 32);
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       st = b->pops + p;
       L = st->L; N = st->N; h = N >> 1; hw = h >> 2; Wr = st->Wr; rpp = st->rpp; kconst = st->kconst;
       step = st->step;
+      nstep = native_step_word(st);
       sweeps = energy_only ? 0 : st->sweeps;
       seed = st->seed;
       tag = kTagSscSweep | (uint32_t)st->pop_id;
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
             s[1] = self[w1];
             na[0] = anti(ty0, oth, s[0], hf);
             na[1] = two ? anti(ty1, oth, s[1], hf) : 0x02020202u;  // no decision needed
-            const U4 rn = philox10((uint32_t)(r * hw + w0), c1, (uint32_t)step, tag, k0, k1);
+            const U4 rn = philox10((uint32_t)(r * hw + w0), c1, nstep, tag, k0, k1);
             const uint32_t top[2] = {rn.x, rn.y};
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 const int bit = __ffs(pend) - 1;
                 pend &= pend - 1;
                 if (used == 2 || used == 6) {
-                  const U4 x = philox10((uint32_t)(r * hw + w0), c1 + 1u, (uint32_t)step,
+                  const U4 x = philox10((uint32_t)(r * hw + w0), c1 + 1u, nstep,
                                         tag | ((uint32_t)(used >> 2) << 12), k0, k1);
                   a0 = x.x; a1 = x.y; a2 = x.z; a3 = x.w;
                 }

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         P.M0 = m0;
         P.ML = m0 << (P.seg - 1);
         P.V = P.segs * P.seg == 32 ? 0xffffffffu : (1u << (P.segs * P.seg)) - 1u;
-        P.step = st->step;
+        P.step = (int)native_step_word(st);
         P.sweeps = energy_only ? 0 : st->sweeps;
         P.tag = kTagSscSweep | (uint32_t)st->pop_id;
         P.T4 = st->thr[(size_t)st->step * kThrPerStep + 10];

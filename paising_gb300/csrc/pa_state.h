@@ -60,7 +60,7 @@ struct PopDev {
   int error;           // 0 ok, 1 capacity exceeded, 2 population extinct
   int Emin;            // minimum energy of the current population
   unsigned int ticket;     // last-block tickets of the resampling kernels
-  unsigned int pad2;
+  int run;             // runs begun on this population before the current one (native stream key)
   unsigned long long iseq;  // reference subsequence counter (initial_sequence, PAisingSSC.cu:418)
   double Emean;        // <E> of the current population (Emean, PAisingSSC.cu:483,620)
   double sumlnQ;       // -sum of lnQ over the steps so far (PAisingSSC.cu:627)

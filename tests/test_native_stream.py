@@ -1,0 +1,121 @@
+"""The engine's native random stream (no counterpart in the reference).
+
+CPU: the oracle's restatement of the native acceptance (oracle/native_stream.c)
+decides each replica's Metropolis test with probability exactly T/2^32 -- the
+reference's thresholds -- and without correlation between replicas or sites.
+The thresholds are chosen so that the single-bit finish after digit 7 carries
+a visible share of the probability (T4 mod 2^24 = 2^24 - 1, T8 mod 2^24 = 0).
+
+GPU: the production MSC sweep (pa_msc_sweep, native stream) equals that
+restatement bit for bit, and its energy epilogue equals energyKer's; two
+consecutive whole runs of one handle equal the oracle's anneal with the same
+native sweeps row for row (the run number is part of the sweep counter).
+"""
+import numpy as np
+import pytest
+
+import paising_gb300 as pa
+
+N_CALLS = 60000
+
+
+def _accept_samples(oracle, T4, T8, n=N_CALLS, seed=3):
+    """n batches of four word-sites, every bit undecided; replica bits of site
+    k use T4 where a[k] is set.  Returns (accepted bits [n, 128], a bits)."""
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 2**32, size=(n, 4), dtype=np.uint64).astype(np.uint32)
+    und = np.full(4, 0xFFFFFFFF, dtype=np.uint32)
+    zero = np.zeros(4, dtype=np.uint32)
+    out = np.empty((n, 4), dtype=np.uint32)
+    for i in range(n):
+        site = np.array([4 * i, 4 * i + 1, 4 * i + 2, 4 * i + 3], dtype=np.uint32)
+        out[i] = oracle.native_accept4(a[i], und, zero, site, 4, i, 0x50, 9, oracle.NATIVE_TAG_MSC | 7, 2026, T4, T8)
+    bits = lambda x: ((x[:, :, None] >> np.arange(32, dtype=np.uint32)) & 1).reshape(len(x), 128)
+    return bits(out).astype(np.float64), bits(a).astype(bool)
+
+
+@pytest.mark.parametrize("T4,T8", [(0xA5FFFFFF, 0x3C000000), (0x2BFFFFFF, 0x07000000)])
+def test_native_acceptance_is_exact(oracle, T4, T8):
+    acc, use4 = _accept_samples(oracle, T4, T8)
+    for mask, T in ((use4, T4), (~use4, T8)):
+        p = T / 2**32
+        n = mask.sum()
+        f = acc[mask].mean()
+        assert abs(f - p) < 5 * np.sqrt(p * (1 - p) / n), (hex(T), f, p, n)
+
+
+def test_native_acceptance_finish_uses_each_bits_threshold(oracle):
+    """With T4 and T8 equal in their first 8 digits, only the single-bit finish
+    tells them apart: T4 mod 2^24 = 2^24 - 1, T8 mod 2^24 = 0, so the two
+    classes must differ by 2^-8 in acceptance."""
+    T4, T8 = 0x47FFFFFF, 0x47000000
+    acc, use4 = _accept_samples(oracle, T4, T8, seed=11)
+    f4, f8 = acc[use4].mean(), acc[~use4].mean()
+    n4, n8 = use4.sum(), (~use4).sum()
+    for f, T, n in ((f4, T4, n4), (f8, T8, n8)):
+        p = T / 2**32
+        assert abs(f - p) < 5 * np.sqrt(p * (1 - p) / n), (hex(T), f, p)
+    assert f4 - f8 > 2**-8 - 10 * np.sqrt(0.28 * 0.72 / min(n4, n8))
+
+
+def test_native_acceptance_uncorrelated(oracle):
+    """No two of a batch's 128 decisions (4 word-sites x 32 replicas) share
+    randomness: every pairwise correlation is within sampling noise."""
+    acc, _ = _accept_samples(oracle, 0x40000000, 0x10000000, seed=5)
+    c = np.corrcoef(acc.T)
+    np.fill_diagonal(c, 0.0)
+    assert np.abs(c).max() < 6.0 / np.sqrt(len(acc)), np.abs(c).max()
+
+
+def test_native_acceptance_partial_batch(oracle):
+    """Slots beyond nvalid draw nothing and keep their outright accepts."""
+    a = np.array([0x0F0F0F0F, 0, 0xFFFF0000, 0x12345678], dtype=np.uint32)
+    und = np.array([0xFFFFFFFF, 0xFFFFFFFF, 0, 0], dtype=np.uint32)
+    acc0 = np.array([0, 0, 0xF0, 0x0F], dtype=np.uint32)
+    site = np.arange(4, dtype=np.uint32)
+    out = oracle.native_accept4(a, und, acc0, site, 2, 1, 0x30, 1, oracle.NATIVE_TAG_MSC, 5, 0x80000000, 0x20000000)
+    assert out[2] == 0xF0 and out[3] == 0x0F
+    # the first two sites drew: the same call is deterministic
+    again = oracle.native_accept4(a, und, acc0, site, 2, 1, 0x30, 1, oracle.NATIVE_TAG_MSC, 5, 0x80000000,
+                                  0x20000000)
+    assert np.array_equal(out, again)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,sweeps,beta", [(16, 64, 3, 0.3), (10, 40, 2, 0.44), (12, 96, 2, 0.9),
+                                             (24, 33, 2, 0.44), (64, 70, 2, 0.35), (128, 32, 1, 0.44)])
+def test_msc_sweep_native_stream_bit_exact(cuda, st, oracle, L, R, sweeps, beta):
+    seed, step = 777 + L, 5
+    w, act = st.msc_init(L, R, seed=seed, iseq=0)
+    ow, _ = oracle.msc_init(L, R, seed, 0)
+    E, M = st.msc_sweep(w, act, L, sweeps, beta, pa.RNG_NATIVE, seed=seed, iseq=0, step=step)
+    T4, T8 = (int(x) for x in oracle.msc_thresholds(beta))
+    # the stage call runs temperature step 1 of population `step`
+    ref = oracle.msc_sweep_native(ow, L, sweeps, T4, T8, seed, 1, oracle.NATIVE_TAG_MSC | step)
+    got = w.cpu().numpy().view(np.uint32)
+    assert (ref != ow).any()
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {got.size} words differ"
+    oE, oM = oracle.msc_energy(ref, L)
+    assert np.array_equal(E.cpu().numpy(), oE) and np.array_equal(M.cpu().numpy(), oM)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("L,R,sweeps,dbeta", [(16, 200, 5, 0.05), (24, 700, 3, 0.1), (64, 1000, 4, 0.1)])
+def test_msc_anneal_native_stream_two_runs(cuda, oracle, graph, L, R, sweeps, dbeta):
+    """Whole anneals with the production stream: two runs of one handle
+    (one-CTA sweep, one group per work unit, FP64 weights) equal the oracle's
+    sequential runs row for row -- population sizes exactly -- and the second
+    run draws sweep randomness of its own (temperature i of run r is native
+    counter word i | r << 14)."""
+    from conftest import compare_rows
+    seed = 100 + L
+    with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=1.0, seed=seed, coding="msc", rng="native",
+                   weights="fp64", graph=graph, sweep_variant=1, tile_groups=1, device=0) as e:
+        got = []
+        for _ in range(2):
+            e.run()
+            got.append(e.rows(0))
+    ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 2, seed, seed, oracle.NATIVE_TAG_MSC | 0)
+    for r in range(2):
+        compare_rows(got[r], ref[r], rtol=2e-10)
