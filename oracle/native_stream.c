@@ -130,61 +130,105 @@ static inline void count4(uint32_t s, const uint32_t n[4], uint32_t* c0, uint32_
     *c2 = b2;
 }
 
-/* `sweeps` native checkerboard sweeps of rg groups of 32 replicas at
- * thresholds T4, T8, with the thread layout of the engine's one-CTA sweep
- * over one group per work unit: `threads` threads, thread (rsub, tx) =
- * (tid / (L/2), tid % (L/2)) updates word column tx of sublattice rows
- * rsub + pass * rpp, rpp = min(threads / (L/2), L), four passes per batch;
- * its batch number is chain = (group * threads + tid) * nbatch + pass / 4.
- * Layout as the reference's MSC Replica (PAisingMSC.cu:84-92): group g at
- * words + g*N, sublattice A then B, site (x, y) of a sublattice at
- * y*L/2 + x/2; the horizontal neighbour of an A site in an even row is on
- * its left (PAisingMSC.cu:203, 238). */
-void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
-                         uint32_t step, uint32_t tag, int threads) {
+/* One thread's batches of one half-sweep: word column tx of the rows
+ * first_row + rsub + pass * rpp (pass < npass, row index below nrows) of a
+ * stack of sublattice rows in which row v belongs to group group0 + v / L at
+ * row v % L (a one-group unit: nrows = L; a stacked tile: nrows = groups * L;
+ * a cluster stripe: the stripe's rows of one group).  Batch b of the thread
+ * is Philox chain chain0 + b. */
+static void thread_half(uint32_t* words, int L, int group0, int first_row, int nrows, int rsub, int tx, int rpp,
+                        int npass, int hf, uint32_t c1, uint32_t chain0, uint64_t key, uint32_t step, uint32_t tag,
+                        uint32_t T4, uint32_t T8) {
     const int N = L * L, h = N / 2, Wr = L / 2;
-    int rpp = threads / Wr;
-    if (rpp > L) rpp = L;
-    const int npass = (L + rpp - 1) / rpp, nbatch = (npass + 3) / 4;
+    for (int p0 = 0; p0 < npass; p0 += 4) {
+        uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
+        uint32_t* word[4] = {NULL, NULL, NULL, NULL};
+        for (int k = 0; k < 4; ++k) {
+            const int pass = p0 + k, v = first_row + rsub + pass * rpp;
+            if (pass >= npass || v >= first_row + nrows) continue;
+            const int g = group0 + v / L, y = v % L, i = y * Wr + tx;
+            uint32_t* self = words + (size_t)g * N + (hf ? h : 0);
+            const uint32_t* oth = words + (size_t)g * N + (hf ? 0 : h);
+            /* horizontal neighbour: left for A in even rows and B in odd
+             * rows, else right */
+            const int left = (hf == 0) == ((y & 1) == 0);
+            const int xs = left ? (tx + Wr - 1) % Wr : (tx + 1) % Wr;
+            const uint32_t n[4] = {oth[y * Wr + xs], oth[i], oth[((y + L - 1) % L) * Wr + tx],
+                                   oth[((y + 1) % L) * Wr + tx]};
+            uint32_t c0, cc1, cc2;
+            count4(self[i], n, &c0, &cc1, &cc2);
+            a[k] = c0;
+            acc[k] = cc1 | cc2;  /* two or more anti-parallel: dE <= 0 */
+            und[k] = ~(cc1 | cc2);
+            site[k] = (uint32_t)g * (uint32_t)h + (uint32_t)i;
+            word[k] = self + i;
+        }
+        or_native_accept4(a, und, acc, site, npass - p0, chain0 + (uint32_t)(p0 / 4), c1, step, tag, key, T4, T8);
+        for (int k = 0; k < 4; ++k)
+            if (word[k]) *word[k] ^= acc[k];
+    }
+}
+
+/* `sweeps` native checkerboard sweeps of rg groups of 32 replicas at
+ * thresholds T4, T8, with the thread layouts of the engine's MSC sweeps:
+ *   cs = 1: one CTA of `threads` threads per work unit of G groups (tile
+ *           ti = groups G ti .. G ti + G - 1, the last one possibly short),
+ *           whose sublattices form one stack of G L rows; thread
+ *           (rsub, tx) = (tid / (L/2), tid % (L/2)) updates word column tx of
+ *           stacked rows rsub + pass * rpp, rpp = min(threads / (L/2), G L);
+ *           its batch of four passes p0 / 4 is chain (ti threads + tid)
+ *           nbatch + p0 / 4;
+ *   cs > 1: a cluster of cs CTAs per group; CTA `rank` updates rows
+ *           [rank L/cs, (rank + 1) L/cs) with rpp the largest divisor of L/cs
+ *           with (L/2) rpp <= threads; chain ((g cs + rank) threads + tid)
+ *           nbatch + p0 / 4.
+ * Within a half-sweep every update reads the other sublattice only, so the
+ * order in which threads are visited does not matter.  Layout as the
+ * reference's MSC Replica (PAisingMSC.cu:84-92): group g at words + g*N,
+ * sublattice A then B, site (x, y) of a sublattice at y*L/2 + x/2; the
+ * horizontal neighbour of an A site in an even row is on its left
+ * (PAisingMSC.cu:203, 238). */
+void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                          uint32_t step, uint32_t tag, int threads, int G, int cs) {
+    const int Wr = L / 2;
+    int rpp, npass, nunits;
+    if (cs <= 1) {
+        rpp = threads / Wr;
+        if (rpp > G * L) rpp = G * L;
+        npass = (G * L + rpp - 1) / rpp;
+        nunits = (rg + G - 1) / G;
+    } else {
+        const int LR = L / cs;
+        rpp = 1;
+        for (int r = 1; r <= LR; ++r)
+            if (LR % r == 0 && Wr * r <= threads) rpp = r;
+        npass = LR / rpp;
+        nunits = rg * cs;
+    }
+    const int nbatch = (npass + 3) / 4;
 #pragma omp parallel for schedule(static)
-    for (int g = 0; g < rg; ++g) {
-        uint32_t* A = words + (size_t)g * N;
-        uint32_t* B = A + h;
+    for (int u = 0; u < nunits; ++u) {
+        /* units touch disjoint groups except the CTAs of one cluster, which
+         * are visited together below */
+        if (cs > 1 && u % cs) continue;
+        const int g0 = cs > 1 ? u / cs : u * G, gc = cs > 1 ? 1 : (rg - g0 < G ? rg - g0 : G);
         for (int sw = 0; sw < sweeps; ++sw)
             for (int hf = 0; hf < 2; ++hf) {
-                uint32_t* self = hf ? B : A;
-                const uint32_t* oth = hf ? A : B;
                 const uint32_t c1 = (uint32_t)(sw * 2 + hf) << 4;
-                for (int tid = 0; tid < Wr * rpp; ++tid) {
-                    const int tx = tid % Wr, rsub = tid / Wr;
-                    for (int p0 = 0; p0 < npass; p0 += 4) {
-                        uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
-                        int idx[4] = {-1, -1, -1, -1};
-                        for (int k = 0; k < 4; ++k) {
-                            const int pass = p0 + k, y = rsub + pass * rpp;
-                            if (pass >= npass || y >= L) continue;
-                            const int i = y * Wr + tx;
-                            /* horizontal neighbour: left for A in even rows and
-                             * B in odd rows, else right */
-                            const int left = (hf == 0) == ((y & 1) == 0);
-                            const int xs = left ? (tx + Wr - 1) % Wr : (tx + 1) % Wr;
-                            const uint32_t n[4] = {oth[y * Wr + xs], oth[i], oth[((y + L - 1) % L) * Wr + tx],
-                                                   oth[((y + 1) % L) * Wr + tx]};
-                            uint32_t c0, cc1, cc2;
-                            count4(self[i], n, &c0, &cc1, &cc2);
-                            a[k] = c0;
-                            acc[k] = cc1 | cc2;  /* two or more anti-parallel: dE <= 0 */
-                            und[k] = ~(cc1 | cc2);
-                            site[k] = (uint32_t)g * (uint32_t)h + (uint32_t)i;
-                            idx[k] = i;
-                        }
-                        const uint32_t chain = ((uint32_t)g * (uint32_t)threads + (uint32_t)tid) * (uint32_t)nbatch +
-                                               (uint32_t)(p0 / 4);
-                        or_native_accept4(a, und, acc, site, npass - p0, chain, c1, step, tag, key, T4, T8);
-                        for (int k = 0; k < 4; ++k)
-                            if (idx[k] >= 0) self[idx[k]] ^= acc[k];
+                for (int rank = 0; rank < (cs > 1 ? cs : 1); ++rank)
+                    for (int tid = 0; tid < Wr * rpp; ++tid) {
+                        const uint32_t unit = cs > 1 ? (uint32_t)(g0 * cs + rank) : (uint32_t)u;
+                        const uint32_t chain0 = (unit * (uint32_t)threads + (uint32_t)tid) * (uint32_t)nbatch;
+                        const int first = cs > 1 ? rank * (L / cs) : 0, nrows = cs > 1 ? L / cs : gc * L;
+                        thread_half(words, L, g0, first, nrows, tid / Wr, tid % Wr, rpp, npass, hf, c1, chain0, key,
+                                    step, tag, T4, T8);
                     }
-                }
             }
     }
+}
+
+/* The one-CTA sweep over one group per work unit (cs = 1, G = 1). */
+void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                         uint32_t step, uint32_t tag, int threads) {
+    or_msc_sweep_native2(words, L, rg, sweeps, T4, T8, key, step, tag, threads, 1, 1);
 }

@@ -487,17 +487,17 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
                double* fam, double* attempts);
 
-/* The engine's native-stream MSC sweep (native_stream.c). */
-void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
-                         uint32_t step, uint32_t tag, int threads);
+/* The engine's native-stream MSC sweeps (native_stream.c). */
+void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                          uint32_t step, uint32_t tag, int threads, int G, int cs);
 
-/* Native-stream sweeps in place of checkKerALL's (MSC only): key, tag and
- * thread count of or_msc_sweep_native; temperature i of run r is counter
- * word i | r << 14. */
+/* Native-stream sweeps in place of checkKerALL's (MSC only): key, tag,
+ * threads per CTA, groups per work unit and CTAs per group of
+ * or_msc_sweep_native2; temperature i of run r is counter word i | r << 14. */
 typedef struct {
     uint64_t key;
     uint32_t tag;
-    int threads;
+    int threads, G, cs;
 } native_sweep_cfg;
 
 static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
@@ -528,8 +528,9 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
  * as in the engine); runs are sequential and continue the subsequence
  * counter. */
 int or_anneal_msc_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
-                         uint64_t key, uint32_t tag, int threads, double* rows, int max_rows, double* attempts) {
-    const native_sweep_cfg nat = {key, tag, threads};
+                         uint64_t key, uint32_t tag, int threads, int G, int cs, double* rows, int max_rows,
+                         double* attempts) {
+    const native_sweep_cfg nat = {key, tag, threads, G, cs};
     return anneal_impl(1, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
                        attempts, &nat);
 }
@@ -638,8 +639,8 @@ static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, dou
                 uint32_t thr[2];
                 or_msc_thresholds(B[i], thr);
                 if (nat)
-                    or_msc_sweep_native(wd, L, rg, sweeps, thr[0], thr[1], nat->key,
-                                        (uint32_t)i | ((uint32_t)r << 14), nat->tag, nat->threads);
+                    or_msc_sweep_native2(wd, L, rg, sweeps, thr[0], thr[1], nat->key,
+                                         (uint32_t)i | ((uint32_t)r << 14), nat->tag, nat->threads, nat->G, nat->cs);
                 else
                     or_msc_sweep(wd, L, rg, sweeps, thr, seed, iseq);
                 iseq += (uint64_t)rg * EQT;

@@ -43,7 +43,7 @@ _SIGS = {
     "or_anneal": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _vp, _i, _vp], _i),
     "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
-    "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _vp, _i, _vp], _i),
+    "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _i, _i, _vp, _i, _vp], _i),
     "or_native_accept4": ([_vp, _vp, _vp, _vp, _i, _u32, _u32, _u32, _u32, _u64, _u32, _u32], None),
     "or_msc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], None),
 }
@@ -271,14 +271,15 @@ def anneal_family(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005
 
 
 def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
-                      key: int, tag: int, threads: int = 256):
+                      key: int, tag: int, threads: int = 256, tile: int = 1, cluster: int = 1):
     """Rows of `runs` sequential MSC runs whose sweeps use the engine's
-    native stream (one-CTA sweep, one group per work unit): runs x nrows x 10."""
+    native stream: runs x nrows x 10.  tile: groups per work unit of the
+    one-CTA sweep; cluster: CTAs per group (threads = threads per CTA)."""
     maxr = int(beta_final / dbeta) + 8
     rows = np.zeros((runs, maxr, 10))
     att = ctypes.c_double()
-    n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, threads, _p(rows), maxr,
-                                   ctypes.byref(att))
+    n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, threads, tile, cluster,
+                                   _p(rows), maxr, ctypes.byref(att))
     if n < 0:
         raise RuntimeError("oracle anneal failed")
     return rows[:, :n]

@@ -119,3 +119,39 @@ def test_msc_anneal_native_stream_two_runs(cuda, oracle, graph, L, R, sweeps, db
     ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 2, seed, seed, oracle.NATIVE_TAG_MSC | 0)
     for r in range(2):
         compare_rows(got[r], ref[r], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,tile", [(16, 300, 2), (16, 1000, 8), (32, 500, 4), (24, 400, 2), (32, 900, 8)])
+def test_msc_anneal_native_stream_stacked_tiles(cuda, oracle, L, R, tile):
+    """Stacked tiles (several groups per work unit of the one-CTA sweep, the
+    last tile short where the group count is not a multiple): every batch of
+    four stacked rows is numbered by its tile, so the stream differs from the
+    one-group sweep and must still equal the oracle's restatement."""
+    from conftest import compare_rows
+    seed = 31 + tile
+    with pa.Engine(L=L, R=R, sweeps=3, dbeta=0.1, beta_final=1.0, seed=seed, coding="msc", rng="native",
+                   weights="fp64", graph=True, sweep_variant=1, tile_groups=tile, device=0) as e:
+        assert e.sweep_form(0)["tile"] == tile
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_msc_native(L, R, 3, 0.1, 1.0, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256, tile, 1)
+    compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,cs", [(16, 200, 2), (16, 200, 4), (64, 100, 4), (256, 40, 2)])
+def test_msc_anneal_native_stream_clusters(cuda, oracle, L, R, cs):
+    """Thread-block clusters (cs CTAs per group, 1024 or 512 threads each,
+    halo rows over distributed shared memory) under the native stream equal
+    the oracle's restatement of the same thread layout row for row."""
+    from conftest import compare_rows
+    seed, threads = 57 + cs, {2: 1024, 4: 512}[cs]
+    sweeps, dbeta = (2, 0.25) if L == 256 else (3, 0.1)
+    with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=1.0, seed=seed, coding="msc", rng="native",
+                   weights="fp64", graph=True, sweep_variant=cs, device=0) as e:
+        assert e.sweep_form(0)["cluster_ctas"] == cs
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_MSC, threads, 1, cs)
+    compare_rows(got, ref[0], rtol=2e-10)
