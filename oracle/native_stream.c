@@ -35,6 +35,7 @@
  * difference it is decided, "less" iff T's digit is 1.
  */
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "inj_stream.h"
@@ -231,4 +232,99 @@ void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T
 void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
                          uint32_t step, uint32_t tag, int threads) {
     or_msc_sweep_native2(words, L, rg, sweeps, T4, T8, key, step, tag, threads, 1, 1);
+}
+
+/* ---------------------------------------------------------------------------
+ * SSC populations swept on bit planes (native stream; no counterpart in the
+ * reference, whose SSC sweep draws one cuRAND double per site,
+ * PAisingSSC.cu:159-193).
+ *
+ * Row layout: a sublattice row of S = L/2 sites is Wq words of seg sites,
+ * the smallest Wq (at most 8) with seg = S/Wq a multiple of 4 and at most 32;
+ * when Wq = 1, segs = floor(32/seg) replicas share a word, replica j of the
+ * word in bits [j seg, (j + 1) seg); bit i of a segment is site x = c seg + i
+ * of the row (c = word of the row).  A tile holds G replicas (G a multiple of
+ * segs), i.e. G/segs word groups of wpp = L Wq words per sublattice; the last
+ * tile of a population may be short: the word groups it touches are complete,
+ * the missing replicas' segments start at bit 0 and are swept like the others
+ * (their decisions take part in the acceptance's merging) but never stored.
+ * Half-sweep: 256 threads; word it = tid + 256 q of the tile's plane goes to
+ * thread tid, four words (q = q0..q0+3) per batch, batch chain
+ * (tile 256 + tid) 8 + q0/4; word-site number (tile G/segs + word group) wpp
+ * + word of the group.
+ * ------------------------------------------------------------------------- */
+static int bits_layout_c(int L, int* Wq, int* seg, int* segs) {
+    if (L < 8 || L % 8 != 0 || L > 256) return 0;
+    const int S = L / 2;
+    for (int w = (S + 31) / 32; w <= 8; ++w)
+        if (S % w == 0 && (S / w) % 4 == 0) {
+            *Wq = w;
+            *seg = S / w;
+            *segs = w == 1 ? 32 / *seg : 1;
+            return 1;
+        }
+    return 0;
+}
+
+/* returns 0 where L has no bit-plane layout or G is not a multiple of segs */
+int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                             uint32_t step, uint32_t tag, int G) {
+    int Wq, seg, segs;
+    if (!bits_layout_c(L, &Wq, &seg, &segs) || G < segs || G % segs) return 0;
+    const int N = L * L, h = N / 2, S = L / 2, wpp = L * Wq, GW = G / segs, ntiles = (R + G - 1) / G;
+#pragma omp parallel for schedule(static)
+    for (int ti = 0; ti < ntiles; ++ti) {
+        const int r0 = ti * G, gc = R - r0 < G ? R - r0 : G;
+        const int ngroups = (gc + segs - 1) / segs, slots = ngroups * segs, items = ngroups * wpp;
+        /* sp[slot][X][y][x] in {0, 1} (1 == +1); slots beyond gc start at 0 */
+        uint8_t* sp = (uint8_t*)calloc((size_t)slots * N, 1);
+        for (int r = 0; r < gc; ++r)
+            for (int i = 0; i < N; ++i) sp[(size_t)r * N + i] = spins[(size_t)(r0 + r) * N + i] > 0;
+        for (int sw = 0; sw < sweeps; ++sw)
+            for (int hf = 0; hf < 2; ++hf) {
+                const uint32_t c1 = (uint32_t)(sw * 2 + hf) << 4;
+                for (int tid = 0; tid < 256; ++tid)
+                    for (int q0 = 0; q0 * 256 < items; q0 += 4) {
+                        uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
+                        int item[4] = {-1, -1, -1, -1}, nvalid = 0;
+                        for (int k = 0; k < 4; ++k) {
+                            const int it = tid + (q0 + k) * 256;
+                            if (it >= items) continue;
+                            const int g = it / wpp, wr = it % wpp, y = wr / Wq, c = wr % Wq;
+                            const int left = (hf == 0) == ((y & 1) == 0);
+                            for (int j = 0; j < segs; ++j)
+                                for (int i = 0; i < seg; ++i) {
+                                    const uint8_t* me = sp + (size_t)(g * segs + j) * N + (hf ? h : 0);
+                                    const uint8_t* ot = sp + (size_t)(g * segs + j) * N + (hf ? 0 : h);
+                                    const int x = c * seg + i, xs = left ? (x + S - 1) % S : (x + 1) % S;
+                                    const int s = me[y * S + x];
+                                    const int n = (s != ot[y * S + x]) + (s != ot[y * S + xs]) +
+                                                  (s != ot[((y + L - 1) % L) * S + x]) +
+                                                  (s != ot[((y + 1) % L) * S + x]);
+                                    const uint32_t bit = 1u << (j * seg + i);
+                                    if (n >= 2) acc[k] |= bit;
+                                    else und[k] |= bit;
+                                    if (n == 1) a[k] |= bit;
+                                }
+                            site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)wr;
+                            item[k] = it;
+                            ++nvalid;
+                        }
+                        or_native_accept4(a, und, acc, site, nvalid, ((uint32_t)ti * 256u + (uint32_t)tid) * 8u +
+                                          (uint32_t)(q0 / 4), c1, step, tag, key, T4, T8);
+                        for (int k = 0; k < 4; ++k) {
+                            if (item[k] < 0) continue;
+                            const int g = item[k] / wpp, wr = item[k] % wpp, y = wr / Wq, c = wr % Wq;
+                            for (int j = 0; j < segs; ++j)
+                                for (int i = 0; i < seg; ++i)
+                                    if ((acc[k] >> (j * seg + i)) & 1u)
+                                        sp[(size_t)(g * segs + j) * N + (hf ? h : 0) + y * S + c * seg + i] ^= 1;
+                        }
+                    }
+            }
+        for (int r = 0; r < gc; ++r)
+            for (int i = 0; i < N; ++i) spins[(size_t)(r0 + r) * N + i] = sp[(size_t)r * N + i] ? 1 : -1;
+        free(sp);
+    }
+    return 1;
 }

@@ -491,9 +491,13 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
 void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
                           uint32_t step, uint32_t tag, int threads, int G, int cs);
 
-/* Native-stream sweeps in place of checkKerALL's (MSC only): key, tag,
- * threads per CTA, groups per work unit and CTAs per group of
- * or_msc_sweep_native2; temperature i of run r is counter word i | r << 14. */
+int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                             uint32_t step, uint32_t tag, int G);
+
+/* Native-stream sweeps in place of checkKerALL's: key, tag, threads per CTA,
+ * groups (MSC) or replicas (SSC bit planes) per work unit and CTAs per group
+ * of or_msc_sweep_native2 / or_ssc_sweep_bits_native; temperature i of run r
+ * is counter word i | r << 14. */
 typedef struct {
     uint64_t key;
     uint32_t tag;
@@ -532,6 +536,14 @@ int or_anneal_msc_native(int L, int Rinit, int sweeps, double dBinit, double Bfi
                          double* attempts) {
     const native_sweep_cfg nat = {key, tag, threads, G, cs};
     return anneal_impl(1, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
+                       attempts, &nat);
+}
+
+/* The same for SSC with the bit-plane sweep (tile replicas per work unit). */
+int or_anneal_ssc_bits_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
+                              uint64_t key, uint32_t tag, int tile, double* rows, int max_rows, double* attempts) {
+    const native_sweep_cfg nat = {key, tag, 256, tile, 1};
+    return anneal_impl(0, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
                        attempts, &nat);
 }
 
@@ -607,9 +619,19 @@ static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, dou
                 int32_t* ta2 = anc; anc = anc2; anc2 = ta2;
                 Rn[i] = (int)Rnew;
                 if (fr) family_stats(anc, NULL, Rn[i], Rinit, Rn[i], fr + (size_t)i * 3);
-                double tab[10];
-                or_ssc_boltz(B[i], tab);
-                or_ssc_sweep(sp, L, Rn[i], sweeps, tab, seed, iseq);
+                if (nat) {
+                    uint32_t thr[2];
+                    or_msc_thresholds(B[i], thr);
+                    if (!or_ssc_sweep_bits_native(sp, L, Rn[i], sweeps, thr[0], thr[1], nat->key,
+                                                  (uint32_t)i | ((uint32_t)r << 14), nat->tag, nat->G)) {
+                        ret = -1;
+                        break;
+                    }
+                } else {
+                    double tab[10];
+                    or_ssc_boltz(B[i], tab);
+                    or_ssc_sweep(sp, L, Rn[i], sweeps, tab, seed, iseq);
+                }
                 iseq += (uint64_t)Rn[i] * EQT;
                 or_ssc_energy(sp, L, Rn[i], Ev, Mm);
                 double avg[5];

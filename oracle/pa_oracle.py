@@ -44,6 +44,8 @@ _SIGS = {
     "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
     "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _i, _i, _vp, _i, _vp], _i),
+    "or_anneal_ssc_bits_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _vp, _i, _vp], _i),
+    "or_ssc_sweep_bits_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], _i),
     "or_native_accept4": ([_vp, _vp, _vp, _vp, _i, _u32, _u32, _u32, _u32, _u64, _u32, _u32], None),
     "or_msc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], None),
 }
@@ -219,6 +221,7 @@ def msc_resample(old: np.ndarray, L: int, roff, offs, Rnew: int):
 # (native_stream.c: no counterpart in the reference; pins the engine's
 # production sweep bit for bit)
 NATIVE_TAG_MSC = 0x4D << 24     # 'M' in the top byte of counter word 3
+NATIVE_TAG_SSC = 0x53 << 24     # 'S': the SSC sweeps
 FINISH_TAG_FLIP = 0x20 << 24    # single-bit finishing words: 'M' -> 'm'
 
 
@@ -270,6 +273,39 @@ def anneal_family(coding: str, L: int, R: int, sweeps: int, dbeta: float = 0.005
     return rows[:, :n], (fam[:, :n] if family else None), att.value
 
 
+def bits_layout(L: int):
+    """(words per sublattice row, sites per segment, segments per word) of the
+    SSC bit-plane sweep, or None where L has no layout."""
+    if L < 8 or L % 8 or L > 256:
+        return None
+    S = L // 2
+    for w in range((S + 31) // 32, 9):
+        if S % w == 0 and (S // w) % 4 == 0:
+            return w, S // w, (32 // (S // w) if w == 1 else 1)
+    return None
+
+
+def bits_max_tile(L: int) -> int:
+    """Replicas per tile of the bit-plane sweep when none is asked for: the
+    word groups of 1024 words per sublattice plane (at least one), at most
+    256 replicas."""
+    Wq, seg, segs = bits_layout(L)
+    gw = max(1, 1024 // (L * Wq))
+    if gw * segs > 256:
+        gw = 256 // segs
+    return gw * segs
+
+
+def ssc_sweep_bits_native(spins: np.ndarray, L: int, sweeps: int, T4: int, T8: int, key: int, step: int, tag: int,
+                          tile: int) -> np.ndarray:
+    """Native-stream SSC sweeps on bit planes with `tile` replicas per work
+    unit, on a copy of spins [R][N] (int8 +-1)."""
+    s = np.ascontiguousarray(spins, dtype=np.int8).copy()
+    if not lib().or_ssc_sweep_bits_native(_p(s), L, s.shape[0], sweeps, T4, T8, key, step, tag, tile):
+        raise ValueError(f"no bit-plane layout for L={L} with {tile} replicas per tile")
+    return s
+
+
 def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
                       key: int, tag: int, threads: int = 256, tile: int = 1, cluster: int = 1):
     """Rows of `runs` sequential MSC runs whose sweeps use the engine's
@@ -280,6 +316,20 @@ def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: flo
     att = ctypes.c_double()
     n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, threads, tile, cluster,
                                    _p(rows), maxr, ctypes.byref(att))
+    if n < 0:
+        raise RuntimeError("oracle anneal failed")
+    return rows[:, :n]
+
+
+def anneal_ssc_bits_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
+                           key: int, tag: int, tile: int):
+    """Rows of `runs` sequential SSC runs swept on bit planes with the
+    engine's native stream, `tile` replicas per work unit: runs x nrows x 10."""
+    maxr = int(beta_final / dbeta) + 8
+    rows = np.zeros((runs, maxr, 10))
+    att = ctypes.c_double()
+    n = lib().or_anneal_ssc_bits_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, tile, _p(rows), maxr,
+                                        ctypes.byref(att))
     if n < 0:
         raise RuntimeError("oracle anneal failed")
     return rows[:, :n]

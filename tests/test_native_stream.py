@@ -6,7 +6,7 @@ reference's thresholds -- and without correlation between replicas or sites.
 The thresholds are chosen so that the single-bit finish after digit 7 carries
 a visible share of the probability (T4 mod 2^24 = 2^24 - 1, T8 mod 2^24 = 0).
 
-GPU: the production MSC sweep (pa_msc_sweep, native stream) equals that
+GPU: the production MSC and SSC bit-plane sweeps (native stream) equal that
 restatement bit for bit, and its energy epilogue equals energyKer's; two
 consecutive whole runs of one handle equal the oracle's anneal with the same
 native sweeps row for row (the run number is part of the sweep counter).
@@ -155,3 +155,47 @@ def test_msc_anneal_native_stream_clusters(cuda, oracle, L, R, cs):
         got = e.rows(0)
     ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_MSC, threads, 1, cs)
     compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,beta", [(8, 521, 0.44), (16, 303, 0.3), (24, 171, 0.44), (32, 130, 0.9),
+                                      (40, 45, 0.44), (48, 50, 0.35), (64, 37, 0.44), (96, 11, 0.44),
+                                      (128, 9, 0.5)])
+def test_ssc_sweep_bits_native_stream_bit_exact(cuda, st, oracle, L, R, beta):
+    """The SSC bit-plane sweep (pa_ssc_sweep_bits: largest tile, short last
+    tiles, rows sharing a word as segments for L <= 32, rows of several words
+    for L = 96, 128) equals the oracle's site-by-site restatement bit for bit,
+    and its popcount energies equal energyKer's."""
+    seed, step = 4000 + L, 3
+    g = st.ssc_init(L, R, seed=seed, iseq=0)
+    init = oracle.ssc_init(L, R, seed, 0)
+    E, M = st.ssc_sweep_bits(g, L, 2, beta, seed=seed, step=step)
+    T4, T8 = (int(x) for x in oracle.msc_thresholds(beta))
+    ref = oracle.ssc_sweep_bits_native(init, L, 2, T4, T8, seed, 1, oracle.NATIVE_TAG_SSC | step,
+                                       oracle.bits_max_tile(L))
+    got = g.cpu().numpy()
+    assert (ref != init).any()
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {got.size} sites differ"
+    oE, oM = oracle.ssc_energy(ref, L)
+    assert np.array_equal(E.cpu().numpy(), oE) and np.array_equal(M.cpu().numpy(), oM)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R", [(16, 1000), (24, 500), (64, 700)])
+def test_ssc_anneal_native_stream_bit_planes(cuda, oracle, L, R):
+    """Whole SSC anneals on bit planes (the engine's automatic tile, two runs
+    of one handle, FP64 weights) equal the oracle's anneal with the same
+    native sweeps row for row."""
+    from conftest import compare_rows
+    seed = 900 + L
+    with pa.Engine(L=L, R=R, sweeps=3, dbeta=0.1, beta_final=1.0, seed=seed, coding="ssc", rng="native",
+                   weights="fp64", graph=True, device=0) as e:
+        form = e.sweep_form(0)
+        assert form["spins_per_word"] == 32
+        got = []
+        for _ in range(2):
+            e.run()
+            got.append(e.rows(0))
+    ref = oracle.anneal_ssc_bits_native(L, R, 3, 0.1, 1.0, 2, seed, seed, oracle.NATIVE_TAG_SSC, form["tile"])
+    for r in range(2):
+        compare_rows(got[r], ref[r], rtol=2e-10)
