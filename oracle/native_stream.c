@@ -328,3 +328,80 @@ int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T
     }
     return 1;
 }
+
+/* ---------------------------------------------------------------------------
+ * SSC populations swept one int8 spin per site (native stream; the sweep of
+ * lattices without a dense bit-plane layout, or when asked for).
+ *
+ * A site with dE <= 0 flips; otherwise it flips iff U < T (T4 for one
+ * anti-parallel neighbour, T8 for none), decided a byte at a time.  Words of
+ * four sites (site x = 4 c + j of a sublattice row is byte j of word c) are
+ * handled in pairs: thread (rsub, c) = (tid / (L/8), tid % (L/8)) of the
+ * replica's unit, tid < (L/8) rpp (rpp the largest divisor of L with
+ * (L/8) rpp <= 256), takes rows ty0 = rsub, rsub + 2 rpp, ... and with each
+ * also row ty1 = ty0 + rpp if ty1 < L.  Block (r h/4 + w0, 2 (2 sweep + half),
+ * step, tag), w0 = ty0 L/8 + c: word x gives U's top bytes for row ty0, word
+ * y for row ty1; a site whose top byte equals T's is decided by U's low 24
+ * bits, taken in order of (row ty0 sites, row ty1 sites) from words z, w,
+ * then from blocks (r h/4 + w0, 2 (2 sweep + half) + 1, step, tag | k << 12),
+ * k = 0, 1, four words each.
+ * ------------------------------------------------------------------------- */
+void or_ssc_sweep_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                         uint32_t step, uint32_t tag) {
+    const int N = L * L, h = N / 2, S = L / 2, Wr = L / 8, hw = h / 4;
+    int rpp = 1;
+    for (int q = 1; q <= L; ++q)
+        if (L % q == 0 && Wr * q <= 256) rpp = q;
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < R; ++r) {
+        int8_t* A = spins + (size_t)r * N;
+        for (int sw = 0; sw < sweeps; ++sw)
+            for (int hf = 0; hf < 2; ++hf) {
+                int8_t* self = A + (hf ? h : 0);
+                const int8_t* oth = A + (hf ? 0 : h);
+                const uint32_t c1 = (uint32_t)(sw * 2 + hf) * 2u;
+                for (int tid = 0; tid < Wr * rpp; ++tid) {
+                    const int c = tid % Wr, rsub = tid / Wr;
+                    for (int ty0 = rsub; ty0 < L; ty0 += 2 * rpp) {
+                        const int rows[2] = {ty0, ty0 + rpp}, nrow = ty0 + rpp < L ? 2 : 1;
+                        uint32_t o[4];
+                        blk(key, (uint32_t)(r * hw + ty0 * Wr + c), c1, step, tag, o);
+                        int flip[8] = {0}, pend[8], npend = 0, na_of[8];
+                        for (int q = 0; q < nrow; ++q) {
+                            const int y = rows[q], left = (hf == 0) == ((y & 1) == 0);
+                            for (int j = 0; j < 4; ++j) {
+                                const int x = 4 * c + j, xs = left ? (x + S - 1) % S : (x + 1) % S;
+                                const int s = self[y * S + x];
+                                const int na = (s != oth[y * S + x]) + (s != oth[y * S + xs]) +
+                                               (s != oth[((y + L - 1) % L) * S + x]) +
+                                               (s != oth[((y + 1) % L) * S + x]);
+                                na_of[4 * q + j] = na;
+                                if (na >= 2) {
+                                    flip[4 * q + j] = 1;
+                                    continue;
+                                }
+                                const uint32_t T = na == 1 ? T4 : T8;
+                                const uint32_t ub = (o[q] >> (8 * j)) & 0xFFu, tb = T >> 24;
+                                if (ub < tb) flip[4 * q + j] = 1;
+                                else if (ub == tb) pend[npend++] = 4 * q + j;
+                            }
+                        }
+                        uint32_t words[10] = {o[2], o[3]};
+                        if (npend > 2) {
+                            blk(key, (uint32_t)(r * hw + ty0 * Wr + c), c1 + 1u, step, tag, words + 2);
+                            if (npend > 6) blk(key, (uint32_t)(r * hw + ty0 * Wr + c), c1 + 1u, step, tag | (1u << 12),
+                                               words + 6);
+                        }
+                        for (int p = 0; p < npend; ++p) {
+                            const int b = pend[p];
+                            const uint32_t T = na_of[b] == 1 ? T4 : T8;
+                            if ((words[p] & 0xFFFFFFu) < (T & 0xFFFFFFu)) flip[b] = 1;
+                        }
+                        for (int q = 0; q < nrow; ++q)
+                            for (int j = 0; j < 4; ++j)
+                                if (flip[4 * q + j]) self[rows[q] * S + 4 * c + j] = (int8_t)-self[rows[q] * S + 4 * c + j];
+                    }
+                }
+            }
+    }
+}

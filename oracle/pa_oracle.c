@@ -493,11 +493,13 @@ void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T
 
 int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
                              uint32_t step, uint32_t tag, int G);
+void or_ssc_sweep_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
+                         uint32_t step, uint32_t tag);
 
 /* Native-stream sweeps in place of checkKerALL's: key, tag, threads per CTA,
- * groups (MSC) or replicas (SSC bit planes) per work unit and CTAs per group
- * of or_msc_sweep_native2 / or_ssc_sweep_bits_native; temperature i of run r
- * is counter word i | r << 14. */
+ * groups (MSC) or replicas (SSC bit planes; 0: the int8 SSC sweep) per work
+ * unit and CTAs per group of or_msc_sweep_native2 / or_ssc_sweep_bits_native
+ * / or_ssc_sweep_native; temperature i of run r is counter word i | r << 14. */
 typedef struct {
     uint64_t key;
     uint32_t tag;
@@ -539,7 +541,8 @@ int or_anneal_msc_native(int L, int Rinit, int sweeps, double dBinit, double Bfi
                        attempts, &nat);
 }
 
-/* The same for SSC with the bit-plane sweep (tile replicas per work unit). */
+/* The same for SSC with the bit-plane sweep (tile replicas per work unit),
+ * or with the int8 sweep (tile = 0). */
 int or_anneal_ssc_bits_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                               uint64_t key, uint32_t tag, int tile, double* rows, int max_rows, double* attempts) {
     const native_sweep_cfg nat = {key, tag, 256, tile, 1};
@@ -622,8 +625,11 @@ static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, dou
                 if (nat) {
                     uint32_t thr[2];
                     or_msc_thresholds(B[i], thr);
-                    if (!or_ssc_sweep_bits_native(sp, L, Rn[i], sweeps, thr[0], thr[1], nat->key,
-                                                  (uint32_t)i | ((uint32_t)r << 14), nat->tag, nat->G)) {
+                    const uint32_t word = (uint32_t)i | ((uint32_t)r << 14);
+                    if (nat->G == 0)
+                        or_ssc_sweep_native(sp, L, Rn[i], sweeps, thr[0], thr[1], nat->key, word, nat->tag);
+                    else if (!or_ssc_sweep_bits_native(sp, L, Rn[i], sweeps, thr[0], thr[1], nat->key, word,
+                                                       nat->tag, nat->G)) {
                         ret = -1;
                         break;
                     }

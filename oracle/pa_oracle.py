@@ -45,6 +45,7 @@ _SIGS = {
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
     "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _i, _i, _vp, _i, _vp], _i),
     "or_anneal_ssc_bits_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _vp, _i, _vp], _i),
+    "or_ssc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32], None),
     "or_ssc_sweep_bits_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], _i),
     "or_native_accept4": ([_vp, _vp, _vp, _vp, _i, _u32, _u32, _u32, _u32, _u64, _u32, _u32], None),
     "or_msc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], None),
@@ -321,10 +322,19 @@ def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: flo
     return rows[:, :n]
 
 
+def ssc_sweep_native(spins: np.ndarray, L: int, sweeps: int, T4: int, T8: int, key: int, step: int,
+                     tag: int) -> np.ndarray:
+    """Native-stream SSC sweeps one int8 spin per site, on a copy of spins."""
+    s = np.ascontiguousarray(spins, dtype=np.int8).copy()
+    lib().or_ssc_sweep_native(_p(s), L, s.shape[0], sweeps, T4, T8, key, step, tag)
+    return s
+
+
 def anneal_ssc_bits_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
                            key: int, tag: int, tile: int):
     """Rows of `runs` sequential SSC runs swept on bit planes with the
-    engine's native stream, `tile` replicas per work unit: runs x nrows x 10."""
+    engine's native stream, `tile` replicas per work unit (0: the int8 sweep):
+    runs x nrows x 10."""
     maxr = int(beta_final / dbeta) + 8
     rows = np.zeros((runs, maxr, 10))
     att = ctypes.c_double()

@@ -199,3 +199,39 @@ def test_ssc_anneal_native_stream_bit_planes(cuda, oracle, L, R):
     ref = oracle.anneal_ssc_bits_native(L, R, 3, 0.1, 1.0, 2, seed, seed, oracle.NATIVE_TAG_SSC, form["tile"])
     for r in range(2):
         compare_rows(got[r], ref[r], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,beta", [(8, 60, 0.44), (16, 33, 0.3), (24, 20, 0.9), (40, 17, 0.44),
+                                      (56, 9, 0.35), (64, 12, 0.44), (136, 3, 0.44)])
+def test_ssc_sweep_int8_native_stream_bit_exact(cuda, st, oracle, L, R, beta):
+    """The int8 SSC sweep's byte-at-a-time acceptance (pa_ssc_sweep, native
+    stream) equals the oracle's restatement bit for bit, energies included."""
+    seed, step = 5000 + L, 2
+    g = st.ssc_init(L, R, seed=seed, iseq=0)
+    init = oracle.ssc_init(L, R, seed, 0)
+    E, M = st.ssc_sweep(g, L, 3, beta, pa.RNG_NATIVE, seed=seed, iseq=0, step=step)
+    T4, T8 = (int(x) for x in oracle.msc_thresholds(beta))
+    ref = oracle.ssc_sweep_native(init, L, 3, T4, T8, seed, 1, oracle.NATIVE_TAG_SSC | step)
+    got = g.cpu().numpy()
+    assert (ref != init).any()
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {got.size} sites differ"
+    oE, oM = oracle.ssc_energy(ref, L)
+    assert np.array_equal(E.cpu().numpy(), oE) and np.array_equal(M.cpu().numpy(), oM)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,variant", [(40, 600, 0), (64, 500, 1)])
+def test_ssc_anneal_native_stream_int8(cuda, oracle, L, R, variant):
+    """Whole SSC anneals on the int8 sweep (L=40, whose bit-plane words would
+    be 5/8 full, by default; L=64 by sweep_variant=1) equal the oracle's
+    anneal with the same native sweeps row for row."""
+    from conftest import compare_rows
+    seed = 700 + L
+    with pa.Engine(L=L, R=R, sweeps=3, dbeta=0.1, beta_final=1.0, seed=seed, coding="ssc", rng="native",
+                   weights="fp64", graph=True, sweep_variant=variant, device=0) as e:
+        assert e.sweep_form(0)["spins_per_word"] == 4
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_ssc_bits_native(L, R, 3, 0.1, 1.0, 1, seed, seed, oracle.NATIVE_TAG_SSC, 0)
+    compare_rows(got, ref[0], rtol=2e-10)
