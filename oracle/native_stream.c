@@ -132,20 +132,21 @@ static inline void count4(uint32_t s, const uint32_t n[4], uint32_t* c0, uint32_
 }
 
 /* One thread's batches of one half-sweep: word column tx of the rows
- * first_row + rsub + pass * rpp (pass < npass, row index below nrows) of a
+ * first_row + rsub + pass * rpp (interleaved) or first_row + rsub * npass +
+ * pass (consecutive), pass < npass, row index below first_row + nrows, of a
  * stack of sublattice rows in which row v belongs to group group0 + v / L at
  * row v % L (a one-group unit: nrows = L; a stacked tile: nrows = groups * L;
  * a cluster stripe: the stripe's rows of one group).  Batch b of the thread
  * is Philox chain chain0 + b. */
 static void thread_half(uint32_t* words, int L, int group0, int first_row, int nrows, int rsub, int tx, int rpp,
-                        int npass, int hf, uint32_t c1, uint32_t chain0, uint64_t key, uint32_t step, uint32_t tag,
-                        uint32_t T4, uint32_t T8) {
+                        int npass, int consecutive, int hf, uint32_t c1, uint32_t chain0, uint64_t key, uint32_t step,
+                        uint32_t tag, uint32_t T4, uint32_t T8) {
     const int N = L * L, h = N / 2, Wr = L / 2;
     for (int p0 = 0; p0 < npass; p0 += 4) {
         uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
         uint32_t* word[4] = {NULL, NULL, NULL, NULL};
         for (int k = 0; k < 4; ++k) {
-            const int pass = p0 + k, v = first_row + rsub + pass * rpp;
+            const int pass = p0 + k, v = first_row + (consecutive ? rsub * npass + pass : rsub + pass * rpp);
             if (pass >= npass || v >= first_row + nrows) continue;
             const int g = group0 + v / L, y = v % L, i = y * Wr + tx;
             uint32_t* self = words + (size_t)g * N + (hf ? h : 0);
@@ -176,9 +177,10 @@ static void thread_half(uint32_t* words, int L, int group0, int first_row, int n
  *           ti = groups G ti .. G ti + G - 1, the last one possibly short),
  *           whose sublattices form one stack of G L rows; thread
  *           (rsub, tx) = (tid / (L/2), tid % (L/2)) updates word column tx of
- *           stacked rows rsub + pass * rpp, rpp = min(threads / (L/2), G L);
- *           its batch of four passes p0 / 4 is chain (ti threads + tid)
- *           nbatch + p0 / 4;
+ *           stacked rows rsub + pass * rpp (G > 1) or of its own consecutive
+ *           rows rsub * npass + pass (G = 1), rpp = min(threads / (L/2), G L),
+ *           npass = ceil(G L / rpp); its batch of four passes p0 / 4 is chain
+ *           (ti threads + tid) nbatch + p0 / 4;
  *   cs > 1: a cluster of cs CTAs per group; CTA `rank` updates rows
  *           [rank L/cs, (rank + 1) L/cs) with rpp the largest divisor of L/cs
  *           with (L/2) rpp <= threads; chain ((g cs + rank) threads + tid)
@@ -221,8 +223,8 @@ void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T
                         const uint32_t unit = cs > 1 ? (uint32_t)(g0 * cs + rank) : (uint32_t)u;
                         const uint32_t chain0 = (unit * (uint32_t)threads + (uint32_t)tid) * (uint32_t)nbatch;
                         const int first = cs > 1 ? rank * (L / cs) : 0, nrows = cs > 1 ? L / cs : gc * L;
-                        thread_half(words, L, g0, first, nrows, tid / Wr, tid % Wr, rpp, npass, hf, c1, chain0, key,
-                                    step, tag, T4, T8);
+                        thread_half(words, L, g0, first, nrows, tid / Wr, tid % Wr, rpp, npass, cs <= 1 && G == 1,
+                                    hf, c1, chain0, key, step, tag, T4, T8);
                     }
             }
     }

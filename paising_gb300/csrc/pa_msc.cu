@@ -71,18 +71,41 @@ __global__ void msc_init_kernel(PopDev* pops) {
 //   (accept_native); each replica's acceptance probability is exactly
 //   T/2^32, as in the reference.  The stream is keyed by stream_seed (one
 //   per batch; populations differ in counter word 3).
-// Tile gi0 (gc groups present) <-> HBM: group gi0+g's sublattice X goes to
-// lat + X*G*h + g*h (for G = 1 simply the group's N words; G > 1 implies
-// h % 4 == 0).  Out of line: keeps the sweep loop's registers free.
+// Tile gi0 (gc groups present) <-> HBM.  G > 1 (implies h % 4 == 0): group
+// gi0+g's sublattice X goes to lat + X*G*h + g*h.  G = 1: sublattice X is a
+// block of L + 2 rows at lat + X*sb -- row -1 (a copy of row L-1), rows
+// 0..L-1, row L (a copy of row 0) -- so that the native sweep reads its
+// vertical neighbours without wrapping; the sweep keeps the copies current.
+// Out of line: keeps the sweep loop's registers free.
 __device__ __noinline__ void msc_move_tile(const UnitParams& P, uint32_t* lat, int gi0, int gc, bool to_smem) {
   const int N = P.N, h = P.h, G = P.G;
   uint4* lat4 = (uint4*)lat;
   uint4* g4 = (uint4*)(P.words + (size_t)gi0 * N);
   if (G == 1) {
-    for (int v = threadIdx.x; v < (N >> 2); v += blockDim.x) {
-      if (to_smem) lat4[v] = g4[v];
-      else g4[v] = lat4[v];
+    const int Wr = P.Wr, L = P.L;
+    uint32_t* gw = P.words + (size_t)gi0 * N;
+    if ((Wr & 3) == 0) {  // rows start on 16-byte boundaries in both places
+      const int h4 = h >> 2;
+      for (int v = threadIdx.x; v < 2 * h4; v += blockDim.x) {
+        const int X = v >= h4 ? 1 : 0, i = v - X * h4;
+        uint4* s = (uint4*)(lat + X * P.sb + Wr) + i;
+        uint4* d = (uint4*)(gw + X * h) + i;
+        if (to_smem) *s = *d;
+        else *d = *s;
+      }
+    } else {
+      for (int v = threadIdx.x; v < N; v += blockDim.x) {
+        const int X = v >= h ? 1 : 0, i = v - X * h;
+        uint32_t* s = lat + X * P.sb + Wr + i;
+        if (to_smem) *s = gw[v];
+        else gw[v] = *s;
+      }
     }
+    if (to_smem)  // periodic copies: row -1 = row L-1, row L = row 0
+      for (int v = threadIdx.x; v < 4 * Wr; v += blockDim.x) {
+        const int X = v >= 2 * Wr ? 1 : 0, r = v - X * 2 * Wr, top = r < Wr ? 1 : 0, i = top ? r : r - Wr;
+        lat[X * P.sb + (top ? 0 : (L + 1) * Wr) + i] = gw[X * h + (top ? (L - 1) * Wr : 0) + i];
+      }
     return;
   }
   const int h4 = h >> 2, n4 = N >> 2;
@@ -107,8 +130,8 @@ __device__ __noinline__ void msc_count(const UnitParams& P, const uint32_t* lat,
   const int w = tid >> 5, g = w / wpg, ws = w - g * wpg;
   int cE = 0, cM = 0;  // lane k accumulates bit k
   if (g >= gc) return;  // warp-uniform
-  const uint32_t* A = lat + g * h;
-  const uint32_t* B = lat + G * h + g * h;
+  const uint32_t* A = G == 1 ? lat + Wr : lat + g * h;
+  const uint32_t* B = G == 1 ? lat + P.sb + Wr : lat + G * h + g * h;
   for (int j0 = ws * 32; j0 < h; j0 += wpg * 32) {
     const int j = j0 + lane;
     uint32_t s0 = 0, s1 = 0, s2 = 0, sA = 0, sB = 0;
@@ -170,6 +193,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         P.nbatch = (st->npass + kKB - 1) / kKB;
         P.G = st->gpt > 0 ? st->gpt : 1;
         P.rg = (st->R_cur + kMsb - 1) / kMsb;
+        P.sb = msc_halo_block(st->L, st->Wr);
         P.invL = st->invL;
         P.invWr = st->invWr;
         const unsigned long long h4 = (unsigned long long)(st->N >> 3);
@@ -230,8 +254,9 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
       for (int hf = 0; hf < 2; ++hf) {
-        uint32_t* self = lat + (hf ? G * h : 0);
-        const uint32_t* oth = lat + (hf ? 0 : G * h);
+        // row 0 of the swept and of the other sublattice
+        uint32_t* self = G == 1 ? lat + (hf ? P.sb : 0) + P.Wr : lat + (hf ? G * h : 0);
+        const uint32_t* oth = G == 1 ? lat + (hf ? 0 : P.sb) + P.Wr : lat + (hf ? 0 : G * h);
         const int Wr = P.Wr, rpp = P.rpp, npass = P.npass;
         if (MODE == kRefCoords) {
 #pragma unroll 1
@@ -266,12 +291,55 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
             if (valid) self[sidx] = s ^ acc;
           }
         } else {
-          // one code path for single-group tiles (the common L >= 64 case, kept
-          // free of the stacking arithmetic) and one for stacked tiles
-          auto native_half = [&](auto tiled_c) {
-            constexpr bool kTiled = decltype(tiled_c)::value;
-            const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
-            const uint32_t base = (uint32_t)gi0 * (uint32_t)h;  // site number of the tile's first word
+          const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+          const uint32_t base = (uint32_t)gi0 * (uint32_t)h;  // site number of the tile's first word
+          if (G == 1) {
+            // one group (the common L >= 64 case): thread rsub owns the
+            // consecutive rows rsub*npass .. rsub*npass + npass - 1 of column
+            // tx, so a batch of kKB rows shares the other sublattice's rows
+            // around them, and the periodic copies of rows -1 and L spare the
+            // vertical wrap
+            const int L = P.L;
+#pragma unroll 1
+            for (int p0 = 0; p0 < npass; p0 += kKB) {
+              const int vb = rsub * npass + p0;  // first row of the batch
+              uint32_t o[kKB + 2];  // other sublattice, rows vb-1 .. vb+kKB (clamped to the copy of row 0)
+#pragma unroll
+              for (int j = 0; j < kKB + 2; ++j) o[j] = oth[min(vb - 1 + j, L) * Wr + tx];
+              // horizontal neighbour not at the same index: left for A on even
+              // rows and B on odd rows (PAisingMSC.cu:203, 238); alternates by row
+              const bool left0 = (hf == 0) == ((vb & 1) == 0);
+              uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+              uint32_t vm = 0;  // slots holding a site
+#pragma unroll
+              for (int k = 0; k < kKB; ++k) {
+                const int y = vb + k;
+                const bool valid = worker && p0 + k < npass && y < L;
+                const int row = min(y, L) * Wr;
+                const uint32_t s = self[row + tx];
+                const uint32_t side = oth[row + ((left0 != ((k & 1) != 0)) ? txl : txr)];
+                uint32_t s0, s1, s2;
+                adder4(s ^ side, s ^ o[k + 1], s ^ o[k], s ^ o[k + 2], s0, s1, s2);
+                av[k] = s0;
+                ac[k] = s1 | s2;
+                un[k] = valid ? ~(s1 | s2) : 0u;
+                vm |= valid ? 1u << k : 0u;
+                site[k] = base + (uint32_t)(row + tx);  // = group * h + word in the group
+              }
+              const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
+              accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0, P.T4, P.T8);
+#pragma unroll
+              for (int k = 0; k < kKB; ++k)
+                if (vm >> k & 1u) {
+                  const int y = vb + k;
+                  const uint32_t nw = self[y * Wr + tx] ^ ac[k];
+                  self[y * Wr + tx] = nw;
+                  if (y == 0) self[L * Wr + tx] = nw;         // copy below row L-1
+                  if (y == L - 1) self[-Wr + tx] = nw;        // copy above row 0
+                }
+            }
+          } else {
+            // stacked tiles: thread (rsub, tx) takes stacked rows rsub + pass*rpp
 #pragma unroll 1
             for (int p0 = 0; p0 < npass; p0 += kKB) {
               uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
@@ -280,25 +348,15 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
               for (int k = 0; k < kKB; ++k) {
                 const int pass = p0 + k;
                 const int v = rsub + pass * rpp;
-                const bool valid = worker && pass < npass && v < (kTiled ? vrows : P.L);
+                const bool valid = worker && pass < npass && v < vrows;
                 const int vc = valid ? v : 0;
-                int row, rowu, rowd;
-                if (kTiled) {
-                  const RowPos q = row_pos(vc);
-                  row = q.row;
-                  rowu = q.rowu;
-                  rowd = q.rowd;
-                } else {
-                  const int L = P.L;
-                  row = vc * Wr;
-                  rowu = (vc == 0 ? L - 1 : vc - 1) * Wr;
-                  rowd = (vc + 1 == L ? 0 : vc + 1) * Wr;
-                }
-                const int sidx = row + tx;
+                const RowPos q = row_pos(vc);
+                const int sidx = q.row + tx;
                 // row parity: stacked groups have even L, so v and y agree
                 const bool left = (hf == 0) == ((vc & 1) == 0);
                 const uint32_t s = self[sidx];
-                const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[sidx], n3 = oth[rowu + tx], n4 = oth[rowd + tx];
+                const uint32_t n1 = oth[q.row + (left ? txl : txr)], n2 = oth[sidx], n3 = oth[q.rowu + tx],
+                               n4 = oth[q.rowd + tx];
                 uint32_t s0, s1, s2;
                 adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
                 av[k] = s0;
@@ -313,9 +371,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
               for (int k = 0; k < kKB; ++k)
                 if (vm >> k & 1u) self[site[k] - base] ^= ac[k];
             }
-          };
-          if (G == 1) native_half(std::integral_constant<bool, false>());
-          else native_half(std::integral_constant<bool, true>());
+          }
         }
         __syncthreads();
       }
@@ -519,7 +575,7 @@ bool msc_geom(int L, SweepGeom* g, int tile, long long groups, int slots) {
   g->T = g->Wr * rpp;
   g->npass = npass;
   g->kconst = (g->half % kRefThreads == 0) ? g->half / kRefThreads : 0;
-  g->smem = best_G * g->N * 4;
+  g->smem = best_G == 1 ? (msc_halo_block(L, g->Wr) + (L + 2) * g->Wr) * 4 : best_G * g->N * 4;
   return true;
 }
 

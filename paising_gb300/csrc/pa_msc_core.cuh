@@ -150,12 +150,18 @@ __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t
   }
 }
 
+// One-group work units keep each sublattice in shared memory as L + 2 rows of
+// Wr words (row -1 and row L are periodic copies); sublattice B's block
+// starts at this word offset (A's block rounded up to 16 bytes).
+__host__ __device__ inline int msc_halo_block(int L, int Wr) { return ((L + 2) * Wr + 3) & ~3; }
+
 // Per-population parameters of the group a CTA is annealing.  They live in
 // shared memory and are read where used, which keeps the hot loops' register
 // footprint independent of how many populations the batch holds.
 struct UnitParams {
   int L, N, h, Wr, rpp, npass, kconst, step, sweeps, nbatch;
   int G, rg;                    // groups per tile, groups in the population
+  int sb;                       // one-group units: word offset of sublattice B's block in shared memory
   uint32_t invL, invWr, invH4;  // reciprocals (recip32) of L, Wr and h/4
   uint32_t tag, T4, T8;
   unsigned long long seed, iseq;
