@@ -182,9 +182,10 @@ static void thread_half(uint32_t* words, int L, int group0, int first_row, int n
  *           npass = ceil(G L / rpp); its batch of four passes p0 / 4 is chain
  *           (ti threads + tid) nbatch + p0 / 4;
  *   cs > 1: a cluster of cs CTAs per group; CTA `rank` updates rows
- *           [rank L/cs, (rank + 1) L/cs) with rpp the largest divisor of L/cs
- *           with (L/2) rpp <= threads; chain ((g cs + rank) threads + tid)
- *           nbatch + p0 / 4.
+ *           [rank L/cs, (rank + 1) L/cs), thread (rsub, tx) the consecutive
+ *           rows rank L/cs + rsub * npass + pass, with rpp the largest divisor
+ *           of L/cs with (L/2) rpp <= threads and npass = L/cs / rpp; chain
+ *           ((g cs + rank) threads + tid) nbatch + p0 / 4.
  * Within a half-sweep every update reads the other sublattice only, so the
  * order in which threads are visited does not matter.  Layout as the
  * reference's MSC Replica (PAisingMSC.cu:84-92): group g at words + g*N,
@@ -223,7 +224,7 @@ void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T
                         const uint32_t unit = cs > 1 ? (uint32_t)(g0 * cs + rank) : (uint32_t)u;
                         const uint32_t chain0 = (unit * (uint32_t)threads + (uint32_t)tid) * (uint32_t)nbatch;
                         const int first = cs > 1 ? rank * (L / cs) : 0, nrows = cs > 1 ? L / cs : gc * L;
-                        thread_half(words, L, g0, first, nrows, tid / Wr, tid % Wr, rpp, npass, cs <= 1 && G == 1,
+                        thread_half(words, L, g0, first, nrows, tid / Wr, tid % Wr, rpp, npass, cs > 1 || G == 1,
                                     hf, c1, chain0, key, step, tag, T4, T8);
                     }
             }

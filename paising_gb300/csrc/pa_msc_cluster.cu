@@ -205,36 +205,40 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
             if (valid) self[row + tx] = s ^ acc;
           }
         } else {
+          // thread rsub owns the consecutive stripe rows rsub*npass ..
+          // rsub*npass + npass - 1 of column tx: a batch of kKB rows shares
+          // the other sublattice's rows around them (halo rows included)
           const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
 #pragma unroll 1
           for (int p0 = 0; p0 < npass; p0 += kKB) {
+            const int vb = rsub * npass + p0;  // first stripe row of the batch
+            uint32_t o[kKB + 2];  // other sublattice, stripe rows vb-1 .. vb+kKB (clamped to the lower halo)
+#pragma unroll
+            for (int j = 0; j < kKB + 2; ++j) o[j] = oth[min(vb - 1 + j, LR) * Wr + tx];
+            const bool left0 = (hf == 0) == (((row0 + vb) & 1) == 0);  // alternates by row
             uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
-            int ix[kKB];
+            uint32_t vm = 0;  // slots holding a site
 #pragma unroll
             for (int k = 0; k < kKB; ++k) {
-              const int pass = p0 + k;
-              const int lr = rsub + pass * rpp;
-              const bool valid = worker && pass < npass && lr < LR;
-              const int lrc = valid ? lr : 0, ty = row0 + lrc;
-              const int row = lrc * Wr;
-              const bool left = (hf == 0) == ((ty & 1) == 0);
+              const int lr = vb + k;
+              const bool valid = worker && p0 + k < npass && lr < LR;
+              const int row = min(lr, LR) * Wr;
               const uint32_t s = self[row + tx];
-              const uint32_t n1 = oth[row + (left ? txl : txr)], n2 = oth[row + tx];
-              const uint32_t n3 = oth[row - Wr + tx], n4 = oth[row + Wr + tx];
+              const uint32_t side = oth[row + ((left0 != ((k & 1) != 0)) ? txl : txr)];
               uint32_t s0, s1, s2;
-              adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
+              adder4(s ^ side, s ^ o[k + 1], s ^ o[k], s ^ o[k + 2], s0, s1, s2);
               av[k] = s0;
               ac[k] = s1 | s2;
               un[k] = valid ? ~(s1 | s2) : 0u;
-              ix[k] = valid ? row + tx : -1;
-              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)(ty * Wr + tx);
+              vm |= valid ? 1u << k : 0u;
+              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)((row0 + lr) * Wr + tx);
             }
             const uint32_t chain =
                 (((uint32_t)gi * CS + (uint32_t)rank) * blockDim.x + (uint32_t)tid) * (uint32_t)P.nbatch + (uint32_t)(p0 / kKB);
             accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, npass - p0, P.T4, P.T8);
 #pragma unroll
             for (int k = 0; k < kKB; ++k)
-              if (ix[k] >= 0) self[ix[k]] ^= ac[k];
+              if (vm >> k & 1u) self[(vb + k) * Wr + tx] ^= ac[k];
           }
         }
         cluster.sync();
