@@ -22,8 +22,6 @@
 //
 // Work per tile and half-sweep: about 1024 words, four per thread, decided
 // together (kKB = 4).
-#include <type_traits>
-
 #include "pa_kernels.h"
 #include "pa_msc_core.cuh"
 
@@ -62,6 +60,7 @@ struct BitsParams {
   int L, N, h, S;          // lattice side, sites, sites per sublattice, sites per sublattice row
   int Wq, seg, segs, wpp;  // words per row, sites per segment, segments per word, words per plane of a word group
   int GW, G, R;            // word groups (of segs replicas) per tile, replicas per tile, replicas
+  int gs, r0;              // words per word group in shared memory, offset of its row 0 (see kFullStride)
   uint32_t invWpp, invWq;  // ceil(2^32 / wpp), ceil(2^32 / Wq) (Wq > 1)
   uint32_t M0, ML, V;      // first site of every segment, last site of every segment, all segment bits
   int step, sweeps;
@@ -70,6 +69,13 @@ struct BitsParams {
   int32_t* E;
   int32_t* M;
 };
+
+// L = 64 (one 32-site word per row, a replica per word group): a word
+// group's rows are a block of kFullStride words in shared memory, row y at
+// y + 1 and periodic copies of rows 63 and 0 at 0 and 65, so the sweep reads
+// vertical neighbours without wrapping; the stride is 1 modulo 32 so that
+// the 32 lanes of a warp -- 4 groups x 8 blocks of 4 rows -- hit 32 banks.
+constexpr int kFullStride = 97;
 
 // Row layout of L: Wq words of seg sites, segs = segments per word.
 __host__ __device__ inline bool bits_layout(int L, int* Wq, int* seg, int* segs) {
@@ -123,7 +129,7 @@ __device__ __noinline__ void bits_move(const BitsParams& P, uint32_t* pl, int ti
     const int X = it >= items ? 1 : 0;
     int g, wr, y, c;
     bits_split(P, it - X * items, g, wr, y, c);
-    uint32_t* word = pl + (X * P.GW + g) * P.wpp + wr;
+    uint32_t* word = pl + (X * P.GW + g) * P.gs + P.r0 + wr;
     uint32_t w = to_smem ? 0u : *word;
     for (int j = 0; j < P.segs; ++j) {
       const int rep = g * P.segs + j;
@@ -134,6 +140,16 @@ __device__ __noinline__ void bits_move(const BitsParams& P, uint32_t* pl, int ti
     }
     if (to_smem) *word = w;
   }
+  if (to_smem && P.r0) {  // periodic copies of the first and last rows (one word per row)
+    __syncthreads();
+    const int ng = items / P.wpp, L = P.L;
+    for (int it = threadIdx.x; it < 4 * ng; it += blockDim.x) {
+      const int X = it >= 2 * ng ? 1 : 0, r = it - X * 2 * ng, g = r >> 1, top = r & 1;
+      uint32_t* blk = pl + (X * P.GW + g) * P.gs;
+      if (top) blk[0] = blk[L];       // row -1 = row L-1
+      else blk[L + 1] = blk[1];       // row L = row 0
+    }
+  }
 }
 
 // anti-parallel bonds (each seen from its A end) and +1 sites of every
@@ -143,8 +159,8 @@ __device__ __noinline__ void bits_count(const BitsParams& P, const uint32_t* pl,
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     int g, wr, y, c;
     bits_split(P, it, g, wr, y, c);
-    const uint32_t* A = pl + g * P.wpp;
-    const uint32_t* B = pl + (P.GW + g) * P.wpp;
+    const uint32_t* A = pl + g * P.gs + P.r0;
+    const uint32_t* B = pl + (P.GW + g) * P.gs + P.r0;
     const uint32_t a = A[wr], ctr = B[wr];
     const uint32_t up = B[(y == 0 ? L - 1 : y - 1) * Wq + c], dn = B[(y + 1 == L ? 0 : y + 1) * Wq + c];
     const uint32_t side = bits_side(P, B, y * Wq, c, ctr, (y & 1) == 0);
@@ -204,7 +220,7 @@ bool ssc_bits_geom(int L, SweepGeom* g, int tile, long long replicas, int slots)
   g->rpp = 0;
   g->npass = (GW * wpp + kSweepThreads - 1) / kSweepThreads;  // words per thread per half-sweep
   g->kconst = 0;
-  g->smem = GW * 2 * wpp * 4;
+  g->smem = GW * 2 * (Wq == 1 && seg == 32 ? kFullStride : wpp) * 4;
   return true;
 }
 
@@ -243,6 +259,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.S = st->L >> 1;
         P.Wq = st->Wr; P.seg = st->seg; P.segs = P.Wq == 1 ? 32 / P.seg : 1;
         P.wpp = P.L * P.Wq;
+        P.r0 = P.Wq == 1 && P.seg == 32 ? 1 : 0;
+        P.gs = P.r0 ? kFullStride : P.wpp;
         P.G = st->gpt;
         P.GW = P.G / P.segs;
         P.R = st->R_cur;
@@ -279,12 +297,10 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
     bits_move(P, pl, ti, true);
     __syncthreads();
 
-    // one half-sweep over the words of plane `self`; kForm 0: one 32-site word
-    // per row (L = 64, rotations only), 1: any other layout
+    // one half-sweep over the words of plane `self` (every layout but L = 64's)
     {
     const int L = P.L, Wq = P.Wq, seg = P.seg, wpp = P.wpp, GW = P.GW, items = bits_items(P, ti);
-    auto half_sweep = [&](auto form_c, uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
-      constexpr int kForm = decltype(form_c)::value;
+    auto half_sweep = [&](uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
 #pragma unroll 1
       for (int q0 = 0; q0 * kSweepThreads < items; q0 += kKB) {
         uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
@@ -296,7 +312,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           const int itc = valid ? it : 0;
           const int g = (int)__umulhi((uint32_t)itc, P.invWpp), wr = itc - g * wpp;
           int y = wr, c = 0;
-          if (kForm == 1 && Wq > 1) {
+          if (Wq > 1) {
             y = (int)__umulhi((uint32_t)wr, P.invWq);
             c = wr - y * Wq;
           }
@@ -305,11 +321,10 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           const uint32_t s = self[base + wr];
           const uint32_t ctr = oth[base + wr], up = oth[base + rowu + c], dn = oth[base + rowd + c];
           const bool left = (hf == 0) == ((y & 1) == 0);
-          const uint32_t side = kForm == 0 ? (left ? __funnelshift_l(ctr, ctr, 1) : __funnelshift_r(ctr, ctr, 1))
-                                           : bits_side(P, oth + base, y * Wq, c, ctr, left);
+          const uint32_t side = bits_side(P, oth + base, y * Wq, c, ctr, left);
           uint32_t s0, s1, s2;
           adder4(s ^ ctr, s ^ side, s ^ up, s ^ dn, s0, s1, s2);
-          const uint32_t v = kForm == 0 ? 0xffffffffu : P.V;
+          const uint32_t v = P.V;
           av[k] = s0;
           ac[k] = (s1 | s2) & v;
           un[k] = valid ? ~(s1 | s2) & v : 0u;
@@ -324,16 +339,58 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           if (vm >> k & 1u) self[site[k] - (uint32_t)(ti * GW) * (uint32_t)wpp] ^= ac[k];
       }
     };
-    const bool full_word = Wq == 1 && seg == 32;  // block-uniform
+    // L = 64: thread (lane, warp) takes the 4 consecutive rows 4*(8*(warp/4) +
+    // lane%8) .. +3 of word group 4*(warp%4) + lane/8, so the 4 words share
+    // the other plane's rows around them (6 loads for 4 words); one batch per
+    // thread and half-sweep
+    auto half_full = [&](uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
+      const int lane = tid & 31, w = tid >> 5;
+      const int g = 4 * (w & 3) + (lane >> 3), y0 = 4 * (8 * (w >> 2) + (lane & 7));
+      const bool valid = g < items / wpp;  // word groups present in this tile
+      const int gc = valid ? g : 0;
+      const uint32_t* ob = oth + gc * kFullStride;  // row y of the other plane at ob[y + 1]
+      uint32_t* sb = self + gc * kFullStride + 1;    // row y of this plane at sb[y]
+      uint32_t o[kKB + 2];
+#pragma unroll
+      for (int j = 0; j < kKB + 2; ++j) o[j] = ob[y0 + j];  // rows y0-1 .. y0+4
+      uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+#pragma unroll
+      for (int k = 0; k < kKB; ++k) {
+        const uint32_t s = sb[y0 + k], ctr = o[k + 1];
+        // y0 is even: the other horizontal neighbour is x-1 for A on even rows
+        // and B on odd rows (PAisingSSC.cu:170,182), a rotation of the word
+        const bool left = (hf == 0) != ((k & 1) != 0);
+        const uint32_t side = left ? __funnelshift_l(ctr, ctr, 1) : __funnelshift_r(ctr, ctr, 1);
+        uint32_t s0, s1, s2;
+        adder4(s ^ ctr, s ^ side, s ^ o[k], s ^ o[k + 2], s0, s1, s2);
+        av[k] = s0;
+        ac[k] = s1 | s2;
+        un[k] = valid ? ~(s1 | s2) : 0u;
+        site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)(y0 + k);  // word number in the population
+      }
+      const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u;
+      accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, valid ? kKB : 0, P.T4, P.T8);
+      if (valid) {
+#pragma unroll
+        for (int k = 0; k < kKB; ++k) {
+          const int y = y0 + k;
+          const uint32_t nw = sb[y] ^ ac[k];
+          sb[y] = nw;
+          if (y == 0) sb[L] = nw;       // copy below row L-1
+          if (y == L - 1) sb[-1] = nw;  // copy above row 0
+        }
+      }
+    };
+    const bool full_word = Wq == 1 && seg == 32;  // block-uniform (L = 64)
     const int sweeps = P.sweeps;
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
       for (int hf = 0; hf < 2; ++hf) {
-        uint32_t* self = pl + hf * GW * wpp;
-        const uint32_t* oth = pl + (1 - hf) * GW * wpp;
+        uint32_t* self = pl + hf * GW * P.gs;
+        const uint32_t* oth = pl + (1 - hf) * GW * P.gs;
         const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
-        if (full_word) half_sweep(std::integral_constant<int, 0>(), self, oth, hf, c1);
-        else half_sweep(std::integral_constant<int, 1>(), self, oth, hf, c1);
+        if (full_word) half_full(self, oth, hf, c1);
+        else half_sweep(self, oth, hf, c1);
         __syncthreads();
       }
     }

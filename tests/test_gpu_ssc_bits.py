@@ -116,16 +116,22 @@ def test_bits_segments_free_energy_vs_kaufman(cuda, oracle, L):
 def test_bits_sweep_matches_int8_sweep_statistically(cuda, oracle):
     """L=64, R=20000, 20 sweeps, dbeta=0.01: the bit-plane sweep and the
     int8 sweep (sweep_variant=1) both stay within 2e-4 of the exact betaF/N
-    and agree with each other in E/N at every beta."""
+    at every beta, and within 1e-2 of the exact E/N, with no bias: their mean
+    deviation over the schedule is below 5e-4.  (With 20 sweeps the largest
+    deviations sit at beta_c = 0.44, where two independent runs differ by
+    about 1e-2.)"""
     out = []
     for variant in (0, 1):
         with pa.Engine(L=64, R=20000, sweeps=20, dbeta=0.01, coding="ssc", seed=21, sweep_variant=variant) as e:
             e.run()
             out.append(e.rows(0))
-    exact = np.array([-oracle.kaufman(64, b)[0] / 4096 for b in out[0][:, 0]])
+    ex = [oracle.kaufman(64, b) for b in out[0][:, 0]]
+    bf = np.array([-x[0] / 4096 for x in ex])
+    en = np.array([x[1] / 4096 for x in ex])
     for r in out:
-        assert np.max(np.abs(r[:, 6] - exact)) < 2e-4
-    assert np.max(np.abs(out[0][1:, 1] - out[1][1:, 1])) < 5e-3
+        assert np.max(np.abs(r[:, 6] - bf)) < 2e-4
+        dev = r[1:, 1] - en[1:]
+        assert np.max(np.abs(dev)) < 1e-2 and abs(dev.mean()) < 5e-4, (np.max(np.abs(dev)), dev.mean())
 
 
 def test_bits_batch_and_invariants(cuda):
