@@ -293,18 +293,20 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         } else {
           const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
           const uint32_t base = (uint32_t)gi0 * (uint32_t)h;  // site number of the tile's first word
-          if (G == 1 && P.L == 64) {
-            // L = 64 with every size fixed at compile time: a row is 32 words,
-            // so warp rsub is the 8 rows rsub*8 .. rsub*8+7 and tx its lane;
-            // a batch is 4 of those rows and every offset an immediate
-            constexpr int kL = 64, kW = 32;
-            const int vb0 = rsub * 8;
+          // L = 64 and 128 with every size fixed at compile time: kW = L/2
+          // words per row, kR = kSweepThreads/kW thread rows of kL/kR
+          // consecutive rows each (64: a warp per row, 8 rows per thread; 128:
+          // two warps per row, 32 rows per thread); every offset an immediate
+          auto native_fixed = [&](auto l_c) {
+            constexpr int kL = decltype(l_c)::value, kW = kL / 2, kR = kSweepThreads / kW, kRows = kL / kR;
+            static_assert(kRows % kKB == 0, "whole batches");
+            const int vb0 = rsub * kRows;
             const uint32_t* txs = oth + (hf == 0 ? txl : txr);  // side neighbour on even rows
             const uint32_t* txo = oth + (hf == 0 ? txr : txl);  // and on odd rows
 #pragma unroll 1
-            for (int p0 = 0; p0 < 8; p0 += kKB) {
+            for (int p0 = 0; p0 < kRows; p0 += kKB) {
               const int vb = vb0 + p0;
-              const uint32_t* po = oth + (vb - 1) * kW + tx;  // rows vb-1 .. vb+4 (row -1 and 64: copies)
+              const uint32_t* po = oth + (vb - 1) * kW + tx;  // rows vb-1 .. vb+4 (rows -1 and kL: copies)
               uint32_t* ps = self + vb * kW + tx;
               uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
 #pragma unroll
@@ -318,16 +320,22 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 un[k] = ~(s1 | s2);
                 site[k] = base + (uint32_t)((vb + k) * kW + tx);
               }
-              const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 2u + (uint32_t)(p0 / kKB);
+              const uint32_t chain =
+                  ((uint32_t)ti * blockDim.x + (uint32_t)tid) * (uint32_t)(kRows / kKB) + (uint32_t)(p0 / kKB);
               accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, kKB, P.T4, P.T8);
 #pragma unroll
               for (int k = 0; k < kKB; ++k) {
                 const uint32_t nw = ps[k * kW] ^ ac[k];
                 ps[k * kW] = nw;
-                if (vb + k == 0) self[kL * kW + tx] = nw;         // copy below row 63
+                if (vb + k == 0) self[kL * kW + tx] = nw;         // copy below row kL-1
                 if (vb + k == kL - 1) self[-kW + tx] = nw;        // copy above row 0
               }
             }
+          };
+          if (G == 1 && P.L == 64) {
+            native_fixed(std::integral_constant<int, 64>());
+          } else if (G == 1 && P.L == 128) {
+            native_fixed(std::integral_constant<int, 128>());
           } else if (G == 1) {
             // one group (the common L >= 64 case): thread rsub owns the
             // consecutive rows rsub*npass .. rsub*npass + npass - 1 of column
