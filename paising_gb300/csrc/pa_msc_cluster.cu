@@ -204,6 +204,41 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
             const uint32_t acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
             if (valid) self[row + tx] = s ^ acc;
           }
+        } else if (P.L == 256) {
+          // L = 256 with every size fixed at compile time: rows of 128 words,
+          // THREADS/128 thread rows of kRows consecutive stripe rows each,
+          // every offset an immediate (same batches as the general form below)
+          constexpr int kW = 128, kLR = 256 / CS, kRpp = THREADS / kW, kRows = kLR / kRpp;
+          static_assert(kLR % kRpp == 0 && kRows % kKB == 0, "whole batches");
+          const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+          const int vb0 = rsub * kRows;
+          // stripes and batches start on even rows: the side neighbour of
+          // even rows is x-1 for A, x+1 for B (PAisingMSC.cu:203, 238)
+          const uint32_t* txs = oth + (hf == 0 ? txl : txr);
+          const uint32_t* txo = oth + (hf == 0 ? txr : txl);
+#pragma unroll 1
+          for (int p0 = 0; p0 < kRows; p0 += kKB) {
+            const int vb = vb0 + p0;
+            const uint32_t* po = oth + (vb - 1) * kW + tx;  // stripe rows vb-1 .. vb+4 (halos included)
+            uint32_t* ps = self + vb * kW + tx;
+            uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+#pragma unroll
+            for (int k = 0; k < kKB; ++k) {
+              const uint32_t s = ps[k * kW];
+              const uint32_t side = ((k & 1) ? txo : txs)[(vb + k) * kW];
+              uint32_t s0, s1, s2;
+              adder4(s ^ side, s ^ po[(k + 1) * kW], s ^ po[k * kW], s ^ po[(k + 2) * kW], s0, s1, s2);
+              av[k] = s0;
+              ac[k] = s1 | s2;
+              un[k] = ~(s1 | s2);
+              site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)((row0 + vb + k) * kW + tx);
+            }
+            const uint32_t chain = (((uint32_t)gi * CS + (uint32_t)rank) * blockDim.x + (uint32_t)tid) *
+                                       (uint32_t)(kRows / kKB) + (uint32_t)(p0 / kKB);
+            accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, kKB, P.T4, P.T8);
+#pragma unroll
+            for (int k = 0; k < kKB; ++k) ps[k * kW] ^= ac[k];
+          }
         } else {
           // thread rsub owns the consecutive stripe rows rsub*npass ..
           // rsub*npass + npass - 1 of column tx: a batch of kKB rows shares
