@@ -128,7 +128,9 @@ PA_API int pa_create_batch(const pa_config* cfgs, int n, pa_handle** out);
 
 /* Runs the handle's anneals (beta from 0 while beta <= beta_final), the
  * population-annealing loop of main() (PAisingSSC.cu:481-664,
- * PAisingMSC.cu:640-814). */
+ * PAisingMSC.cu:640-814).  Each call is a new run: the subsequence counter
+ * continues, and with the native stream the run number enters every sweep
+ * draw's counter, so repeated calls give independent runs. */
 PA_API int pa_run(pa_handle* h);
 
 /* A run stepped from the host, for hosts that interleave their own work or
