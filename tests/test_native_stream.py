@@ -101,7 +101,8 @@ def test_msc_sweep_native_stream_bit_exact(cuda, st, oracle, L, R, sweeps, beta)
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("graph", [True, False])
-@pytest.mark.parametrize("L,R,sweeps,dbeta", [(16, 200, 5, 0.05), (24, 700, 3, 0.1), (64, 1000, 4, 0.1)])
+@pytest.mark.parametrize("L,R,sweeps,dbeta", [(16, 200, 5, 0.05), (24, 700, 3, 0.1), (64, 1000, 4, 0.1),
+                                              (96, 100, 2, 0.2), (128, 64, 2, 0.2)])
 def test_msc_anneal_native_stream_two_runs(cuda, oracle, graph, L, R, sweeps, dbeta):
     """Whole anneals with the production stream: two runs of one handle
     (one-CTA sweep, one group per work unit, FP64 weights) equal the oracle's
@@ -122,7 +123,8 @@ def test_msc_anneal_native_stream_two_runs(cuda, oracle, graph, L, R, sweeps, db
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,R,tile", [(16, 300, 2), (16, 1000, 8), (32, 500, 4), (24, 400, 2), (32, 900, 8)])
+@pytest.mark.parametrize("L,R,tile", [(16, 300, 2), (16, 1000, 8), (32, 500, 4), (24, 400, 2), (32, 900, 8),
+                                      (64, 200, 2)])
 def test_msc_anneal_native_stream_stacked_tiles(cuda, oracle, L, R, tile):
     """Stacked tiles (several groups per work unit of the one-CTA sweep, the
     last tile short where the group count is not a multiple): every batch of
