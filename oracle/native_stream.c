@@ -254,9 +254,11 @@ void or_msc_sweep_native(uint32_t* words, int L, int rg, int sweeps, uint32_t T4
  * Half-sweep: 256 threads; word it = tid + 256 q of the tile's plane goes to
  * thread tid, four words (q = q0..q0+3) per batch, batch chain
  * (tile 256 + tid) 8 + q0/4; word-site number (tile G/segs + word group) wpp
- * + word of the group.  L = 64 (one 32-site word per row) instead: thread
- * tid = 32 w + lane takes the rows 4 (8 (w / 4) + lane % 8) .. + 3 of word
- * group 4 (w % 4) + lane / 8 as its one batch, chain (tile 256 + tid) 8.
+ * + word of the group.  L = 64 and 128 (rows of Wq = 1 or 2 full 32-site
+ * words) instead: with GM = 1024 / (L Wq) and RL = 8 / Wq, thread
+ * tid = 32 w + lane, lane = (gl RL + rl) Wq + c, takes word column c of rows
+ * 4 (RL (w / (GM/4)) + rl) .. + 3 of word group 4 (w % (GM/4)) + gl as its
+ * one batch, chain (tile 256 + tid) 8.
  * ------------------------------------------------------------------------- */
 static int bits_layout_c(int L, int* Wq, int* seg, int* segs) {
     if (L < 8 || L % 8 != 0 || L > 256) return 0;
@@ -288,7 +290,7 @@ int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T
         for (int sw = 0; sw < sweeps; ++sw)
             for (int hf = 0; hf < 2; ++hf) {
                 const uint32_t c1 = (uint32_t)(sw * 2 + hf) << 4;
-                const int full = Wq == 1 && seg == 32;
+                const int full = seg == 32 && (Wq == 1 || Wq == 2);
                 for (int tid = 0; tid < 256; ++tid)
                     for (int q0 = 0; q0 * 256 < (full ? 1 : items); q0 += 4) {
                         uint32_t a[4] = {0}, und[4] = {0}, acc[4] = {0}, site[4] = {0};
@@ -296,8 +298,10 @@ int or_ssc_sweep_bits_native(int8_t* spins, int L, int R, int sweeps, uint32_t T
                         for (int k = 0; k < 4; ++k) {
                             int it = tid + (q0 + k) * 256;
                             if (full) {
-                                const int w = tid / 32, lane = tid % 32, gg = 4 * (w % 4) + lane / 8;
-                                it = gg < ngroups ? gg * wpp + 4 * (8 * (w / 4) + lane % 8) + k : items;
+                                const int GM = 1024 / (L * Wq), RL = 8 / Wq, w = tid / 32, lane = tid % 32;
+                                const int cc = lane % Wq, gl = lane / Wq / RL, rl = lane / Wq % RL;
+                                const int gg = 4 * (w % (GM / 4)) + gl, y0 = 4 * (RL * (w / (GM / 4)) + rl);
+                                it = gg < ngroups ? gg * wpp + (y0 + k) * Wq + cc : items;
                             }
                             if (it >= items) continue;
                             const int g = it / wpp, wr = it % wpp, y = wr / Wq, c = wr % Wq;

@@ -22,6 +22,8 @@
 //
 // Work per tile and half-sweep: about 1024 words, four per thread, decided
 // together (kKB = 4).
+#include <type_traits>
+
 #include "pa_kernels.h"
 #include "pa_msc_core.cuh"
 
@@ -60,7 +62,7 @@ struct BitsParams {
   int L, N, h, S;          // lattice side, sites, sites per sublattice, sites per sublattice row
   int Wq, seg, segs, wpp;  // words per row, sites per segment, segments per word, words per plane of a word group
   int GW, G, R;            // word groups (of segs replicas) per tile, replicas per tile, replicas
-  int gs, r0;              // words per word group in shared memory, offset of its row 0 (see kFullStride)
+  int gs, r0;              // words per word group in shared memory, offset of its row 0 (see full_stride)
   uint32_t invWpp, invWq;  // ceil(2^32 / wpp), ceil(2^32 / Wq) (Wq > 1)
   uint32_t M0, ML, V;      // first site of every segment, last site of every segment, all segment bits
   int step, sweeps;
@@ -70,12 +72,17 @@ struct BitsParams {
   int32_t* M;
 };
 
-// L = 64 (one 32-site word per row, a replica per word group): a word
-// group's rows are a block of kFullStride words in shared memory, row y at
-// y + 1 and periodic copies of rows 63 and 0 at 0 and 65, so the sweep reads
-// vertical neighbours without wrapping; the stride is 1 modulo 32 so that
-// the 32 lanes of a warp -- 4 groups x 8 blocks of 4 rows -- hit 32 banks.
-constexpr int kFullStride = 97;
+// L = 64 and 128 (rows of Wq = 1 or 2 full 32-site words, a replica per word
+// group): a word group's rows are a block of full_stride(Wq) words in shared
+// memory, row y at (y + 1) Wq and periodic copies of rows L-1 and 0 before
+// and after, so the sweep reads vertical neighbours without wrapping.  The
+// stride is Wq modulo 32 so that the 32 lanes of a warp -- 4 groups x 32/(4 Wq)
+// blocks of 4 rows x Wq words -- hit 32 different banks.
+__host__ __device__ constexpr bool full_rows(int Wq, int seg) { return seg == 32 && (Wq == 1 || Wq == 2); }
+__host__ __device__ constexpr int full_stride(int Wq) {
+  return ((64 * Wq + 2) * Wq + 31 - Wq) / 32 * 32 + Wq;  // >= (L + 2) Wq, = Wq mod 32
+}
+static_assert(full_stride(1) == 97 && full_stride(2) == 290, "strides");
 
 // Row layout of L: Wq words of seg sites, segs = segments per word.
 __host__ __device__ inline bool bits_layout(int L, int* Wq, int* seg, int* segs) {
@@ -140,14 +147,14 @@ __device__ __noinline__ void bits_move(const BitsParams& P, uint32_t* pl, int ti
     }
     if (to_smem) *word = w;
   }
-  if (to_smem && P.r0) {  // periodic copies of the first and last rows (one word per row)
+  if (to_smem && P.r0) {  // periodic copies of the first and last rows
     __syncthreads();
-    const int ng = items / P.wpp, L = P.L;
-    for (int it = threadIdx.x; it < 4 * ng; it += blockDim.x) {
-      const int X = it >= 2 * ng ? 1 : 0, r = it - X * 2 * ng, g = r >> 1, top = r & 1;
+    const int ng = items / P.wpp, L = P.L, Wq = P.Wq;
+    for (int it = threadIdx.x; it < 4 * ng * Wq; it += blockDim.x) {
+      const int c = it % Wq, r = it / Wq, X = r >= 2 * ng ? 1 : 0, q = r - X * 2 * ng, g = q >> 1, top = q & 1;
       uint32_t* blk = pl + (X * P.GW + g) * P.gs;
-      if (top) blk[0] = blk[L];       // row -1 = row L-1
-      else blk[L + 1] = blk[1];       // row L = row 0
+      if (top) blk[c] = blk[L * Wq + c];                 // row -1 = row L-1
+      else blk[(L + 1) * Wq + c] = blk[Wq + c];          // row L = row 0
     }
   }
 }
@@ -220,7 +227,7 @@ bool ssc_bits_geom(int L, SweepGeom* g, int tile, long long replicas, int slots)
   g->rpp = 0;
   g->npass = (GW * wpp + kSweepThreads - 1) / kSweepThreads;  // words per thread per half-sweep
   g->kconst = 0;
-  g->smem = GW * 2 * (Wq == 1 && seg == 32 ? kFullStride : wpp) * 4;
+  g->smem = GW * 2 * (full_rows(Wq, seg) ? full_stride(Wq) : wpp) * 4;
   return true;
 }
 
@@ -259,8 +266,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         P.L = st->L; P.N = st->N; P.h = st->N >> 1; P.S = st->L >> 1;
         P.Wq = st->Wr; P.seg = st->seg; P.segs = P.Wq == 1 ? 32 / P.seg : 1;
         P.wpp = P.L * P.Wq;
-        P.r0 = P.Wq == 1 && P.seg == 32 ? 1 : 0;
-        P.gs = P.r0 ? kFullStride : P.wpp;
+        P.r0 = full_rows(P.Wq, P.seg) ? P.Wq : 0;
+        P.gs = P.r0 ? full_stride(P.Wq) : P.wpp;
         P.G = st->gpt;
         P.GW = P.G / P.segs;
         P.R = st->R_cur;
@@ -339,34 +346,47 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           if (vm >> k & 1u) self[site[k] - (uint32_t)(ti * GW) * (uint32_t)wpp] ^= ac[k];
       }
     };
-    // L = 64: thread (lane, warp) takes the 4 consecutive rows 4*(8*(warp/4) +
-    // lane%8) .. +3 of word group 4*(warp%4) + lane/8, so the 4 words share
-    // the other plane's rows around them (6 loads for 4 words); one batch per
-    // thread and half-sweep
-    auto half_full = [&](uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
+    // L = 64, 128 (rows of kWq full words): lane = (gl * kRL + rl) * kWq + c of
+    // warp w takes the 4 consecutive rows 4 rb .. 4 rb + 3, rb = kRL (w / (kGW/4))
+    // + rl, of word column c of word group 4 (w % (kGW/4)) + gl, so the 4 words
+    // share the other plane's rows around them (6 loads for 4 words, plus the
+    // row's other word for the horizontal neighbour when kWq = 2); one batch
+    // per thread and half-sweep
+    auto half_full = [&](auto wq_c, uint32_t* self, const uint32_t* oth, int hf, uint32_t c1) {
+      constexpr int kWq = decltype(wq_c)::value, kL = 64 * kWq, kGW = 1024 / (kL * kWq), kRL = 8 / kWq;
+      constexpr int kS = full_stride(kWq);
+      static_assert(kGW % 4 == 0 && (kGW / 4) * (kL / 4 / kRL) * 32 == kSweepThreads, "one batch per thread");
       const int lane = tid & 31, w = tid >> 5;
-      const int g = 4 * (w & 3) + (lane >> 3), y0 = 4 * (8 * (w >> 2) + (lane & 7));
+      const int c = lane % kWq, gl = (lane / kWq) / kRL, rl = (lane / kWq) % kRL;
+      const int g = 4 * (w % (kGW / 4)) + gl, y0 = 4 * (kRL * (w / (kGW / 4)) + rl);
       const bool valid = g < items / wpp;  // word groups present in this tile
       const int gc = valid ? g : 0;
-      const uint32_t* ob = oth + gc * kFullStride;  // row y of the other plane at ob[y + 1]
-      uint32_t* sb = self + gc * kFullStride + 1;    // row y of this plane at sb[y]
+      const uint32_t* ob = oth + gc * kS + c;  // word c of row y of the other plane at ob[(y + 1) kWq]
+      uint32_t* sb = self + gc * kS + kWq + c;  // and of this plane at sb[y kWq]
       uint32_t o[kKB + 2];
 #pragma unroll
-      for (int j = 0; j < kKB + 2; ++j) o[j] = ob[y0 + j];  // rows y0-1 .. y0+4
+      for (int j = 0; j < kKB + 2; ++j) o[j] = ob[(y0 + j) * kWq];  // rows y0-1 .. y0+4
       uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
 #pragma unroll
       for (int k = 0; k < kKB; ++k) {
-        const uint32_t s = sb[y0 + k], ctr = o[k + 1];
+        const uint32_t s = sb[(y0 + k) * kWq], ctr = o[k + 1];
         // y0 is even: the other horizontal neighbour is x-1 for A on even rows
-        // and B on odd rows (PAisingSSC.cu:170,182), a rotation of the word
+        // and B on odd rows (PAisingSSC.cu:170,182): the word shifted by one
+        // site, the site leaving it taken from the row's other word
         const bool left = (hf == 0) != ((k & 1) != 0);
-        const uint32_t side = left ? __funnelshift_l(ctr, ctr, 1) : __funnelshift_r(ctr, ctr, 1);
+        uint32_t side;
+        if constexpr (kWq == 1) {
+          side = left ? __funnelshift_l(ctr, ctr, 1) : __funnelshift_r(ctr, ctr, 1);
+        } else {
+          const uint32_t other = ob[(y0 + k + 1) * kWq + (c ^ 1) - c];
+          side = left ? __funnelshift_l(other, ctr, 1) : __funnelshift_r(ctr, other, 1);
+        }
         uint32_t s0, s1, s2;
         adder4(s ^ ctr, s ^ side, s ^ o[k], s ^ o[k + 2], s0, s1, s2);
         av[k] = s0;
         ac[k] = s1 | s2;
         un[k] = valid ? ~(s1 | s2) : 0u;
-        site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)(y0 + k);  // word number in the population
+        site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)((y0 + k) * kWq + c);  // word number
       }
       const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u;
       accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, valid ? kKB : 0, P.T4, P.T8);
@@ -374,14 +394,14 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 #pragma unroll
         for (int k = 0; k < kKB; ++k) {
           const int y = y0 + k;
-          const uint32_t nw = sb[y] ^ ac[k];
-          sb[y] = nw;
-          if (y == 0) sb[L] = nw;       // copy below row L-1
-          if (y == L - 1) sb[-1] = nw;  // copy above row 0
+          const uint32_t nw = sb[y * kWq] ^ ac[k];
+          sb[y * kWq] = nw;
+          if (y == 0) sb[kL * kWq] = nw;       // copy below row L-1
+          if (y == kL - 1) sb[-kWq] = nw;      // copy above row 0
         }
       }
     };
-    const bool full_word = Wq == 1 && seg == 32;  // block-uniform (L = 64)
+    const bool full_word = full_rows(Wq, seg);  // block-uniform (L = 64 or 128)
     const int sweeps = P.sweeps;
     for (int sw = 0; sw < sweeps; ++sw) {
 #pragma unroll 1
@@ -389,7 +409,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         uint32_t* self = pl + hf * GW * P.gs;
         const uint32_t* oth = pl + (1 - hf) * GW * P.gs;
         const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
-        if (full_word) half_full(self, oth, hf, c1);
+        if (full_word && Wq == 1) half_full(std::integral_constant<int, 1>(), self, oth, hf, c1);
+        else if (full_word) half_full(std::integral_constant<int, 2>(), self, oth, hf, c1);
         else half_sweep(self, oth, hf, c1);
         __syncthreads();
       }
