@@ -494,6 +494,10 @@ struct pa_handle {
             status = PA_ERR_TOO_MANY_STEPS;
             err = "number of temperature steps exceeds nBmax=10000 (raise R or lower min_overlap)";
             break;
+          case kErrSweepForm:
+            status = PA_ERR_STATE;
+            err = "sweep kernel built for another lattice size";
+            break;
           default:
             status = PA_ERR_CAPACITY;
             err = "population exceeded its buffer capacity (raise pa_config.capacity)";
@@ -536,12 +540,26 @@ struct pa_handle {
 
   // Persistent sweep grid for the populations' current geometry and, in
   // graph mode, the run captured as one graph (again, after a re-tune).
+  // The lattice size of a sweep kernel built for one size, when every
+  // population of the handle can use it (MSC, one group per work unit, one L).
+  int fixed_l(const std::vector<SweepGeom>& geo) const {
+    if (coding != PA_CODING_MSC || cs != 1 || rng_mode != PA_RNG_NATIVE || geo.empty()) return 0;
+    const int l = msc_fixed_l(geo[0].L, geo[0].G);
+    for (const auto& g : geo)
+      if (msc_fixed_l(g.L, g.G) != l) return 0;
+    return l;
+  }
+
   cudaError_t setup_launches() {
     int max_smem = 0;
-    for (const auto& P : pops) max_smem = std::max(max_smem, P.geom.smem);
+    std::vector<SweepGeom> geo;
+    for (const auto& P : pops) {
+      max_smem = std::max(max_smem, P.geom.smem);
+      geo.push_back(P.geom);
+    }
     cudaError_t e = ssc_bits ? ssc_bits_setup(max_smem, &sweep)
                     : cs > 1 ? msc_cluster_setup(cs, rng_mode, max_smem, &sweep)
-                             : sweep_setup(coding, rng_mode, max_smem, &sweep);
+                             : sweep_setup(coding, rng_mode, max_smem, &sweep, fixed_l(geo));
     if (e != cudaSuccess || !graph) return e;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph_t) cudaGraphDestroy(graph_t);
@@ -592,7 +610,7 @@ struct pa_handle {
     }
     cudaError_t e = upload_pops(hp);
     SweepLaunch sl{};
-    if (e == cudaSuccess) e = bits ? ssc_bits_setup(smem, &sl) : sweep_setup(coding, rng_mode, smem, &sl);
+    if (e == cudaSuccess) e = bits ? ssc_bits_setup(smem, &sl) : sweep_setup(coding, rng_mode, smem, &sl, fixed_l(geo));
     float best = 0.f;
     for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {  // the first launch warms up
       e = launch_plan(d_batch, npop, 0, stream);

@@ -46,9 +46,15 @@ void geom_to_pop(const SweepGeom& g, PopDev* h);
 
 struct SweepLaunch {
   int grid, block, smem;
+  int fixed_l;  // MSC, native stream: L of a kernel built for that one size (96), else 0
 };
 // Persistent grid for a sweep kernel with `smem` bytes of dynamic shared memory.
-cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out);
+// fixed_l (MSC, native stream): every population of the launch has this L and
+// one group per work unit, and a kernel built for that size alone is used.
+cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out, int fixed_l = 0);
+// The fixed_l for MSC populations of lattice size L and G groups per work unit
+// (0 where no kernel is built for it).
+int msc_fixed_l(int L, int G);
 
 // Work plan of the next sweep launch: unit counts of the populations that
 // take part (energy_only: populations at step 0), prefix sums, queue reset.
@@ -71,7 +77,7 @@ cudaError_t launch_resample(BatchDev* b, int coding, cudaStream_t s);
 
 // Coding-specific launchers behind the generic ones above.
 cudaError_t ssc_sweep_setup(int rng_mode, int smem, SweepLaunch* out);
-cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out);
+cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out, int fixed_l);
 cudaError_t launch_ssc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
                              const SweepLaunch& sl, cudaStream_t s);
 cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,

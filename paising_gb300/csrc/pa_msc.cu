@@ -158,7 +158,12 @@ __device__ __noinline__ void msc_count(const UnitParams& P, const uint32_t* lat,
 }
 
 static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the tile, bit) in the epilogue");
-template <int MODE>
+// FL != 0 (native stream only): a kernel for populations of lattice size FL
+// with one group per work unit, holding that size's compile-time sweep alone.
+// Built for L = 96 only: the general kernel (FL = 0) carries the compile-time
+// forms of L = 64 and 128, measured as fast there as kernels of their own,
+// while adding L = 96's form to it cost L = 64 1% (register allocation).
+template <int MODE, int FL>
 __global__ void __launch_bounds__(kSweepThreads, 4)
     msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
   extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
@@ -293,19 +298,27 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
         } else {
           const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
           const uint32_t base = (uint32_t)gi0 * (uint32_t)h;  // site number of the tile's first word
-          // L = 64 and 128 with every size fixed at compile time: kW = L/2
-          // words per row, kR = kSweepThreads/kW thread rows of kL/kR
-          // consecutive rows each (64: a warp per row, 8 rows per thread; 128:
-          // two warps per row, 32 rows per thread); every offset an immediate
+          // L = 64, 96 and 128 with every size fixed at compile time: kW = L/2
+          // words per row, kR = kSweepThreads/kW thread rows of kRows =
+          // ceil(kL/kR) consecutive rows each (64: a warp per row, 8 rows per
+          // thread; 96: 5 x 20 rows, the last batch of the fifth thread row
+          // past the lattice; 128: two warps per row, 32 rows per thread);
+          // every offset an immediate.  Same batches as the general form.
           auto native_fixed = [&](auto l_c) {
-            constexpr int kL = decltype(l_c)::value, kW = kL / 2, kR = kSweepThreads / kW, kRows = kL / kR;
-            static_assert(kRows % kKB == 0, "whole batches");
+            constexpr int kL = decltype(l_c)::value, kW = kL / 2, kR = kSweepThreads / kW;
+            constexpr int kRows = (kL + kR - 1) / kR;
+            static_assert(kRows % kKB == 0 && (kR * kRows - kL) % kKB == 0, "whole batches, each in or past the lattice");
             const int vb0 = rsub * kRows;
             const uint32_t* txs = oth + (hf == 0 ? txl : txr);  // side neighbour on even rows
             const uint32_t* txo = oth + (hf == 0 ? txr : txl);  // and on odd rows
 #pragma unroll 1
             for (int p0 = 0; p0 < kRows; p0 += kKB) {
-              const int vb = vb0 + p0;
+              // a batch past the lattice (or of a thread without a column)
+              // reads rows 0..3 and decides nothing, but takes part in the
+              // warp's acceptance
+              constexpr bool kAll = kR * kW == kSweepThreads && kR * kRows == kL;  // every batch of every thread
+              const bool bvalid = kAll || (worker && vb0 + p0 < kL);
+              const int vb = bvalid ? vb0 + p0 : 0;
               const uint32_t* po = oth + (vb - 1) * kW + tx;  // rows vb-1 .. vb+4 (rows -1 and kL: copies)
               uint32_t* ps = self + vb * kW + tx;
               uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
@@ -317,22 +330,30 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 adder4(s ^ side, s ^ po[(k + 1) * kW], s ^ po[k * kW], s ^ po[(k + 2) * kW], s0, s1, s2);
                 av[k] = s0;
                 ac[k] = s1 | s2;
-                un[k] = ~(s1 | s2);
+                un[k] = bvalid ? ~(s1 | s2) : 0u;
                 site[k] = base + (uint32_t)((vb + k) * kW + tx);
               }
               const uint32_t chain =
                   ((uint32_t)ti * blockDim.x + (uint32_t)tid) * (uint32_t)(kRows / kKB) + (uint32_t)(p0 / kKB);
               accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, kKB, P.T4, P.T8);
+              if (bvalid) {
 #pragma unroll
-              for (int k = 0; k < kKB; ++k) {
-                const uint32_t nw = ps[k * kW] ^ ac[k];
-                ps[k * kW] = nw;
-                if (vb + k == 0) self[kL * kW + tx] = nw;         // copy below row kL-1
-                if (vb + k == kL - 1) self[-kW + tx] = nw;        // copy above row 0
+                for (int k = 0; k < kKB; ++k) {
+                  const uint32_t nw = ps[k * kW] ^ ac[k];
+                  ps[k * kW] = nw;
+                  if (vb + k == 0) self[kL * kW + tx] = nw;         // copy below row kL-1
+                  if (vb + k == kL - 1) self[-kW + tx] = nw;        // copy above row 0
+                }
               }
             }
           };
-          if (G == 1 && P.L == 64) {
+          if constexpr (FL != 0) {
+            if (G == 1 && P.L == FL) {  // block-uniform; anything else is a host error, recorded below
+              native_fixed(std::integral_constant<int, FL>());
+            } else if (tid == 0 && sw == 0 && hf == 0) {
+              b->pops[p].error = kErrSweepForm;
+            }
+          } else if (G == 1 && P.L == 64) {
             native_fixed(std::integral_constant<int, 64>());
           } else if (G == 1 && P.L == 128) {
             native_fixed(std::integral_constant<int, 128>());
@@ -623,20 +644,30 @@ bool msc_geom(int L, SweepGeom* g, int tile, long long groups, int slots) {
 }
 
 // -------------------------------------------------------------- launchers
-static const void* msc_sweep_fn(int rng_mode) {
-  return rng_mode == kRefCoords ? (const void*)msc_sweep_kernel<kRefCoords> : (const void*)msc_sweep_kernel<kNative>;
+int msc_fixed_l(int L, int G) { return G == 1 && L == 96 ? L : 0; }
+
+static const void* msc_sweep_fn(int rng_mode, int fixed_l) {
+  if (rng_mode == kRefCoords) return (const void*)msc_sweep_kernel<kRefCoords, 0>;
+  return fixed_l == 96 ? (const void*)msc_sweep_kernel<kNative, 96> : (const void*)msc_sweep_kernel<kNative, 0>;
 }
 
-cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out) {
-  return persistent_launch(msc_sweep_fn(rng_mode), kSweepThreads, smem, out);
+cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out, int fixed_l) {
+  if (rng_mode == kRefCoords || msc_fixed_l(fixed_l, 1) != fixed_l) fixed_l = 0;
+  cudaError_t e = persistent_launch(msc_sweep_fn(rng_mode, fixed_l), kSweepThreads, smem, out);
+  out->fixed_l = fixed_l;
+  return e;
 }
 
 cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
                              const SweepLaunch& sl, cudaStream_t s) {
-  if (rng_mode == kRefCoords)
-    msc_sweep_kernel<kRefCoords><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
-  else
-    msc_sweep_kernel<kNative><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+  if (rng_mode == kRefCoords) {
+    msc_sweep_kernel<kRefCoords, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+  } else {
+    if (sl.fixed_l == 96)
+      msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+    else
+      msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+  }
   return cudaGetLastError();
 }
 

@@ -563,8 +563,9 @@ void geom_to_pop(const SweepGeom& g, PopDev* h) {
   h->invWr = recip32(g.Wr);
 }
 
-cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out) {
-  return coding == kMSC ? msc_sweep_setup(rng_mode, smem, out) : ssc_sweep_setup(rng_mode, smem, out);
+cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out, int fixed_l) {
+  out->fixed_l = 0;
+  return coding == kMSC ? msc_sweep_setup(rng_mode, smem, out, fixed_l) : ssc_sweep_setup(rng_mode, smem, out);
 }
 
 cudaError_t launch_plan(BatchDev* b, int npop, int energy_only, cudaStream_t s) {

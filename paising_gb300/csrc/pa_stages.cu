@@ -97,7 +97,9 @@ int sweep_stage(int coding, void* spins, uint8_t* active, int L, int units, int 
   SweepGeom g;
   if (bits ? !ssc_bits_geom(L, &g) : coding == kMSC ? !msc_geom(L, &g) : !ssc_geom(L, &g)) return PA_ERR_ARG;
   SweepLaunch sl;
-  cudaError_t e = bits ? ssc_bits_setup(g.smem, &sl) : sweep_setup(coding, rng_mode, g.smem, &sl);
+  cudaError_t e = bits ? ssc_bits_setup(g.smem, &sl)
+                       : sweep_setup(coding, rng_mode, g.smem, &sl,
+                                     coding == kMSC && rng_mode == PA_RNG_NATIVE ? msc_fixed_l(g.L, g.G) : 0);
   if (e != cudaSuccess) return stage_fail(e, "sweep setup");
   Scratch S;
   if ((e = S.alloc()) != cudaSuccess) return stage_fail(e, "scratch");

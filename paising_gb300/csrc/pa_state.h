@@ -99,6 +99,7 @@ constexpr int kRecMhr = 1, kRecEnergies = 2;
 constexpr int kNBmax = 10000;  // nBmax, PAisingSSC.cu:57: rows of a schedule at most
 // error codes in PopDev::error
 constexpr int kErrCapacity = 1, kErrExtinct = 2, kErrTooManySteps = 3;
+constexpr int kErrSweepForm = 4;  // a sweep kernel built for one lattice size met another (a host bug)
 
 // Populations advancing together.  unit_prefix[p] .. unit_prefix[p+1]-1 are
 // the sweep work units (SSC replicas, MSC groups) of population p in the
