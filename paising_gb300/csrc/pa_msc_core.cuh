@@ -51,8 +51,11 @@ __device__ __forceinline__ void finish_bit(uint32_t w, uint32_t am, uint32_t t4,
                                            uint32_t& lt) {
   const uint32_t b = und & (0u - und);
   const uint32_t t = (am & b) ? t4 : t8;
-  lt |= (w >> 8) < t ? b : 0u;
-  und ^= b;
+  // b is a bit of und and not yet of lt: the updates are additions, which
+  // the FMA pipe can take (the sweep's logic operations keep the ALU pipe
+  // the busier one)
+  lt += (w >> 8) < t ? b : 0u;
+  und -= b;
 }
 
 // Tag of the words that finish single bits (finish_bit): the sweep's tag with
@@ -132,9 +135,9 @@ __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t
     uint32_t r = 0;
     while (r < 32u && (m & __funnelshift_l(und[k], und[k], r))) ++r;
     rot[k] = r;
-    if (r < 32u) {
-      m |= __funnelshift_l(und[k], und[k], r);
-      am |= __funnelshift_l(a[k] & und[k], a[k] & und[k], r);
+    if (r < 32u) {  // disjoint from the bits merged so far: additions, on the FMA pipe
+      m += __funnelshift_l(und[k], und[k], r);
+      am += __funnelshift_l(a[k] & und[k], a[k] & und[k], r);
     } else {
       ovf |= 1u << k;
     }
