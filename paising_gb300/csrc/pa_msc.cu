@@ -329,8 +329,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 uint32_t s0, s1, s2;
                 adder4(s ^ side, s ^ po[(k + 1) * kW], s ^ po[k * kW], s ^ po[(k + 2) * kW], s0, s1, s2);
                 av[k] = s0;
-                ac[k] = s1 | s2;
-                un[k] = bvalid ? ~(s1 | s2) : 0u;
+                ac[k] = s1 + s2;                             // = s1 | s2: never both set
+                un[k] = bvalid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac: both on the FMA pipe
                 site[k] = base + (uint32_t)((vb + k) * kW + tx);
               }
               const uint32_t chain =

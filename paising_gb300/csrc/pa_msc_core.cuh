@@ -45,7 +45,8 @@ __device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, ui
 // The last undecided bits of a comparison word: their first 8 digits equal
 // T's, so U < T/2^32 is decided by the remaining 24 digits at once,
 // U mod 2^24 < T mod 2^24, with one fresh 32-bit word w per bit (its top 24
-// bits are U's remaining digits).  Takes the lowest undecided bit; a no-op
+// bits are U's remaining digits): w < (T mod 2^24) * 2^8, compared against
+// t4 = T4 << 8 and t8 = T8 << 8.  Takes the lowest undecided bit; a no-op
 // when none is left.
 __device__ __forceinline__ void finish_bit(uint32_t w, uint32_t am, uint32_t t4, uint32_t t8, uint32_t& und,
                                            uint32_t& lt) {
@@ -54,7 +55,7 @@ __device__ __forceinline__ void finish_bit(uint32_t w, uint32_t am, uint32_t t4,
   // b is a bit of und and not yet of lt: the updates are additions, which
   // the FMA pipe can take (the sweep's logic operations keep the ALU pipe
   // the busier one)
-  lt += (w >> 8) < t ? b : 0u;
+  lt += w < t ? b : 0u;
   und -= b;
 }
 
@@ -80,7 +81,7 @@ __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uin
     digit_step(r.z, am, dig[6], und, lt);
     digit_step(r.w, am, dig[7], und, lt);
   }
-  const uint32_t t4 = T4 & 0xFFFFFFu, t8 = T8 & 0xFFFFFFu, ftag = tag ^ kFinishTagFlip;
+  const uint32_t t4 = T4 << 8, t8 = T8 << 8, ftag = tag ^ kFinishTagFlip;
 #pragma unroll 1
   for (uint32_t k = 0; k < 8u; ++k) {
     if (!__any_sync(kFull, und != 0u)) break;
