@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
   extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
   __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMaxTile * kMsb], s_cntM[kMaxTile * kMsb];  // [group of the tile][bit]
-  __shared__ uint2 s_dig[kMsb];  // per digit j: (D8_j, D4_j ^ D8_j)
+  __shared__ uint2 s_dig[kMsb];  // per digit j: digit_table(T4, T8, j)
   __shared__ UnitParams P;
   __shared__ BitStats stats;
 
@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       txl = (tx == 0 ? Wr - 1 : tx - 1);
       txr = (tx + 1 == Wr ? 0 : tx + 1);
       if (tid < kMsb) {
-        const uint32_t d4 = 0u - ((P.T4 >> (31 - tid)) & 1u), d8 = 0u - ((P.T8 >> (31 - tid)) & 1u);
-        s_dig[tid] = make_uint2(d8, d4 ^ d8);
+        s_dig[tid] = digit_table(P.T4, P.T8, tid);
       }
     }
     const int N = P.N, h = P.h, G = P.G, gi0 = ti * G;

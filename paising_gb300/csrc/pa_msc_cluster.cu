@@ -147,8 +147,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
       txl = (tx == 0 ? Wr - 1 : tx - 1);
       txr = (tx + 1 == Wr ? 0 : tx + 1);
       if (tid < kMsb) {
-        const uint32_t d4 = 0u - ((P.T4 >> (31 - tid)) & 1u), d8 = 0u - ((P.T8 >> (31 - tid)) & 1u);
-        s_dig[tid] = make_uint2(d8, d4 ^ d8);
+        s_dig[tid] = digit_table(P.T4, P.T8, tid);
       }
     }
     // stripe of a sublattice in shared memory: halo row, LR rows, halo row

@@ -31,15 +31,26 @@ __device__ __forceinline__ void adder4(uint32_t I1, uint32_t I2, uint32_t I3, ui
 // One binary digit of the comparison U < T/2^32 done for 32 bits at once:
 // U's digit j is bit i of the random word u for replica bit i, T's digit j
 // is selected per bit from T4 (bits in s0: one anti-parallel neighbour,
-// dE = 4) or T8 (no anti-parallel neighbour, dE = 8).  dg = (D8_j, D4_j ^ D8_j)
-// with D_j = all ones iff digit j of the threshold is 1.  Bits decided at this
-// digit leave `und` (a subtraction, since they are a subset of it); those
-// decided "less" enter `lt`.
+// dE = 4) or T8 (no anti-parallel neighbour, dE = 8).  dg = digit_table(j)
+// gives that selection as one multiply-add, p = s0 * dg.x + dg.y (see
+// digit_table).  Bits decided at this digit leave `und` (a subtraction, since
+// they are a subset of it); those decided "less" enter `lt`.  The
+// multiply-add and the subtraction issue on the FMA pipe, leaving the ALU
+// pipe -- the sweep's busiest -- two logic operations per digit.
 __device__ __forceinline__ void digit_step(uint32_t u, uint32_t s0, uint2 dg, uint32_t& und, uint32_t& lt) {
-  const uint32_t p = (s0 & dg.y) ^ dg.x;
+  const uint32_t p = s0 * dg.x + dg.y;
   const uint32_t dec = und & (p ^ u);
   lt |= dec & p;
   und -= dec;
+}
+
+// Digit j of the thresholds T4, T8 as (m, c) with s0 * m + c = the bits'
+// threshold digits: T4's digit where s0 is set, T8's elsewhere.  With D = all
+// ones iff the digit is 1: both digits equal -> (0, D8); T4's 1, T8's 0 ->
+// (1, 0) = s0; T4's 0, T8's 1 -> (-1, ~0) = ~s0.
+__host__ __device__ inline uint2 digit_table(uint32_t T4, uint32_t T8, int j) {
+  const uint32_t b4 = (T4 >> (31 - j)) & 1u, b8 = (T8 >> (31 - j)) & 1u;
+  return make_uint2(b4 == b8 ? 0u : b4 ? 1u : 0xFFFFFFFFu, 0u - b8);
 }
 
 // The last undecided bits of a comparison word: their first 8 digits equal

@@ -297,8 +297,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       if (tid < kMsb && cur >= 0) stats.flush(b->pops + cur, tid);
       cur = p;
       if (tid < kMsb) {
-        const uint32_t d4 = 0u - ((P.T4 >> (31 - tid)) & 1u), d8 = 0u - ((P.T8 >> (31 - tid)) & 1u);
-        s_dig[tid] = make_uint2(d8, d4 ^ d8);
+        s_dig[tid] = digit_table(P.T4, P.T8, tid);
       }
     }
     bits_move(P, pl, ti, true);
