@@ -325,11 +325,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
               for (int k = 0; k < kKB; ++k) {
                 const uint32_t s = ps[k * kW];
                 const uint32_t side = ((k & 1) ? txo : txs)[(vb + k) * kW];
-                uint32_t s0, s1, s2;
-                adder4(s ^ side, s ^ po[(k + 1) * kW], s ^ po[k * kW], s ^ po[(k + 2) * kW], s0, s1, s2);
-                av[k] = s0;
-                ac[k] = s1 + s2;                             // = s1 | s2: never both set
-                un[k] = bvalid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac: both on the FMA pipe
+                count_masks(s, side, po[(k + 1) * kW], po[k * kW], po[(k + 2) * kW], av[k], ac[k]);
+                un[k] = bvalid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac, on the FMA pipe
                 site[k] = base + (uint32_t)((vb + k) * kW + tx);
               }
               const uint32_t chain =

@@ -28,6 +28,20 @@ __device__ __forceinline__ void adder4(uint32_t I1, uint32_t I2, uint32_t I3, ui
   s2 = a12 & a34;
 }
 
+// The two masks the acceptance needs from a word's four neighbour words:
+// odd = an odd number of anti-parallel neighbours (among undecided bits: one,
+// threshold T4), ge2 = two or more (dE <= 0: flipped outright) -- adder4's s0
+// and s1 | s2, in fewer logic operations: the XOR of two neighbours does not
+// depend on the spin itself, and "two or more" is a pair within either half
+// or one in each.
+__device__ __forceinline__ void count_masks(uint32_t s, uint32_t n1, uint32_t n2, uint32_t n3, uint32_t n4,
+                                            uint32_t& odd, uint32_t& ge2) {
+  const uint32_t x12 = n1 ^ n2, x34 = n3 ^ n4;
+  const uint32_t a12 = (s ^ n1) & (s ^ n2), a34 = (s ^ n3) & (s ^ n4);
+  odd = x12 ^ x34;
+  ge2 = a12 | a34 | (x12 & x34);
+}
+
 // One binary digit of the comparison U < T/2^32 done for 32 bits at once:
 // U's digit j is bit i of the random word u for replica bit i, T's digit j
 // is selected per bit from T4 (bits in s0: one anti-parallel neighbour,

@@ -380,11 +380,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           const uint32_t other = ob[(y0 + k + 1) * kWq + (c ^ 1) - c];
           side = left ? __funnelshift_l(other, ctr, 1) : __funnelshift_r(ctr, other, 1);
         }
-        uint32_t s0, s1, s2;
-        adder4(s ^ ctr, s ^ side, s ^ o[k], s ^ o[k + 2], s0, s1, s2);
-        av[k] = s0;
-        ac[k] = s1 + s2;                            // = s1 | s2: never both set
-        un[k] = valid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac: both on the FMA pipe
+        count_masks(s, ctr, side, o[k], o[k + 2], av[k], ac[k]);
+        un[k] = valid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac, on the FMA pipe
         site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)((y0 + k) * kWq + c);  // word number
       }
       const uint32_t chain = ((uint32_t)ti * blockDim.x + (uint32_t)tid) * 8u;
