@@ -378,11 +378,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 const int row = min(y, L) * Wr;
                 const uint32_t s = self[row + tx];
                 const uint32_t side = oth[row + ((left0 != ((k & 1) != 0)) ? txl : txr)];
-                uint32_t s0, s1, s2;
-                adder4(s ^ side, s ^ o[k + 1], s ^ o[k], s ^ o[k + 2], s0, s1, s2);
-                av[k] = s0;
-                ac[k] = s1 | s2;
-                un[k] = valid ? ~(s1 | s2) : 0u;
+                count_masks(s, side, o[k + 1], o[k], o[k + 2], av[k], ac[k]);
+                un[k] = valid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac, on the FMA pipe
                 vm |= valid ? 1u << k : 0u;
                 site[k] = base + (uint32_t)(row + tx);  // = group * h + word in the group
               }
@@ -417,11 +414,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
                 const uint32_t s = self[sidx];
                 const uint32_t n1 = oth[q.row + (left ? txl : txr)], n2 = oth[sidx], n3 = oth[q.rowu + tx],
                                n4 = oth[q.rowd + tx];
-                uint32_t s0, s1, s2;
-                adder4(s ^ n1, s ^ n2, s ^ n3, s ^ n4, s0, s1, s2);
-                av[k] = s0;
-                ac[k] = s1 | s2;
-                un[k] = valid ? ~(s1 | s2) : 0u;
+                count_masks(s, n1, n2, n3, n4, av[k], ac[k]);
+                un[k] = valid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac, on the FMA pipe
                 vm |= valid ? 1u << k : 0u;
                 site[k] = base + (uint32_t)sidx;  // = group * h + word in the group
               }

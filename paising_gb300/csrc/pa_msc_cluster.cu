@@ -256,11 +256,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
               const int row = min(lr, LR) * Wr;
               const uint32_t s = self[row + tx];
               const uint32_t side = oth[row + ((left0 != ((k & 1) != 0)) ? txl : txr)];
-              uint32_t s0, s1, s2;
-              adder4(s ^ side, s ^ o[k + 1], s ^ o[k], s ^ o[k + 2], s0, s1, s2);
-              av[k] = s0;
-              ac[k] = s1 | s2;
-              un[k] = valid ? ~(s1 | s2) : 0u;
+              count_masks(s, side, o[k + 1], o[k], o[k + 2], av[k], ac[k]);
+              un[k] = valid ? 0xFFFFFFFFu - ac[k] : 0u;  // = ~ac, on the FMA pipe
               vm |= valid ? 1u << k : 0u;
               site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)((row0 + lr) * Wr + tx);
             }

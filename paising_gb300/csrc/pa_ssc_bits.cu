@@ -328,12 +328,12 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           const uint32_t ctr = oth[base + wr], up = oth[base + rowu + c], dn = oth[base + rowd + c];
           const bool left = (hf == 0) == ((y & 1) == 0);
           const uint32_t side = bits_side(P, oth + base, y * Wq, c, ctr, left);
-          uint32_t s0, s1, s2;
-          adder4(s ^ ctr, s ^ side, s ^ up, s ^ dn, s0, s1, s2);
-          const uint32_t v = P.V;
-          av[k] = s0;
-          ac[k] = (s1 | s2) & v;
-          un[k] = valid ? ~(s1 | s2) & v : 0u;
+          uint32_t odd, ge2;
+          count_masks(s, ctr, side, up, dn, odd, ge2);
+          const uint32_t v = P.V;  // the bits of the word's segments
+          av[k] = odd;
+          ac[k] = ge2 & v;
+          un[k] = valid ? v - ac[k] : 0u;  // = ~ge2 & v, on the FMA pipe
           vm |= valid ? 1u << k : 0u;
           site[k] = (uint32_t)(ti * GW + g) * (uint32_t)wpp + (uint32_t)wr;  // word number in the population
         }
