@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
           } else if (G == 1 && P.L == 128) {
             native_fixed(std::integral_constant<int, 128>());
           } else if (G == 1) {
-            // one group (the common L >= 64 case): thread rsub owns the
+            // one group, any other L: thread rsub owns the
             // consecutive rows rsub*npass .. rsub*npass + npass - 1 of column
             // tx, so a batch of kKB rows shares the other sublattice's rows
             // around them, and the periodic copies of rows -1 and L spare the
