@@ -61,7 +61,11 @@ __global__ void msc_init_kernel(PopDev* pops) {
 // resident in shared memory as all G sublattices A, then all G sublattices B
 // (so the tile is one stack of G*L sublattice rows of Wr words; a row's
 // vertical neighbours wrap inside its own group).  Thread (rsub, tx) owns
-// word column tx of stacked rows rsub, rsub+rpp, ...
+// word column tx of stacked rows rsub, rsub+rpp, ...; with one group per
+// tile (G = 1) in the native stream it owns the consecutive rows
+// rsub*npass .. rsub*npass + npass - 1 instead, and each sublattice carries
+// periodic copies of rows -1 and L (msc_move_tile), so that a batch of four
+// rows shares its six rows of the other sublattice and nothing wraps.
 //
 // MODE kRefCoords: decisions of checkKerALL exactly -- one draw per word-site
 //   (ctr = sw*2K + hf*K + k of subsequence iseq + t + 128 g) expanded to 32

@@ -21,7 +21,10 @@
 // segments.  The tile is unpacked and written back once per temperature.
 //
 // Work per tile and half-sweep: about 1024 words, four per thread, decided
-// together (kKB = 4).
+// together (kKB = 4).  L = 64 and 128 (rows of one or two full words) have a
+// form of their own (half_full): a thread takes four consecutive rows of one
+// replica's word column, and the word groups carry periodic copies of rows -1
+// and L, padded to a bank-conflict-free stride (full_stride).
 #include <type_traits>
 
 #include "pa_kernels.h"
