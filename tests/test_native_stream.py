@@ -183,7 +183,7 @@ def test_ssc_sweep_bits_native_stream_bit_exact(cuda, st, oracle, L, R, beta):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,R", [(16, 1000), (24, 500), (64, 700)])
+@pytest.mark.parametrize("L,R", [(16, 1000), (24, 500), (64, 700), (128, 300)])
 def test_ssc_anneal_native_stream_bit_planes(cuda, oracle, L, R):
     """Whole SSC anneals on bit planes (the engine's automatic tile, two runs
     of one handle, FP64 weights) equal the oracle's anneal with the same
