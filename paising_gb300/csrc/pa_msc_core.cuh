@@ -171,11 +171,14 @@ __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t
   const uint32_t lt = finish_digits(m, am, chain_c0, c1, 1u, 0u, step, tag, K, dig, T4, T8);
   acc[0] |= lt & und[0];
 #pragma unroll
-  for (int k = 1; k < kKB; ++k) {
+  for (int k = 1; k < kKB; ++k)
     if (!(ovf >> k & 1u)) acc[k] |= __funnelshift_r(lt, lt, rot[k]) & und[k];
-    if (__any_sync(kFull, ovf >> k & 1u))
-      acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, 8u, step, tag, K,
-                              dig, T4, T8);
+  if (__any_sync(kFull, ovf != 0u)) {  // rare: one vote for the three sites
+#pragma unroll
+    for (int k = 1; k < kKB; ++k)
+      if (__any_sync(kFull, ovf >> k & 1u))
+        acc[k] |= finish_digits((ovf >> k & 1u) ? und[k] : 0u, a[k] & und[k], site[k], c1, 8u, 8u, step, tag, K,
+                                dig, T4, T8);
   }
 }
 
