@@ -97,8 +97,10 @@ constexpr uint32_t kFinishTagFlip = 0x20u << 24;
 __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub,
                                                   uint32_t fsub, uint32_t step, uint32_t tag, const PhiloxKeys& K,
                                                   const uint2* dig, uint32_t T4, uint32_t T8) {
+  // no vote first: some lane of the warp nearly always has undecided bits
+  // here (and the overflow path only calls when one has); a lane without
+  // them is left unchanged by every step below
   uint32_t lt = 0;
-  if (!__any_sync(kFull, und != 0u)) return lt;
   {
     const U4 r = philox10k(c0, c1 | sub, step, tag, K);
     digit_step(r.x, am, dig[4], und, lt);
