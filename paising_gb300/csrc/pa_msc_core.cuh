@@ -109,9 +109,11 @@ __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uin
     digit_step(r.w, am, dig[7], und, lt);
   }
   const uint32_t t4 = T4 << 8, t8 = T8 << 8, ftag = tag ^ kFinishTagFlip;
+  // the first block without a vote either: nearly every warp has a lane with
+  // a bit left after digit 7
 #pragma unroll 1
   for (uint32_t k = 0; k < 8u; ++k) {
-    if (!__any_sync(kFull, und != 0u)) break;
+    if (k > 0 && !__any_sync(kFull, und != 0u)) break;
     const U4 r = philox10k(c0, c1 | (fsub + k), step, ftag, K);
     finish_bit(r.x, am, t4, t8, und, lt);
     finish_bit(r.y, am, t4, t8, und, lt);
