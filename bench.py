@@ -52,7 +52,8 @@ def parse_args(argv=None):
     ap.add_argument("--dbeta", type=float, default=0.005)
     ap.add_argument("--beta-final", type=float, default=1.0)
     ap.add_argument("--graph", type=int, default=1)
-    ap.add_argument("--cpu-sample-steps", type=int, default=4, help="temperatures in the CPU baseline sample")
+    ap.add_argument("--cpu-sample-steps", type=int, default=12,
+                    help="temperatures in the CPU baseline sample (about 10 s of CPU work on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     return ap.parse_args(argv)
