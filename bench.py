@@ -11,8 +11,9 @@ metric is the reference's own (PAisingSSC.cu:632,806):
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference runs the reference's own CUDA program (PAisingMSC.cu built
-with cuRAND by oracle/ref_build.py) on the same GPU and reports its own
-timing.  Under torchrun with N > 1 each rank anneals its own populations
+with cuRAND by oracle/ref_build.py) on the same GPU, the same number of
+populations per step (its -M flag), and reports its own timing; the SSC
+program's figure rides along as "other_coding".  Under torchrun with N > 1 each rank anneals its own populations
 (replicas only; the path has no data-parallel exchange) and rank 0 prints.
 """
 from __future__ import annotations
@@ -158,6 +159,13 @@ def reduce_over_ranks(dist, device, elapsed: float, attempts: float):
 
 
 # ------------------------------------------------------------- our engine
+def engine_kwargs(a, seed: int, device: int) -> dict:
+    """The timed engine: P populations of the workload in one launch
+    sequence, native stream, FP32-compensated weights, CUDA graph."""
+    return dict(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=a.populations,
+                seed=seed, coding=a.coding, rng="native", weights="fp32", graph=bool(a.graph), device=device)
+
+
 def cpu_baseline(a) -> dict:
     """The oracle (C restatement of the reference's MSC/SSC loop, OpenMP over
     replicas) on this host's cores, over the first few temperatures of the
@@ -184,9 +192,7 @@ def run_ours(a):
     dev = lrank
     torch.cuda.set_device(dev)
     P = a.populations
-    eng = pa.Engine(L=a.L, R=a.R, sweeps=a.sweeps, dbeta=a.dbeta, beta_final=a.beta_final, runs=P,
-                    seed=rank_seed(rank), coding=a.coding, rng="native", weights="fp32", graph=bool(a.graph),
-                    device=dev)
+    eng = pa.Engine(**engine_kwargs(a, rank_seed(rank), dev))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")  # > L2 (129 MB)
     for _ in range(a.warmup):
         eng.run()
@@ -347,7 +353,8 @@ def profile_leg(a, eng, pa) -> dict:
     ssc_bits = a.coding == "ssc" and eng.sweep_form(0)["spins_per_word"] == 32
     ops_per_attempt = 5.0 if a.coding == "msc" or ssc_bits else 33.0
     achieved = attempts_per_launch * ops_per_attempt / (avg_ms * 1e-3) / 1e12
-    peaks = pa.probe_int_issue(eng.config.device)
+    from bench_probe import build as probe
+    peaks = probe.probe_int_issue(eng.config.device)
     peak = max(peaks) / 1e12
     workload = f"L{a.L}_R{a.R}_sw{a.sweeps}"
     return {
@@ -366,58 +373,90 @@ def profile_leg(a, eng, pa) -> dict:
 
 
 # -------------------------------------------------------- reference program
+def _reference_binary(prog: str, L: int):
+    """oracle/_ref/bin/PAising<prog>_L<L>_curand, built from the patched
+    reference sources when missing; (path, None) or (None, why)."""
+    from oracle import ref_build
+    binp = os.path.join(ROOT, "oracle", "_ref", "bin", f"PAising{prog}_L{L}_curand")
+    if not os.path.exists(binp):
+        try:
+            ref_build.main(["--sizes", str(L)])
+        except Exception as ex:  # noqa: BLE001
+            return None, f"reference build failed: {str(ex)[:200]}"
+    if not os.path.exists(binp):
+        return None, f"reference sources for L={L} not present"
+    return binp, None
+
+
+def _reference_once(binp: str, a, seed: int, runs: int):
+    """One invocation of the reference program: `runs` populations one after
+    the other (its -M flag); (elapsed s, spin-flip attempts) as it reports
+    them (PAisingMSC.cu:956-957: Elapsed time, Time per spin-flip over the
+    attempts of all runs)."""
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([binp, "-R", str(a.R), "-t", str(a.sweeps), "-d", str(a.dbeta), "-f",
+                            str(a.beta_final), "-s", str(seed), "-M", str(runs), "-o", d],
+                           capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout[-500:] + r.stderr[-500:])
+    el = float(re.search(r"Elapsed time:\s*([0-9.eE+-]+)", r.stdout).group(1))
+    tpf = float(re.search(r"Time per spin-flip:\s*([0-9.eE+-]+)", r.stdout).group(1))
+    return el, el * 1e9 / tpf
+
+
 def run_reference(a):
+    """The reference's own CUDA program on the same GPU and workload: each
+    step is one invocation annealing the same number of populations as our
+    batch, one after the other (-M populations), timed by the program itself.
+    The other coding's program is timed once on one population as an extra
+    figure."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    from oracle import ref_build
     prog = "MSC" if a.coding == "msc" else "SSC"
-    binp = os.path.join(ROOT, "oracle", "_ref", "bin", f"PAising{prog}_L{a.L}_curand")
-    if not os.path.exists(binp):
-        try:
-            ref_build.main(["--sizes", str(a.L)])
-        except Exception as ex:  # noqa: BLE001
-            return {"impl": "reference", "unavailable": f"reference build failed: {str(ex)[:200]}"}
-    if not os.path.exists(binp):
-        return {"impl": "reference", "unavailable": f"reference sources for L={a.L} not present"}
-
-    def once(seed):
-        with tempfile.TemporaryDirectory() as d:
-            r = subprocess.run([binp, "-R", str(a.R), "-t", str(a.sweeps), "-d", str(a.dbeta), "-f",
-                                str(a.beta_final), "-s", str(seed), "-o", d], capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(r.stdout[-500:] + r.stderr[-500:])
-        el = float(re.search(r"Elapsed time:\s*([0-9.eE+-]+)", r.stdout).group(1))
-        tpf = float(re.search(r"Time per spin-flip:\s*([0-9.eE+-]+)", r.stdout).group(1))
-        return el, tpf
-
+    binp, why = _reference_binary(prog, a.L)
+    if binp is None:
+        return {"impl": "reference", "unavailable": why}
+    P = a.populations
     for w in range(a.warmup):
-        once(1 + w)
-    els, tpfs = [], []
+        _reference_once(binp, a, 1 + w, 1)
+    els, atts = [], []
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for k in range(a.steps):
-            el, tpf = once(100 + k)
+            el, att = _reference_once(binp, a, 100 + k, P)
             els.append(el)
-            tpfs.append(tpf)
-    # attempts/ns over all steps = total attempts / total ns
-    att = sum(el * 1e9 / tpf for el, tpf in zip(els, tpfs))
-    value = att / (sum(els) * 1e9)
-    sample = f"PAising{prog}.cu (L={a.L}, MSbits=32) built with cuRAND, full anneal per step, " \
+            atts.append(att)
+    value = sum(atts) / (sum(els) * 1e9)
+    sample = f"PAising{prog}.cu (L={a.L}, MSbits=32) built with cuRAND, {P} population(s) per step (-M {P}), " \
              "timed by the program's own CUDA events (Elapsed time / Time per spin-flip)"
-    return {
+    out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * sum(els) / len(els), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 bit-planes" if a.coding == "msc" else "i8 spins",
         "data": "synthetic (random initial spins from the seed, cuRAND Philox)",
-        "config": {"workload": f"reference PAising{prog} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} "
-                               f"beta 0->{a.beta_final}, 1 population", "L": a.L, "R": a.R, "sweeps": a.sweeps,
-                   "dbeta": a.dbeta, "coding": a.coding, "parallelism": "single GPU"},
+        "config": {"workload": f"PA anneal {prog} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} beta 0->"
+                               f"{a.beta_final}, {P} population(s) per step (reference -M {P}: one after the "
+                               "other)", "L": a.L, "R": a.R, "sweeps": a.sweeps, "dbeta": a.dbeta,
+                   "beta_final": a.beta_final, "coding": a.coding, "populations_per_launch": P,
+                   "parallelism": "single GPU"},
         "full_anneal_s": sum(els) / len(els),
+        "full_anneal_s_per_population": sum(els) / len(els) / P,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
                          "sample": sample + " (GPU program; one host thread drives it)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "clocks": clk.summary(),
     }
+    if not a.no_plain:
+        other = "SSC" if prog == "MSC" else "MSC"
+        ob, why = _reference_binary(other, a.L)
+        if ob is None:
+            out["other_coding"] = {"coding": other.lower(), "unavailable": why}
+        else:
+            el, att = _reference_once(ob, a, 100, 1)
+            out["other_coding"] = {"coding": other.lower(), "value": att / (el * 1e9), "unit": UNIT,
+                                   "full_anneal_s": el, "populations": 1,
+                                   "program": f"PAising{other}.cu built with cuRAND (one population)"}
+    return out
 
 
 def main(argv=None) -> int:

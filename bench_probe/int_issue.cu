@@ -1,4 +1,5 @@
-// pa_probe.cu -- integer-issue throughput probe.
+// int_issue.cu -- integer-issue throughput probe of the benchmark (not part
+// of the engine library): bench.py loads it as bench_probe/_build/libintissue.so.
 //
 // The sweeps are bound by the SM's integer pipes (no memory or tensor-core
 // work in the inner loop), so their roofline denominator is the rate at
@@ -10,9 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-
-#include "../../include/paising.h"
-#include "pa_error.h"
+#include <cstdio>
 
 namespace {
 
@@ -49,9 +48,10 @@ __global__ void __launch_bounds__(256) int_issue_probe(uint32_t* out, uint32_t k
 extern "C" {
 
 // lane_ops_per_s[0] = LOP3 only (ALU pipe), [1] = IMAD only (FMA pipe),
-// [2] = alternating LOP3 / IMAD (both integer pipes).
-int pa_probe_int_issue(int device, double* lane_ops_per_s) {
-  if (!lane_ops_per_s) return PA_ERR_ARG;
+// [2] = alternating LOP3 / IMAD (both integer pipes).  Returns 0, or 1 for a
+// null argument, 2 for a CUDA error (message on stderr).
+__attribute__((visibility("default"))) int probe_int_issue(int device, double* lane_ops_per_s) {
+  if (!lane_ops_per_s) return 1;
   cudaError_t e = cudaSetDevice(device);
   int nsm = 0;
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
@@ -81,10 +81,10 @@ int pa_probe_int_issue(int device, double* lane_ops_per_s) {
   if (e1) cudaEventDestroy(e1);
   if (buf) cudaFree(buf);
   if (e != cudaSuccess) {
-    pa::g_last_error = std::string("int issue probe: ") + cudaGetErrorString(e);
-    return PA_ERR_CUDA;
+    std::fprintf(stderr, "int issue probe: %s\n", cudaGetErrorString(e));
+    return 2;
   }
-  return PA_OK;
+  return 0;
 }
 
 }  // extern "C"

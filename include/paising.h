@@ -149,9 +149,21 @@ PA_API int pa_run_end(pa_handle* h);
  * MHR histogram, ancestors) to a binary file, and back into a handle created
  * with the same configurations, which then continues with pa_run_steps and
  * pa_run_end exactly as the original would have.  Runs that store their
- * energies are not checkpointed. */
+ * energies are not checkpointed.
+ *
+ * pa_restore reads and checks the whole file before it writes to the device:
+ * a file of another configuration, a truncated one, or one whose state lies
+ * outside the handle's buffers (a population size beyond the capacity, a
+ * buffer parity other than 0 or 1, a temperature index beyond the schedule,
+ * a buffer of the wrong size) returns PA_ERR_ARG and leaves the handle as it
+ * was.  Only a CUDA error while the buffers are being written leaves it
+ * inconsistent; it then refuses to run (PA_ERR_STATE) until a restore
+ * succeeds.  pa_checkpoint_verify makes the file-level checks alone, on the
+ * host, without a handle or a device (message: pa_last_error(NULL)).  The
+ * reference has no checkpoints (its state lives in one process). */
 PA_API int pa_checkpoint(pa_handle* h, const char* path);
 PA_API int pa_restore(pa_handle* h, const char* path);
+PA_API int pa_checkpoint_verify(const char* path);
 
 /* Autotuner of the sweep's tile shape and spins per word.  It times one
  * sweep launch of the handle's populations (freshly initialised, at the first
@@ -254,11 +266,6 @@ typedef struct pa_kernel_time {
 } pa_kernel_time;
 PA_API int pa_profile_run(pa_handle* h, pa_kernel_time* out, int max, int* n);
 
-/* Measured 32-bit integer lane-operation throughput of `device`:
- * [0] LOP3 only (ALU pipe), [1] IMAD only (FMA pipe), [2] both interleaved.
- * The sweeps are integer-pipe bound; this is their roofline denominator. */
-PA_API int pa_probe_int_issue(int device, double* lane_ops_per_s);
-
 /* Writes dir/PA_results_run_<r>.dat for every run with `precision`
  * significant digits (PAisingSSC.cu:670-692), PA_MHR_results_run_<r>.dat
  * where mhr is on, and PA_energies_<i>.dat (i >= 1, last run) where
@@ -342,9 +349,10 @@ PA_API int pa_resample_plan(const int32_t* E, const uint8_t* active, int coding,
  * the library until the process exits.  Limit: at most 262144 replica slots
  * (SSC: R_prev; MSC: 32 * ceil(R_prev/32)); larger inputs return PA_ERR_ARG.
  * All calls share that one array, so calls whose GPU work overlaps (other
- * streams or host threads) race.  The first call on a device looks up the
- * array's device address with that device current; make it before any
- * stream capture. */
+ * streams or host threads) race.  Every call looks up the array's address
+ * on the current device (which allocates nothing); the first call on a
+ * device may load the library's device code, so make it before any stream
+ * capture. */
 PA_API int pa_resample_plan_noalloc(const int32_t* E, const uint8_t* active, int coding, int R_prev, int Rinit,
                                     int Rcap, double beta_prev, double beta, double e_ref, int weights, uint64_t seed,
                                     uint64_t iseq, uint32_t* roff, uint32_t* offs, uint32_t* src, double* out,

@@ -508,7 +508,7 @@ typedef struct {
 
 static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                        int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
-                       double* fam, double* attempts, const native_sweep_cfg* nat);
+                       double* fam, double* attempts, const native_sweep_cfg* nat, uint64_t iseq0);
 
 int or_anneal(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
               int max_steps, double* rows, int max_rows, double* attempts) {
@@ -526,33 +526,35 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
                double* fam, double* attempts) {
     return anneal_impl(msc, L, Rinit, sweeps, dBinit, Bfin, runs, seed, max_steps, adaptive, minov, maxov, rows,
-                       max_rows, fam, attempts, NULL);
+                       max_rows, fam, attempts, NULL, 0);
 }
 
 /* or_anneal2 for MSC with the engine's native-stream sweeps (the
  * initialisation and the copy-number draws stay in reference coordinates,
  * as in the engine); runs are sequential and continue the subsequence
- * counter. */
+ * counter, which starts at iseq0 (population k of an engine batch with the
+ * native stream starts at k << 40 and sweeps with tag | k). */
 int or_anneal_msc_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
-                         uint64_t key, uint32_t tag, int threads, int G, int cs, double* rows, int max_rows,
-                         double* attempts) {
+                         uint64_t key, uint32_t tag, uint64_t iseq0, int threads, int G, int cs, double* rows,
+                         int max_rows, double* attempts) {
     const native_sweep_cfg nat = {key, tag, threads, G, cs};
     return anneal_impl(1, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
-                       attempts, &nat);
+                       attempts, &nat, iseq0);
 }
 
 /* The same for SSC with the bit-plane sweep (tile replicas per work unit),
  * or with the int8 sweep (tile = 0). */
 int or_anneal_ssc_bits_native(int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
-                              uint64_t key, uint32_t tag, int tile, double* rows, int max_rows, double* attempts) {
+                              uint64_t key, uint32_t tag, uint64_t iseq0, int tile, double* rows, int max_rows,
+                              double* attempts) {
     const native_sweep_cfg nat = {key, tag, 256, tile, 1};
     return anneal_impl(0, L, Rinit, sweeps, dBinit, Bfin, runs, seed, 0, 0, 0.0, 0.0, rows, max_rows, NULL,
-                       attempts, &nat);
+                       attempts, &nat, iseq0);
 }
 
 static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin, int runs, uint64_t seed,
                        int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
-                       double* fam, double* attempts, const native_sweep_cfg* nat) {
+                       double* fam, double* attempts, const native_sweep_cfg* nat, uint64_t iseq0) {
     int N = L * L;
     const int nBmax = 10000;
     double* B = (double*)calloc(nBmax, sizeof(double));
@@ -565,7 +567,7 @@ static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, dou
     double* BF = (double*)calloc(nBmax, sizeof(double));
     double* S = (double*)calloc(nBmax, sizeof(double));
     int* Rn = (int*)calloc(nBmax, sizeof(int));
-    uint64_t iseq = 0;
+    uint64_t iseq = iseq0;
     double tot_att = 0;
     int nB = 0, ret = 0;
     BF[0] = -N * log(2.0);

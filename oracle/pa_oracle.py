@@ -43,8 +43,8 @@ _SIGS = {
     "or_anneal": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _vp, _i, _vp], _i),
     "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
-    "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _i, _i, _vp, _i, _vp], _i),
-    "or_anneal_ssc_bits_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _i, _vp, _i, _vp], _i),
+    "or_anneal_msc_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _u64, _i, _i, _i, _vp, _i, _vp], _i),
+    "or_anneal_ssc_bits_native": ([_i, _i, _i, _d, _d, _i, _u64, _u64, _u32, _u64, _i, _vp, _i, _vp], _i),
     "or_ssc_sweep_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32], None),
     "or_ssc_sweep_bits_native": ([_vp, _i, _i, _i, _u32, _u32, _u64, _u32, _u32, _i], _i),
     "or_native_accept4": ([_vp, _vp, _vp, _vp, _i, _u32, _u32, _u32, _u32, _u64, _u32, _u32], None),
@@ -308,15 +308,17 @@ def ssc_sweep_bits_native(spins: np.ndarray, L: int, sweeps: int, T4: int, T8: i
 
 
 def anneal_msc_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
-                      key: int, tag: int, threads: int = 256, tile: int = 1, cluster: int = 1):
+                      key: int, tag: int, threads: int = 256, tile: int = 1, cluster: int = 1, iseq0: int = 0):
     """Rows of `runs` sequential MSC runs whose sweeps use the engine's
     native stream: runs x nrows x 10.  tile: groups per work unit of the
-    one-CTA sweep; cluster: CTAs per group (threads = threads per CTA)."""
+    one-CTA sweep; cluster: CTAs per group (threads = threads per CTA);
+    iseq0: first subsequence of the reference-coordinate draws (population k
+    of an engine batch: k << 40, with tag | k)."""
     maxr = int(beta_final / dbeta) + 8
     rows = np.zeros((runs, maxr, 10))
     att = ctypes.c_double()
-    n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, threads, tile, cluster,
-                                   _p(rows), maxr, ctypes.byref(att))
+    n = lib().or_anneal_msc_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, iseq0, threads, tile,
+                                   cluster, _p(rows), maxr, ctypes.byref(att))
     if n < 0:
         raise RuntimeError("oracle anneal failed")
     return rows[:, :n]
@@ -331,15 +333,15 @@ def ssc_sweep_native(spins: np.ndarray, L: int, sweeps: int, T4: int, T8: int, k
 
 
 def anneal_ssc_bits_native(L: int, R: int, sweeps: int, dbeta: float, beta_final: float, runs: int, seed: int,
-                           key: int, tag: int, tile: int):
+                           key: int, tag: int, tile: int, iseq0: int = 0):
     """Rows of `runs` sequential SSC runs swept on bit planes with the
     engine's native stream, `tile` replicas per work unit (0: the int8 sweep):
-    runs x nrows x 10."""
+    runs x nrows x 10.  iseq0 as in anneal_msc_native."""
     maxr = int(beta_final / dbeta) + 8
     rows = np.zeros((runs, maxr, 10))
     att = ctypes.c_double()
-    n = lib().or_anneal_ssc_bits_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, tile, _p(rows), maxr,
-                                        ctypes.byref(att))
+    n = lib().or_anneal_ssc_bits_native(L, R, sweeps, dbeta, beta_final, runs, seed, key, tag, iseq0, tile,
+                                        _p(rows), maxr, ctypes.byref(att))
     if n < 0:
         raise RuntimeError("oracle anneal failed")
     return rows[:, :n]

@@ -24,7 +24,12 @@ Step 1 (patch) needs the reference checkout and runs in the build container;
 step 2 (nvcc) runs wherever the patched sources are, e.g. on the GPU host,
 which does not have the reference checkout.
 
-usage: python oracle/ref_build.py [--patch-only] [--sizes 16,64] [--jobs N]
+usage: python oracle/ref_build.py [--reference DIR] [--patch-only] [--sizes 16,64] [--jobs N]
+
+DIR is the reference checkout (the directory holding PAisingSSC.cu and
+PAisingMSC.cu), from --reference or the environment variable
+PAISING_REFERENCE_DIR; without one, the patched copies already under
+oracle/_ref/src are compiled.
 """
 from __future__ import annotations
 
@@ -37,7 +42,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = "/root/reference"
+REF_ENV = "PAISING_REFERENCE_DIR"
 OUT = os.path.join(HERE, "_ref")
 SRC_OUT = os.path.join(OUT, "src")
 BIN_OUT = os.path.join(OUT, "bin")
@@ -76,15 +81,19 @@ def _patch(text: str, rules, L: int) -> str:
     return text
 
 
-def reference_available() -> bool:
-    """The reference checkout is present (true in the build container only)."""
-    return os.path.isdir(REF_DIR)
+def reference_dir(explicit: str | None = None) -> str | None:
+    """The reference checkout: the given directory, else $PAISING_REFERENCE_DIR;
+    None when neither names a directory holding both programs."""
+    d = explicit or os.environ.get(REF_ENV)
+    if d and all(os.path.isfile(os.path.join(d, f"PAising{p}.cu")) for p in ("SSC", "MSC")):
+        return d
+    return None
 
 
-def patch(sizes) -> None:
+def patch(sizes, ref_dir: str) -> None:
     os.makedirs(SRC_OUT, exist_ok=True)
     for prog, rules in (("SSC", _SSC), ("MSC", _MSC)):
-        with open(os.path.join(REF_DIR, f"PAising{prog}.cu")) as f:
+        with open(os.path.join(ref_dir, f"PAising{prog}.cu")) as f:
             text = f.read()
         for L in sizes:
             with open(os.path.join(SRC_OUT, f"PAising{prog}_L{L}.cu"), "w") as f:
@@ -111,9 +120,12 @@ def _compile(src: str, variant: str) -> str:
     return out
 
 
-def compile_all(jobs: int) -> list[str]:
+def compile_all(jobs: int, sizes) -> list[str]:
+    """Compiles the patched sources of the given lattice sizes (every variant
+    that exists for them)."""
     os.makedirs(BIN_OUT, exist_ok=True)
-    srcs = sorted(f for f in os.listdir(SRC_OUT) if f.endswith(".cu") and f.startswith("PAising"))
+    want = tuple(f"_L{L}.cu" for L in sizes)
+    srcs = sorted(f for f in os.listdir(SRC_OUT) if f.startswith("PAising") and f.endswith(want))
     tasks = [(os.path.join(SRC_OUT, s), v) for s in srcs for v in ("inj", "curand")]
     tasks += [(os.path.join(SRC_OUT, s), v) for s in srcs if s.endswith("_L16.cu") for v in ("inj_adaptive", "inj_records")]
     tasks += [(os.path.join(SRC_OUT, s), "inj_lattice") for s in srcs if s == "PAisingSSC_L16.cu"]
@@ -123,18 +135,20 @@ def compile_all(jobs: int) -> list[str]:
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help=f"reference checkout (default: ${REF_ENV})")
     ap.add_argument("--patch-only", action="store_true")
     ap.add_argument("--sizes", default=",".join(map(str, DEFAULT_SIZES)))
     ap.add_argument("--jobs", type=int, default=min(8, os.cpu_count() or 1))
     a = ap.parse_args(argv)
     sizes = [int(s) for s in a.sizes.split(",") if s]
-    if os.path.isdir(REF_DIR):
-        patch(sizes)
+    ref = reference_dir(a.reference)
+    if ref:
+        patch(sizes, ref)
     elif not os.path.isdir(SRC_OUT):
         print("reference sources unavailable and no patched copy present", file=sys.stderr)
         return 1
     if not a.patch_only:
-        for b in compile_all(a.jobs):
+        for b in compile_all(a.jobs, sizes):
             print(b)
     return 0
 

@@ -85,6 +85,7 @@ _SIGS = {
     "pa_run_end": ([_vp], _i),
     "pa_checkpoint": ([_vp, ctypes.c_char_p], _i),
     "pa_restore": ([_vp, ctypes.c_char_p], _i),
+    "pa_checkpoint_verify": ([ctypes.c_char_p], _i),
     "pa_num_rows": ([_vp, ctypes.POINTER(_i)], _i),
     "pa_get_rows": ([_vp, _i, _vp, _i, ctypes.POINTER(_i)], _i),
     "pa_get_timing": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
@@ -99,7 +100,6 @@ _SIGS = {
     "pa_set_population": ([_vp, _vp], _i),
     "pa_get_population": ([_vp, _i, _vp, ctypes.c_size_t, ctypes.POINTER(_i)], _i),
     "pa_profile_run": ([_vp, _vp, _i, ctypes.POINTER(_i)], _i),
-    "pa_probe_int_issue": ([_i, _vp], _i),
     "pa_ssc_init": ([_vp, _i, _i, _u64, _u64, _vp], _i),
     "pa_ssc_sweep": ([_vp, _i, _i, _i, _d, _i, _u64, _u64, _i, _vp, _vp, _vp], _i),
     "pa_ssc_sweep_bits": ([_vp, _i, _i, _i, _d, _u64, _i, _vp, _vp, _vp], _i),
@@ -230,6 +230,12 @@ class Engine:
         """Continue a checkpointed run in this handle (same configuration)."""
         _check(lib().pa_restore(self._h, path.encode()), self._h)
 
+    @staticmethod
+    def verify_checkpoint(path: str) -> None:
+        """File-level checks of a checkpoint (host only): raises PaisingError
+        for a file pa_restore would refuse whatever the handle."""
+        _check(lib().pa_checkpoint_verify(path.encode()))
+
     def set_lattice_dump(self, directory: str | None, precision: int = 11) -> None:
         """Per-temperature population text files of the first run
         (PA_lattice_<i>.dat); None switches them off."""
@@ -342,13 +348,6 @@ def schedule(dbeta: float = 0.005, beta_final: float = 1.0) -> np.ndarray:
     out = np.zeros(n.value)
     _check(lib().pa_schedule(dbeta, beta_final, out.ctypes.data, n.value, ctypes.byref(n)))
     return out
-
-
-def probe_int_issue(device: int = 0) -> tuple[float, float, float]:
-    """Measured integer lane-ops/s: (LOP3 only, IMAD only, interleaved)."""
-    out = (ctypes.c_double * 3)()
-    _check(lib().pa_probe_int_issue(device, out))
-    return out[0], out[1], out[2]
 
 
 def ref_word(seed: int, subseq: int, ctr: int) -> int:

@@ -61,64 +61,66 @@ std::vector<double> schedule(double dbeta, double bfin) {
   return b;
 }
 
-// Multi-histogram reweighting of one run (the MHR build's analysis,
-// PAisingSSC.cu:694-767, one iteration as MHR_Niter = 1): from the energy
-// histogram of all temperatures, the free energies betaF_i and population
-// sizes R_i, the density of states
-//   ln Omega(E) = ln H(E) - max_i S_i - ln sum_i R_i exp(S_i - max S),
-//   S_i = betaF_i - beta_i E,
-// then at every beta_i the reweighted E/N, C/N and betaF/N.  rows: the run's
-// results rows; betaF_i is recomputed from the lnQ column exactly as the
-// reference accumulates it (BF_i = -N ln 2 + sum_{j<=i} -lnQ_j).  Returns
-// 4 doubles per temperature: beta, E/N, C/N, betaF/N.
+// Multi-histogram reweighting of one run: the single-iteration estimate the
+// reference's MHR build writes (PAisingSSC.cu:694-767 with MHR_Niter = 1),
+// written from the weighted-histogram equations.  Population i (inverse
+// temperature b_i, R_i replicas, free energy f_i = betaF_i, Z_i = e^{-f_i})
+// samples energy level E with probability Omega(E) e^{-b_i E} / Z_i, so the
+// pooled histogram H(E) of all temperatures estimates
+//     Omega(E) = H(E) / D(E),   D(E) = sum_i R_i e^{f_i - b_i E},
+// and at every b_j the reweighted ensemble is Omega(E) e^{-b_j E}:
+//     Z_j = sum_E Omega e^{-b_j E},  <E>_j,  C_j = b_j^2 var_j(E),
+//     betaF_j = -ln Z_j.
+// Logarithms of sums are taken relative to their largest exponent.  The f_i
+// are recomputed from the rows' lnQ column in the order the reference
+// accumulates them (f_i = -N ln 2 + sum_{j<=i} -lnQ_j); every sum runs over
+// temperatures and energy levels in ascending order.  Returns 4 doubles per
+// temperature: beta, E/N, C/N, betaF/N.
 std::vector<double> mhr_analysis(int N, const std::vector<double>& rows, const std::vector<unsigned long long>& hist) {
-  const int nB = (int)(rows.size() / kRowCols);
-  std::vector<double> B(nB), BF(nB), R(nB);
-  double sumlnQ = 0.0;
-  for (int i = 0; i < nB; ++i) {
-    B[i] = rows[(size_t)i * kRowCols];
-    R[i] = rows[(size_t)i * kRowCols + 8];
-    if (i > 0) sumlnQ -= rows[(size_t)i * kRowCols + 9];
-    BF[i] = -N * std::log(2.0) + sumlnQ;
+  const int nT = (int)(rows.size() / kRowCols);
+  std::vector<double> beta(nT), f(nT), pop(nT);
+  double acc = 0.0;
+  for (int i = 0; i < nT; ++i) {
+    const double* r = &rows[(size_t)i * kRowCols];
+    beta[i] = r[0];
+    pop[i] = r[8];
+    if (i > 0) acc -= r[9];
+    f[i] = -N * std::log(2.0) + acc;
   }
-  auto Ei = [N](int k) { return (double)(4 * k - 2 * N); };
-  std::vector<double> lnOmega((size_t)N + 1, 0.0), Sigma(nB);
-  std::vector<char> rel((size_t)N + 1, 0);
+  // energy levels the anneal visited (the others carry no information)
+  std::vector<int> level;
+  std::vector<double> energy, ln_omega;
   for (int k = 0; k <= N; ++k) {
-    double mSigma = Sigma[0] = BF[0] - B[0] * Ei(k);
-    for (int i = 1; i < nB; ++i) {
-      Sigma[i] = BF[i] - B[i] * Ei(k);
-      if (mSigma < Sigma[i]) mSigma = Sigma[i];
-    }
-    double sD = 0;
-    for (int i = 0; i < nB; ++i) sD += R[i] * std::exp(Sigma[i] - mSigma);
-    if (hist[k] == 0 || sD == 0) continue;
-    rel[k] = 1;
-    lnOmega[k] = std::log((double)hist[k]) - mSigma - std::log(sD);
+    if (hist[k] == 0) continue;
+    const double E = 4.0 * k - 2.0 * N;
+    double top = f[0] - beta[0] * E;
+    for (int i = 1; i < nT; ++i) top = std::max(top, f[i] - beta[i] * E);
+    double d = 0.0;  // D(E) e^{-top}
+    for (int i = 0; i < nT; ++i) d += pop[i] * std::exp(f[i] - beta[i] * E - top);
+    if (d == 0.0) continue;
+    level.push_back(k);
+    energy.push_back(E);
+    ln_omega.push_back(std::log((double)hist[k]) - top - std::log(d));
   }
-  std::vector<double> out((size_t)nB * 4), expOm((size_t)N + 1), Om((size_t)N + 1);
-  for (int i = 0; i < nB; ++i) {
-    double mOm = lnOmega[0] - B[i] * Ei(0);
-    for (int k = 0; k <= N; ++k) {
-      Om[k] = lnOmega[k] - B[i] * Ei(k);
-      if (mOm < Om[k]) mOm = Om[k];
+  const size_t nL = level.size();
+  std::vector<double> out((size_t)nT * 4, 0.0), w(nL);
+  for (int j = 0; j < nT; ++j) {
+    double top = -HUGE_VAL;
+    for (size_t l = 0; l < nL; ++l) top = std::max(top, ln_omega[l] - beta[j] * energy[l]);
+    double z = 0.0, e1 = 0.0;  // Z_j e^{-top}, sum E Omega e^{-b_j E - top}
+    for (size_t l = 0; l < nL; ++l) {
+      w[l] = std::exp(ln_omega[l] - beta[j] * energy[l] - top);
+      z += w[l];
     }
-    double p = 0;
-    for (int k = 0; k <= N; ++k) {
-      expOm[k] = std::exp(Om[k] - mOm);
-      if (rel[k]) p += expOm[k];
-    }
-    double s = 0;
-    for (int k = 0; k <= N; ++k)
-      if (rel[k]) s += Ei(k) * expOm[k];
-    const double E = s / p / N, BFm = -mOm - std::log(p);
-    s = 0;
-    for (int k = 0; k <= N; ++k)
-      if (rel[k]) s += std::pow(Ei(k) - E * N, 2) * expOm[k];
-    out[(size_t)i * 4 + 0] = B[i];
-    out[(size_t)i * 4 + 1] = E;
-    out[(size_t)i * 4 + 2] = B[i] * B[i] * s / p / N;
-    out[(size_t)i * 4 + 3] = BFm / N;
+    for (size_t l = 0; l < nL; ++l) e1 += energy[l] * w[l];
+    const double mean = e1 / z;
+    double var = 0.0;
+    for (size_t l = 0; l < nL; ++l) var += (energy[l] - mean) * (energy[l] - mean) * w[l];
+    var /= z;
+    out[(size_t)j * 4 + 0] = beta[j];
+    out[(size_t)j * 4 + 1] = mean / N;
+    out[(size_t)j * 4 + 2] = beta[j] * beta[j] * var / N;
+    out[(size_t)j * 4 + 3] = -(top + std::log(z)) / N;
   }
   return out;
 }
@@ -232,6 +234,7 @@ struct pa_handle {
   int lattice_prec = 11;
   bool lattice_failed = false;
   int step_run = -1;  // stepped run in progress (pa_run_begin .. pa_run_end): its index, else -1
+  bool unusable = false;  // a restore failed after writing device buffers: runs refused until one succeeds
   int step_i = 0;     // temperatures done in it
   std::vector<std::vector<double>> fam;  // per set: rows of (families, rho_t, S_f)
   std::vector<std::vector<double>> mhr;                    // per set: rows of (beta, E/N, C/N, betaF/N)
@@ -1005,6 +1008,10 @@ int pa_num_sets(const pa_handle* H, int* n) {
 
 int pa_run(pa_handle* H) {
   if (!H) return PA_ERR_ARG;
+  if (H->unusable) {
+    H->err = "a failed restore left this handle inconsistent: restore again or destroy it";
+    return PA_ERR_STATE;
+  }
   if (H->step_run >= 0) {
     H->err = "a stepped run is in progress (pa_run_end first)";
     return PA_ERR_STATE;
@@ -1039,6 +1046,10 @@ int pa_run(pa_handle* H) {
 
 int pa_run_begin(pa_handle* H) {
   if (!H) return PA_ERR_ARG;
+  if (H->unusable) {
+    H->err = "a failed restore left this handle inconsistent: restore again or destroy it";
+    return PA_ERR_STATE;
+  }
   if (H->step_run >= 0 || H->seq_runs != 1) {
     H->err = H->seq_runs != 1 ? "stepped runs need one run per handle (runs = 1 or a native batch)"
                               : "a stepped run is already in progress";
@@ -1081,40 +1092,160 @@ int pa_run_end(pa_handle* H) {
 }
 
 // ---------------------------------------------------------------- checkpoint
-// File: "PAGB300C", version, population count, coding, temperatures done,
-// runs completed; per population (device order) its shape, its PopDev and
-// the contents of the device buffers that carry state between temperatures.
+// File (version 2, little-endian, every field naturally aligned):
+//   "PAGB300C", int32 {version, populations, coding, temperatures done,
+//   runs completed}; then per population (device order) CkptPop (the shape
+//   it was written for), CkptScalars (the dynamic scalars of its PopDev) and
+//   its stateful buffers as (uint64 bytes, bytes) in ckpt_buffer_sizes'
+//   order.  Device addresses and the configuration fields of PopDev are not
+//   stored: a restore takes them from the handle.
 namespace {
 constexpr char kCkptMagic[8] = {'P', 'A', 'G', 'B', '3', '0', '0', 'C'};
-constexpr uint32_t kCkptVersion = 1;
+constexpr int32_t kCkptVersion = 2;
 
 struct CkptPop {
-  int L, R, Rcap, rgcap, cap, gpt, coding, rec, family;
+  int32_t L, R, Rcap, rgcap, cap, gpt, coding, rec, family;
 };
 
-// (device pointer, bytes) of every stateful buffer of population st (the
-// current half of the double buffers)
-std::vector<std::pair<void*, size_t>> state_buffers(const PopDev& st, const PopHost& P) {
-  const size_t units = st.coding == PA_CODING_MSC ? (size_t)st.rgcap * kMsb : (size_t)st.Rcap;
-  std::vector<std::pair<void*, size_t>> b;
-  b.push_back({st.spins[st.parity], population_bytes(st.coding, st.L, st.R_cur)});
-  if (st.coding == PA_CODING_MSC) b.push_back({st.active[st.parity], units});
-  b.push_back({st.E, units * sizeof(int32_t)});
-  b.push_back({st.M, units * sizeof(int32_t)});
-  b.push_back({st.rows, (size_t)P.cap * kRowCols * sizeof(double)});
-  b.push_back({st.betas, (size_t)P.cap * sizeof(double)});
-  b.push_back({st.thr, (size_t)P.cap * kThrPerStep * sizeof(uint32_t)});
-  if (st.mhr_hist) b.push_back({st.mhr_hist, ((size_t)st.N + 1) * sizeof(unsigned long long)});
-  if (st.family) {
-    b.push_back({st.anc[st.parity], units * sizeof(int32_t)});
-    b.push_back({st.fam_rows, (size_t)P.cap * 3 * sizeof(double)});
+struct CkptScalars {
+  int32_t nsteps, step, R_prev, R_cur, parity, error, Emin, run, Emin_acc, last_rec, last_fam, pad;
+  uint64_t iseq, sM4lo, sM4hi;
+  int64_t sE, sE2, sM, sM2;
+  double Emean, sumlnQ, lnQ, q, dbeta_cur;
+};
+static_assert(sizeof(CkptPop) == 36 && sizeof(CkptScalars) == 144, "checkpoint records are packed");
+
+CkptScalars scalars_of(const PopDev& st) {
+  CkptScalars c{};
+  c.nsteps = st.nsteps; c.step = st.step; c.R_prev = st.R_prev; c.R_cur = st.R_cur; c.parity = st.parity;
+  c.error = st.error; c.Emin = st.Emin; c.run = st.run; c.Emin_acc = st.Emin_acc; c.last_rec = st.last_rec;
+  c.last_fam = st.last_fam; c.iseq = st.iseq; c.sM4lo = st.sM4lo; c.sM4hi = st.sM4hi; c.sE = st.sE;
+  c.sE2 = st.sE2; c.sM = st.sM; c.sM2 = st.sM2; c.Emean = st.Emean; c.sumlnQ = st.sumlnQ; c.lnQ = st.lnQ;
+  c.q = st.q; c.dbeta_cur = st.dbeta_cur;
+  return c;
+}
+
+void apply_scalars(const CkptScalars& c, PopDev* st) {
+  st->nsteps = c.nsteps; st->step = c.step; st->R_prev = c.R_prev; st->R_cur = c.R_cur; st->parity = c.parity;
+  st->error = c.error; st->Emin = c.Emin; st->run = c.run; st->Emin_acc = c.Emin_acc; st->last_rec = c.last_rec;
+  st->last_fam = c.last_fam; st->iseq = c.iseq; st->sM4lo = c.sM4lo; st->sM4hi = c.sM4hi; st->sE = c.sE;
+  st->sE2 = c.sE2; st->sM = c.sM; st->sM2 = c.sM2; st->Emean = c.Emean; st->sumlnQ = c.sumlnQ; st->lnQ = c.lnQ;
+  st->q = c.q; st->dbeta_cur = c.dbeta_cur;
+  st->ticket = 0;
+}
+
+// Bytes of every stateful buffer of a population of shape cp holding R_cur
+// replicas: current spins, MSC active flags, E, M, rows, betas, thresholds,
+// MHR histogram (rec & kRecMhr), ancestors and family rows (family).
+std::vector<size_t> ckpt_buffer_sizes(const CkptPop& cp, int R_cur) {
+  const size_t units = cp.coding == PA_CODING_MSC ? (size_t)cp.rgcap * kMsb : (size_t)cp.Rcap;
+  std::vector<size_t> b;
+  b.push_back(population_bytes(cp.coding, cp.L, R_cur));
+  if (cp.coding == PA_CODING_MSC) b.push_back(units);
+  b.push_back(units * sizeof(int32_t));
+  b.push_back(units * sizeof(int32_t));
+  b.push_back((size_t)cp.cap * kRowCols * sizeof(double));
+  b.push_back((size_t)cp.cap * sizeof(double));
+  b.push_back((size_t)cp.cap * kThrPerStep * sizeof(uint32_t));
+  if (cp.rec & kRecMhr) b.push_back(((size_t)cp.L * cp.L + 1) * sizeof(unsigned long long));
+  if (cp.family) {
+    b.push_back(units * sizeof(int32_t));
+    b.push_back((size_t)cp.cap * 3 * sizeof(double));
   }
   return b;
+}
+
+// The same buffers of population st on the device (current half of the
+// double buffers), in the same order.
+std::vector<void*> state_buffers(const PopDev& st) {
+  std::vector<void*> b;
+  b.push_back(st.spins[st.parity]);
+  if (st.coding == PA_CODING_MSC) b.push_back(st.active[st.parity]);
+  b.push_back(st.E);
+  b.push_back(st.M);
+  b.push_back(st.rows);
+  b.push_back(st.betas);
+  b.push_back(st.thr);
+  if (st.rec & kRecMhr) b.push_back(st.mhr_hist);
+  if (st.family) {
+    b.push_back(st.anc[st.parity]);
+    b.push_back(st.fam_rows);
+  }
+  return b;
+}
+
+CkptPop shape_of(const PopHost& P) {
+  return CkptPop{P.h.L, P.cfg.R, P.h.Rcap, P.h.rgcap, P.cap, P.h.gpt, P.h.coding, P.h.rec, P.h.family};
+}
+
+// A checkpoint file read into host memory.
+struct CkptFile {
+  int32_t head[5] = {0, 0, 0, 0, 0};
+  struct Pop {
+    CkptPop shape{};
+    CkptScalars sc{};
+    std::vector<std::vector<uint8_t>> bufs;
+  };
+  std::vector<Pop> pops;
+};
+
+// Reads and checks a whole checkpoint file before anything is written to a
+// device: the header, every population's shape and scalars (sizes within the
+// capacity, parity 0 or 1, step within the schedule) and every buffer's size
+// against what that shape and population size need.  Returns "" or what is
+// wrong.
+std::string read_checkpoint(const char* path, CkptFile* out) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return "cannot read the file";
+  struct Closer {
+    FILE* f;
+    ~Closer() { std::fclose(f); }
+  } closer{f};
+  char magic[8];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kCkptMagic, 8) != 0) return "not a checkpoint";
+  int32_t* head = out->head;
+  if (std::fread(head, sizeof(int32_t), 5, f) != 5) return "truncated header";
+  if (head[0] != kCkptVersion) return "unknown version";
+  if (head[1] < 1 || head[1] > kMaxPop) return "population count out of range";
+  if (head[2] != PA_CODING_SSC && head[2] != PA_CODING_MSC) return "unknown coding";
+  if (head[3] < 0 || head[3] >= kNBmax || head[4] < 0) return "temperature or run count out of range";
+  out->pops.resize(head[1]);
+  for (int k = 0; k < head[1]; ++k) {
+    CkptFile::Pop& p = out->pops[k];
+    if (std::fread(&p.shape, sizeof(p.shape), 1, f) != 1 || std::fread(&p.sc, sizeof(p.sc), 1, f) != 1)
+      return "truncated";
+    const CkptPop& cp = p.shape;
+    const CkptScalars& c = p.sc;
+    if (cp.coding != head[2] || cp.L < 2 || cp.L > 4096 || cp.R < 1 || cp.Rcap < cp.R ||
+        cp.rgcap != (int)(((long long)cp.Rcap + kMsb - 1) / kMsb) || cp.cap < 1 || cp.cap > kNBmax)
+      return "population shape out of range";
+    if (c.parity != 0 && c.parity != 1) return "buffer parity is not 0 or 1";
+    if (c.R_cur < 0 || c.R_cur > cp.Rcap || c.R_prev < 0 || c.R_prev > cp.Rcap)
+      return "population size beyond the capacity";
+    if (c.nsteps < 0 || c.nsteps >= cp.cap || c.step < 0 || c.step > c.nsteps + 1)
+      return "temperature index beyond the schedule";
+    if (c.error < 0 || c.error > kErrSweepForm || c.run < -1 || c.last_rec < -1 || c.last_rec > cp.cap ||
+        c.last_fam < -1 || c.last_fam > cp.cap)
+      return "state field out of range";
+    for (size_t want : ckpt_buffer_sizes(cp, c.R_cur)) {
+      uint64_t n = 0;
+      if (std::fread(&n, sizeof(n), 1, f) != 1) return "truncated";
+      if (n != want) return "buffer size does not match the population";
+      p.bufs.emplace_back(n);
+      if (std::fread(p.bufs.back().data(), 1, n, f) != n) return "truncated";
+    }
+  }
+  if (std::fgetc(f) != EOF) return "trailing bytes";
+  return "";
 }
 }  // namespace
 
 int pa_checkpoint(pa_handle* H, const char* path) {
   if (!H || !path) return PA_ERR_ARG;
+  if (H->unusable) {
+    H->err = "a failed restore left this handle inconsistent: restore again or destroy it";
+    return PA_ERR_STATE;
+  }
   if (H->step_run < 0) {
     H->err = "checkpoints are taken between the steps of a stepped run";
     return PA_ERR_STATE;
@@ -1134,18 +1265,19 @@ int pa_checkpoint(pa_handle* H, const char* path) {
     return PA_ERR_ARG;
   }
   bool ok = std::fwrite(kCkptMagic, 1, 8, f) == 8;
-  const int32_t head[5] = {(int32_t)kCkptVersion, H->npop, H->coding, H->step_i, H->runs_done};
+  const int32_t head[5] = {kCkptVersion, H->npop, H->coding, H->step_i, H->runs_done};
   ok = ok && std::fwrite(head, sizeof(head), 1, f) == 1;
   std::vector<uint8_t> buf;
   for (int k = 0; k < H->npop && ok; ++k) {
-    const PopHost& P = H->pops[k];
-    const CkptPop cp{P.h.L, P.cfg.R, P.h.Rcap, P.h.rgcap, P.cap, P.h.gpt, P.h.coding, P.h.rec, P.h.family};
-    ok = std::fwrite(&cp, sizeof(cp), 1, f) == 1 && std::fwrite(&st[k], sizeof(PopDev), 1, f) == 1;
-    for (const auto& b : state_buffers(st[k], P)) {
-      if (!ok) break;
-      buf.resize(b.second);
-      e = cudaMemcpy(buf.data(), b.first, b.second, cudaMemcpyDeviceToHost);
-      const uint64_t n = b.second;
+    const CkptPop cp = shape_of(H->pops[k]);
+    const CkptScalars sc = scalars_of(st[k]);
+    ok = std::fwrite(&cp, sizeof(cp), 1, f) == 1 && std::fwrite(&sc, sizeof(sc), 1, f) == 1;
+    const std::vector<size_t> sizes = ckpt_buffer_sizes(cp, sc.R_cur);
+    const std::vector<void*> ptrs = state_buffers(st[k]);
+    for (size_t j = 0; j < sizes.size() && ok; ++j) {
+      buf.resize(sizes[j]);
+      e = cudaMemcpy(buf.data(), ptrs[j], sizes[j], cudaMemcpyDeviceToHost);
+      const uint64_t n = sizes[j];
       ok = e == cudaSuccess && std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(buf.data(), 1, n, f) == n;
     }
   }
@@ -1158,74 +1290,61 @@ int pa_checkpoint(pa_handle* H, const char* path) {
   return PA_OK;
 }
 
+int pa_checkpoint_verify(const char* path) {
+  if (!path) return PA_ERR_ARG;
+  CkptFile cf;
+  const std::string why = read_checkpoint(path, &cf);
+  if (!why.empty()) {
+    pa::g_last_error = std::string(path) + ": " + why;
+    return PA_ERR_ARG;
+  }
+  return PA_OK;
+}
+
 int pa_restore(pa_handle* H, const char* path) {
   if (!H || !path) return PA_ERR_ARG;
   if (H->step_run >= 0) {
     H->err = "a stepped run is in progress";
     return PA_ERR_STATE;
   }
-  FILE* f = std::fopen(path, "rb");
-  if (!f) {
-    H->err = std::string("cannot read ") + path;
-    return PA_ERR_ARG;
-  }
-  auto bad = [&](const char* m) {
-    std::fclose(f);
-    H->err = std::string(path) + ": " + m;
-    return PA_ERR_ARG;
-  };
-  char magic[8];
-  int32_t head[5];
-  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kCkptMagic, 8) != 0) return bad("not a checkpoint");
-  if (std::fread(head, sizeof(head), 1, f) != 1 || head[0] != (int32_t)kCkptVersion) return bad("unknown version");
-  if (head[1] != H->npop || head[2] != H->coding) return bad("written by a handle of another configuration");
-  std::vector<PopDev> cur(H->npop), saved(H->npop);
-  cudaError_t e = cudaMemcpy(cur.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    std::fclose(f);
-    return H->cuda_fail(e, "restore");
-  }
-  std::vector<uint8_t> buf;
-  for (int k = 0; k < H->npop; ++k) {
+  // the whole file is read and checked first: a bad file changes nothing
+  CkptFile cf;
+  std::string why = read_checkpoint(path, &cf);
+  if (why.empty() && (cf.head[1] != H->npop || cf.head[2] != H->coding))
+    why = "written by a handle of another configuration";
+  for (int k = 0; k < H->npop && why.empty(); ++k) {
     const PopHost& P = H->pops[k];
-    CkptPop cp;
-    if (std::fread(&cp, sizeof(cp), 1, f) != 1 || std::fread(&saved[k], sizeof(PopDev), 1, f) != 1)
-      return bad("truncated");
-    if (cp.L != P.h.L || cp.R != P.cfg.R || cp.Rcap != P.h.Rcap || cp.rgcap != P.h.rgcap || cp.cap != P.cap ||
-        cp.gpt != P.h.gpt || cp.coding != P.h.coding || cp.rec != P.h.rec || cp.family != P.h.family)
-      return bad("written by a handle of another configuration");
-    // the saved scalars with this handle's buffers
-    PopDev m = saved[k];
-    std::memcpy(m.spins, cur[k].spins, sizeof(m.spins));
-    std::memcpy(m.active, cur[k].active, sizeof(m.active));
-    std::memcpy(m.anc, cur[k].anc, sizeof(m.anc));
-    m.E = cur[k].E; m.M = cur[k].M; m.roff = cur[k].roff; m.offs = cur[k].offs; m.src = cur[k].src;
-    m.blk_tot = cur[k].blk_tot; m.blk_off = cur[k].blk_off; m.qpart_d = cur[k].qpart_d; m.qpart_f = cur[k].qpart_f;
-    m.rows = cur[k].rows; m.betas = cur[k].betas; m.thr = cur[k].thr; m.init_src = cur[k].init_src;
-    m.hist = cur[k].hist; m.mhr_hist = cur[k].mhr_hist; m.elog = cur[k].elog; m.alog = cur[k].alog;
-    m.nlog = cur[k].nlog; m.fam_cnt = cur[k].fam_cnt; m.fam_rows = cur[k].fam_rows; m.fam_part = cur[k].fam_part;
-    m.ticket = 0;
-    for (const auto& b : state_buffers(m, P)) {
-      uint64_t n = 0;
-      if (std::fread(&n, sizeof(n), 1, f) != 1 || n != b.second) return bad("truncated or mismatched buffer");
-      buf.resize(n);
-      if (std::fread(buf.data(), 1, n, f) != n) return bad("truncated");
-      e = cudaMemcpy(b.first, buf.data(), n, cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) {
-        std::fclose(f);
-        return H->cuda_fail(e, "restore");
-      }
-    }
-    cur[k] = m;
+    const CkptPop want = shape_of(P);
+    const CkptFile::Pop& p = cf.pops[k];
+    if (std::memcmp(&p.shape, &want, sizeof(want)) != 0) why = "written by a handle of another configuration";
+    else if (P.h.adaptive ? p.sc.nsteps > P.h.nsteps : p.sc.nsteps != P.h.nsteps)
+      why = "schedule length differs from the handle's";
   }
-  std::fclose(f);
-  e = cudaMemcpy(H->d_pops, cur.data(), sizeof(PopDev) * H->npop, cudaMemcpyHostToDevice);
+  if (!why.empty()) {
+    H->err = std::string(path) + ": " + why;
+    return PA_ERR_ARG;
+  }
+  std::vector<PopDev> cur(H->npop);
+  cudaError_t e = cudaMemcpy(cur.data(), H->d_pops, sizeof(PopDev) * H->npop, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return H->cuda_fail(e, "restore");
+  // from here on a failure leaves device buffers half written
+  for (int k = 0; k < H->npop && e == cudaSuccess; ++k) {
+    apply_scalars(cf.pops[k].sc, &cur[k]);  // the handle's own configuration and buffers
+    const std::vector<void*> ptrs = state_buffers(cur[k]);
+    for (size_t j = 0; j < ptrs.size() && e == cudaSuccess; ++j)
+      e = cudaMemcpy(ptrs[j], cf.pops[k].bufs[j].data(), cf.pops[k].bufs[j].size(), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(H->d_pops, cur.data(), sizeof(PopDev) * H->npop, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    H->unusable = true;
+    return H->cuda_fail(e, "restore (the handle is unusable until a restore succeeds)");
+  }
+  H->unusable = false;
   H->reset_results();
-  H->runs_done = head[4];
+  H->runs_done = cf.head[4];
   H->drained.assign(H->npop, -1);
   H->step_run = 0;
-  H->step_i = head[3];
+  H->step_i = cf.head[3];
   return PA_OK;
 }
 

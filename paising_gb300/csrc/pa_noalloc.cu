@@ -17,12 +17,13 @@
 // 32 * ceil(R_prev / 32)); larger inputs are rejected with PA_ERR_ARG.  Every
 // call shares the one array and leaves its contents behind, so calls whose
 // GPU work overlaps (other streams, other host threads) race with each other.
-// The first call on a device looks up the array's device address on that
-// device (cudaGetSymbolAddress, with the device current); make that first
+// Every call looks up the array's device address on the current device
+// (cudaGetSymbolAddress, which allocates nothing), so the address stays right
+// after cudaDeviceReset re-creates the context.  The first call on a device
+// may load the library's device code (lazy module loading): make that first
 // call before any stream capture.
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <cstring>
 #include <string>
 
@@ -37,7 +38,6 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = 32768;
 constexpr long long kNoAllocMaxUnits = (long long)kResBlocksMax * 256;
-constexpr int kMaxDevices = 64;
 
 // layout of the scratch array
 constexpr size_t kOffState = 0;
@@ -51,9 +51,6 @@ static_assert(sizeof(PopDev) <= kOffBetas, "descriptor does not fit its slot");
 static_assert(kOffEnd <= kNoAllocScratchBytes, "scratch layout exceeds the array");
 
 static __device__ __align__(256) unsigned char g_plan_scratch[kNoAllocScratchBytes];
-
-// device address of g_plan_scratch, per device (looked up once)
-std::atomic<unsigned char*> g_scratch_addr[kMaxDevices];
 
 // Writes the call's descriptor and inverse temperatures into the scratch
 // array; the descriptor's ticket and error fields start at zero.
@@ -81,23 +78,17 @@ int pa_resample_plan_noalloc(const int32_t* E, const uint8_t* active, int coding
   if (coding != PA_CODING_SSC && coding != PA_CODING_MSC) return fail(PA_ERR_ARG, "bad coding");
   if (coding == PA_CODING_MSC && !active) return fail(PA_ERR_ARG, "MSC needs the active flags");
   if (weights != PA_WEIGHTS_FP32 && weights != PA_WEIGHTS_FP64) return fail(PA_ERR_ARG, "bad weights");
-  const long long units = coding == PA_CODING_MSC ? (long long)((R_prev + kMsb - 1) / kMsb) * kMsb : R_prev;
+  const long long units = coding == PA_CODING_MSC ? ((long long)R_prev + kMsb - 1) / kMsb * kMsb : R_prev;
   if (units > kNoAllocMaxUnits)
     return fail(PA_ERR_ARG, "population of " + std::to_string(units) + " replica slots exceeds the maximum of " +
                                 std::to_string(kNoAllocMaxUnits) + " supported without allocation");
   cudaStream_t s = (cudaStream_t)stream;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(PA_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(PA_ERR_ARG, "device ordinal out of range");
-  unsigned char* base = g_scratch_addr[dev].load();
-  if (!base) {  // set-up, once per device, with that device current
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_plan_scratch);
-    if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    base = static_cast<unsigned char*>(p);
-    g_scratch_addr[dev].store(base);
-  }
+  // the array's address on the current device; the host-side symbol
+  // g_plan_scratch is a stand-in, never a device address
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_plan_scratch);
+  if (e != cudaSuccess) return fail(PA_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  unsigned char* base = static_cast<unsigned char*>(p);
 
   PopDev h;
   std::memset(&h, 0, sizeof(h));
@@ -108,7 +99,7 @@ int pa_resample_plan_noalloc(const int32_t* E, const uint8_t* active, int coding
   h.nsteps = 1;
   h.Rinit = Rinit;
   h.Rcap = Rcap;
-  h.rgcap = (Rcap + kMsb - 1) / kMsb;
+  h.rgcap = (int)(((long long)Rcap + kMsb - 1) / kMsb);
   h.R_prev = R_prev;
   h.R_cur = R_prev;
   h.weights = weights;

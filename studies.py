@@ -1,15 +1,16 @@
-"""Reproducible studies on the GPU engine (run on a CUDA host):
+"""Reproducible studies on the GPU engine (run on a CUDA host, from the
+repository root):
 
-    python -m paising_gb300.studies precision   [--out FILE]
-    python -m paising_gb300.studies batch       [--coding msc|ssc] [--out FILE]
-    python -m paising_gb300.studies large       [--out FILE]
+    python studies.py precision   [--out FILE]
+    python studies.py batch       [--coding msc|ssc] [--out FILE]
+    python studies.py large       [--out FILE]
+    python studies.py reference_large [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
     resampling weights (FP64 lnQ) against all-FP64 weights; errors of betaF/N,
     E/N and C/N against the exact finite-lattice solution (Kaufman) at every
-    beta.  The exact values come from the formula in closed form (FP64),
-    evaluated inside this module.
+    beta, from the oracle's FP64 evaluation (the studies' checker).
 batch: 64 populations with L drawn from {16,32,48,64,96,128}, R uniform in
     [1000, 20000], dbeta from {0.0025, 0.005, 0.01}, beta_final 1, 20 sweeps
     (seed 2026), annealed as one batch and as 64 sequential plain runs, MSC
@@ -19,68 +20,26 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
+import os
 import sys
 import time
 
 import numpy as np
 
-import paising_gb300 as pa
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+import paising_gb300 as pa  # noqa: E402
+from oracle import pa_oracle  # noqa: E402
 
 
 # ------------------------------------------------ exact solution (Kaufman)
-def _log2cosh(x):
-    x = abs(x)
-    return x + math.log1p(math.exp(-2 * x))
-
-
-def _log2sinh(x):
-    x = abs(x)
-    if x < 1e-3:
-        return math.log(2 * x) + math.log1p(x * x / 6)
-    return x + math.log(-math.expm1(-2 * x))
-
-
-def kaufman_lnz(L: int, K: float) -> float:
-    """ln Z of the L x L periodic Ising model at coupling K (B. Kaufman,
-    Phys. Rev. 76, 1232 (1949); form of Ferdinand and Fisher, Phys. Rev. 185,
-    832 (1969)), evaluated in the log domain."""
-    if K <= 0:
-        return L * L * math.log(2.0)
-    c2, s2 = math.cosh(2 * K), math.sinh(2 * K)
-    base = c2 * c2 / s2
-    l = [0.0, 0.0, 0.0, 0.0]
-    sign4 = 1
-    for r in range(L):
-        for par in (0, 1):
-            k = 2 * r + par
-            g = 2 * K + math.log(math.tanh(K)) if k == 0 else math.acosh(base - math.cos(math.pi * k / L))
-            x = 0.5 * L * g
-            ic, is_ = (0, 1) if par else (2, 3)
-            l[ic] += _log2cosh(x)
-            if x == 0:
-                l[is_] = -math.inf
-            else:
-                l[is_] += _log2sinh(x)
-            if is_ == 3 and x < 0:
-                sign4 = -sign4
-    mx = max(v for v in l if math.isfinite(v))
-    s = sum(math.exp(v - mx) * (sign4 if i == 3 else 1) for i, v in enumerate(l) if math.isfinite(v))
-    return -math.log(2) + 0.5 * L * L * math.log(2 * s2) + mx + math.log(s)
-
-
 def kaufman(L: int, beta: float):
-    """(betaF/N, E/N, C/N) by central differences of ln Z."""
+    """(betaF/N, E/N, C/N) of the L x L torus from the oracle's exact
+    partition function (oracle/kaufman.c, checked against enumeration and
+    mpmath by tests/test_kaufman.py); the studies use it as the checker."""
+    lz, e, c = pa_oracle.kaufman(L, beta)
     N = L * L
-    lz = kaufman_lnz(L, beta)
-    if beta <= 0:
-        return -lz / N, 0.0, 0.0
-    h = 1e-4
-    lp, lm = kaufman_lnz(L, beta + h), kaufman_lnz(L, beta - h)
-    lpp, lmm = kaufman_lnz(L, beta + 2 * h), kaufman_lnz(L, beta - 2 * h)
-    d1 = (-lpp + 8 * lp - 8 * lm + lmm) / (12 * h)
-    d2 = (-lpp + 16 * lp - 30 * lz + 16 * lm - lmm) / (12 * h * h)
-    return -lz / N, -d1 / N, beta * beta * d2 / N
+    return -lz / N, e / N, c / N
 
 
 # ----------------------------------------------------------------- studies
@@ -174,13 +133,47 @@ def large(seed: int = 256, variants=(2, 4), sweeps: int = 50) -> dict:
     return res
 
 
+def reference_large(seed: int = 256, sweeps: int = 50) -> dict:
+    """The reference's own MSC program (PAisingMSC.cu with #define L 256,
+    cuRAND, built by oracle/ref_build.py) on the same workload as large():
+    its whole-anneal seconds and attempts/ns as it reports them, and the
+    errors of its results file against the exact solution."""
+    import re
+    import subprocess
+    import tempfile
+    from oracle import ref_build
+    L, R = 256, 131072
+    binp = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "_ref", "bin",
+                        f"PAisingMSC_L{L}_curand")
+    if not os.path.exists(binp):
+        ref_build.main(["--sizes", str(L)])
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([binp, "-R", str(R), "-t", str(sweeps), "-d", "0.005", "-s", str(seed), "-o", d],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout[-800:] + r.stderr[-800:])
+        rows = np.loadtxt(os.path.join(d, "PA_results_run_0.dat"))
+    el = float(re.search(r"Elapsed time:\s*([0-9.eE+-]+)", r.stdout).group(1))
+    tpf = float(re.search(r"Time per spin-flip:\s*([0-9.eE+-]+)", r.stdout).group(1))
+    ex = np.array([kaufman(L, b) for b in rows[:, 0]])
+    res = {"program": f"PAisingMSC.cu, L={L}, cuRAND (its own build)", "R": R, "sweeps": sweeps, "seed": seed,
+           "seconds": el, "attempts_per_ns": 1.0 / tpf,
+           "max_abs_err_betaF_per_site": float(np.max(np.abs(rows[:, 6] - ex[:, 0]))),
+           "max_abs_err_E_per_site": float(np.max(np.abs(rows[1:, 1] - ex[1:, 1]))),
+           "beta_at_max_betaF_err": float(rows[np.argmax(np.abs(rows[:, 6] - ex[:, 0])), 0]),
+           "rows": len(rows)}
+    print(json.dumps(res), flush=True)
+    return res
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "batch", "large"])
+    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large"])
     ap.add_argument("--out", default=None)
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
-    r = batch(coding=a.coding) if a.study == "batch" else {"precision": precision, "large": large}[a.study]()
+    r = batch(coding=a.coding) if a.study == "batch" else \
+        {"precision": precision, "large": large, "reference_large": reference_large}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0

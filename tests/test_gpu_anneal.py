@@ -90,6 +90,31 @@ def test_native_free_energy_vs_kaufman_C2(cuda, oracle, coding):
     assert np.max(np.abs(r[1:, 1] - eE)) < 5e-3
 
 
+@pytest.mark.slow
+def test_benchmarked_configuration_every_population_vs_kaufman(cuda, oracle):
+    """The headline workload exactly as bench.py builds it (L=64, R=20000,
+    100 sweeps, dbeta=0.005, 8 populations per launch, native stream, FP32
+    weights, CUDA graph): every population meets |betaF/N - exact| <= 1e-4
+    at every beta and |E/N - exact| < 5e-3, against Kaufman's finite-torus
+    solution in FP64."""
+    import bench
+    a = bench.parse_args([])
+    with pa.Engine(**bench.engine_kwargs(a, seed=bench.rank_seed(0), device=0)) as e:
+        e.run()
+        assert e.num_sets() == a.populations == 8
+        rows = [e.rows(k) for k in range(e.num_sets())]
+    N = a.L * a.L
+    betas = rows[0][:, 0]
+    exact = np.array([oracle.kaufman(a.L, b) for b in betas])
+    bf_exact, e_exact = -exact[:, 0] / N, exact[:, 1] / N
+    assert len({tuple(r[1:20, 8]) for r in rows}) == len(rows)
+    for k, r in enumerate(rows):
+        assert np.array_equal(r[:, 0], betas)
+        err = np.abs(r[:, 6] - bf_exact)
+        assert err.max() <= 1e-4, (k, err.max(), r[np.argmax(err), 0])
+        assert np.max(np.abs(r[1:, 1] - e_exact[1:])) < 5e-3, k
+
+
 @pytest.mark.parametrize("coding", ["ssc", "msc"])
 def test_population_roundtrip(cuda, coding):
     """pa_set_population / pa_get_population: with no temperature step

@@ -74,3 +74,40 @@ def test_checkpoint_rejects_other_configuration(cuda, tmp_path):
         with pytest.raises(pa.PaisingError) as ei:
             c.checkpoint(path)  # no stepped run in progress
         assert ei.value.status == 5
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_restore_refuses_tampered_files_and_keeps_the_handle(cuda, tmp_path, coding):
+    """A checkpoint whose population size or buffer parity was altered is
+    refused before any device write (PA_ERR_ARG); the same handle then
+    restores the intact file and finishes with the uninterrupted run's rows."""
+    kw = dict(L=16, R=500, sweeps=3, dbeta=0.1, seed=5, coding=coding)
+    with pa.Engine(**kw) as e:
+        e.run()
+        ref = e.rows(0)
+    good = tmp_path / "good.bin"
+    with pa.Engine(**kw) as a:
+        a.run_begin()
+        a.run_steps(4)
+        a.checkpoint(str(good))
+    data = good.read_bytes()
+    # header 8 + 5 int32, shape 9 int32, then the scalars: nsteps, step, R_prev, R_cur, parity, ...
+    off = 8 + 20 + 36
+    import struct
+    with pa.Engine(**kw) as b:
+        for name, pos, val in (("R_cur", off + 12, 10 ** 7), ("parity", off + 16, 2), ("step", off + 4, 999)):
+            bad = bytearray(data)
+            bad[pos:pos + 4] = struct.pack("<i", val)
+            p = tmp_path / f"bad_{name}.bin"
+            p.write_bytes(bytes(bad))
+            with pytest.raises(pa.PaisingError) as ei:
+                b.restore(str(p))
+            assert ei.value.status == 1, name
+            with pytest.raises(pa.PaisingError):
+                pa.Engine.verify_checkpoint(str(p))
+        pa.Engine.verify_checkpoint(str(good))
+        b.restore(str(good))
+        while not b.run_steps(3):
+            pass
+        b.run_end()
+        assert np.array_equal(b.rows(0), ref)

@@ -47,3 +47,71 @@ def test_family_batch_adaptive_and_files(cuda, oracle, tmp_path):
         got = np.loadtxt(tmp_path / "PA_family_run_0.dat")
         assert np.array_equal(got[:, 1], e.family_rows(0)[:, 0])
         assert np.allclose(got[:, 0], e.rows(0)[:, 0])
+
+
+def _family_stats_of(sizes: np.ndarray):
+    """The definitions themselves, from family sizes c_f (sum R): number of
+    families, rho_t = sum c_f^2 / R, S_f = ln R - sum c_f ln c_f / R."""
+    sizes = sizes[sizes > 0].astype(np.float64)
+    R = sizes.sum()
+    return len(sizes), (sizes ** 2).sum() / R, np.log(R) - (sizes * np.log(sizes)).sum() / R
+
+
+def _replica_lattices(coding: str, pop: np.ndarray, R: int, L: int) -> np.ndarray:
+    """Active replicas of a population read back with pa_get_population, one
+    row of bytes per replica.  MSC slot (g, b) holds offspring s = b * rg + g
+    (PAisingMSC.cu:413-414) and is active when s < R."""
+    if coding == "ssc":
+        return pop[:R].astype(np.int8)
+    rg = pop.shape[0]
+    out = []
+    for g in range(rg):
+        for b in range(32):
+            if b * rg + g < R:
+                out.append(((pop[g] >> np.uint32(b)) & np.uint32(1)).astype(np.int8))
+    return np.array(out)
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
+@pytest.mark.parametrize("R,steps", [(8, 2), (300, 4)])
+def test_family_statistics_from_observed_ancestors(cuda, coding, R, steps):
+    """Family statistics checked against ancestors observed directly, not
+    against a restatement of the engine's bookkeeping.  With no Metropolis
+    sweeps (sweeps = 0) a replica's lattice is an exact copy of its initial
+    ancestor's, and every initial lattice is distinct, so after k
+    temperatures each replica's family is found by matching its lattice
+    against the uploaded initial population.  The family sizes counted that
+    way give the three columns of row k through their definitions."""
+    L, N, dB, seed = 8, 64, 0.05, 31 + R
+    rng = np.random.default_rng(R * 10 + steps)
+    rg0 = (R + 31) // 32
+    if coding == "ssc":
+        init = np.where(rng.integers(0, 2, (R, N)) > 0, 1, -1).astype(np.int8)
+        slots = init
+    else:
+        init = rng.integers(0, 2**32, (rg0, N), dtype=np.uint32)
+        slots = np.array([((init[g] >> np.uint32(b)) & np.uint32(1)).astype(np.int8)
+                          for g in range(rg0) for b in range(32)])
+    index = {row.tobytes(): i for i, row in enumerate(slots)}
+    assert len(index) == len(slots)  # every initial lattice distinct
+    longest = None
+    for k in range(1, steps + 1):
+        with pa.Engine(L=L, R=R, sweeps=0, dbeta=dB, beta_final=(k + 0.5) * dB, seed=seed, coding=coding,
+                       family=True) as e:
+            e.set_population(init)
+            e.run()
+            rows, fam, pop = e.rows(0), e.family_rows(0), e.population()
+        assert rows.shape[0] == k + 1 and fam.shape[0] == k + 1
+        Rk = int(rows[k, 8])
+        lat = _replica_lattices(coding, pop, Rk, L)
+        assert len(lat) == Rk
+        anc = np.array([index[row.tobytes()] for row in lat])  # KeyError: a lattice that descends from none
+        nf, rho, sf = _family_stats_of(np.bincount(anc))
+        assert fam[k, 0] == nf, (k, fam[k], nf)
+        assert fam[k, 1] == pytest.approx(rho, rel=1e-12) and fam[k, 2] == pytest.approx(sf, rel=1e-12, abs=1e-12)
+        if longest is not None:  # the same trajectory: earlier rows repeat
+            assert np.array_equal(fam[:k], longest)
+        longest = fam
+    assert fam[0, 0] == R and fam[0, 1] == 1.0 and fam[0, 2] == pytest.approx(np.log(R), rel=1e-12)
+    if R > 100:
+        assert fam[-1, 0] < R  # resampling removed families

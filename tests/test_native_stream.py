@@ -237,3 +237,34 @@ def test_ssc_anneal_native_stream_int8(cuda, oracle, L, R, variant):
         got = e.rows(0)
     ref = oracle.anneal_ssc_bits_native(L, R, 3, 0.1, 1.0, 1, seed, seed, oracle.NATIVE_TAG_SSC, 0)
     compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("coding", ["msc", "ssc"])
+def test_native_batch_each_population_equals_oracle(cuda, oracle, coding):
+    """The batched form the benchmark times (runs=P concurrent populations of
+    one configuration in one launch sequence, native stream, graph), here
+    with FP64 weights so that every R_i must agree exactly: population k
+    equals the oracle's anneal started at subsequence k << 40 with sweep tag
+    | k, row for row.  The reference's -M runs (PAisingMSC.cu:583,784) are
+    the sequential form this batching generalises."""
+    from conftest import compare_rows
+    L, R, P, seed, sweeps, dbeta = 64, 2000, 4, 4242, 2, 0.05
+    with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=1.0, runs=P, seed=seed, coding=coding,
+                   rng="native", weights="fp64", graph=True, device=0) as e:
+        e.run()
+        assert e.num_sets() == P
+        forms = [e.sweep_form(k) for k in range(P)]
+        got = [e.rows(k) for k in range(P)]
+    assert len({tuple(g[1:, 8]) for g in got}) == P  # disjoint streams: different trajectories
+    for k in range(P):
+        f = forms[k]
+        if coding == "msc":
+            threads = {2: 1024, 4: 512}.get(f["cluster_ctas"], 256)
+            ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_MSC | k,
+                                           threads, f["tile"], max(1, f["cluster_ctas"]), iseq0=k << 40)
+        else:
+            assert f["spins_per_word"] == 32
+            ref = oracle.anneal_ssc_bits_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_SSC | k,
+                                                f["tile"], iseq0=k << 40)
+        compare_rows(got[k], ref[0], rtol=2e-10)

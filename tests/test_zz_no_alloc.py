@@ -77,3 +77,35 @@ def test_noalloc_rejects_oversize_population(cuda):
                                            p(buf), p(buf), out, None)
     assert st == 1
     assert b"exceeds the maximum" in pa.lib().pa_last_error(None)
+
+
+def test_noalloc_allocates_no_device_memory(cuda, oracle):
+    """What the entry point exists for: it takes no device memory.  After a
+    first call (which may load the library's device code), further calls
+    leave the device's free memory unchanged to the byte -- also with most of
+    that memory held by another allocation, as a caching allocator that has
+    reserved the device would hold it."""
+    torch = cuda
+    lib = pa.lib()
+    E, act = _energies(oracle, "msc", 16, 3000, 8, 0.4)
+    e_ref = float(E[act.astype(bool)].min())
+    args = (torch, E, act, pa.MSC, 3000, 6000, 0.4, 0.41, e_ref, pa.WEIGHTS_FP32, 8, 77)
+    first = _plan(lib.pa_resample_plan_noalloc, *args)
+    torch.cuda.synchronize()
+    # the buffers _plan creates come from torch's cache once it holds them
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(4):
+        again = _plan(lib.pa_resample_plan_noalloc, *args)
+        assert np.array_equal(again[0], first[0]) and again[5] == first[5]
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    hog = torch.empty(max(0, free0 - (4 << 30)), dtype=torch.uint8, device="cuda")
+    try:
+        free1 = torch.cuda.mem_get_info()[0]
+        again = _plan(lib.pa_resample_plan_noalloc, *args)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free1
+        assert np.array_equal(again[0], first[0])
+    finally:
+        del hog
+        torch.cuda.empty_cache()
