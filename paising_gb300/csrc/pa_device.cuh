@@ -48,11 +48,14 @@ __host__ __device__ __forceinline__ U4 philox10(uint32_t c0, uint32_t c1, uint32
   return U4{c0, c1, c2, c3};
 }
 
-// Philox4x32-10 with the key schedule k + r*W precomputed once per thread
-// (kk[2r], kk[2r+1] = round-r key); same output as philox10.
+// Philox4x32-10 with the key schedule k + r*W precomputed (k[2r], k[2r+1] =
+// round-r key); same output as philox10.  The sweep kernels take it as a
+// __grid_constant__ kernel parameter, computed on the host, so the round keys
+// are read from the parameter bank as instruction operands instead of being
+// held in (or recomputed into) registers.
 struct PhiloxKeys {
   uint32_t k[20];
-  __device__ __forceinline__ explicit PhiloxKeys(unsigned long long seed) {
+  __host__ __device__ __forceinline__ explicit PhiloxKeys(unsigned long long seed) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
       k[2 * r] = (uint32_t)seed + (uint32_t)r * kPhiloxW0;

@@ -169,7 +169,7 @@ static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the ti
 // while adding L = 96's form to it cost L = 64 1% (register allocation).
 template <int MODE, int FL>
 __global__ void __launch_bounds__(kSweepThreads, 4)
-    msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
+    msc_sweep_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeys keys) {
   extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
   __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMaxTile * kMsb], s_cntM[kMaxTile * kMsb];  // [group of the tile][bit]
@@ -179,7 +179,6 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int total = b->unit_prefix[b->npop];
-  const PhiloxKeys keys(stream_seed);
   int cur = -1;
   int tx = 0, rsub = 0, txl = 0, txr = 0;
   bool worker = false;
@@ -655,12 +654,12 @@ cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out, int fixed_
 cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
                              const SweepLaunch& sl, cudaStream_t s) {
   if (rng_mode == kRefCoords) {
-    msc_sweep_kernel<kRefCoords, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+    msc_sweep_kernel<kRefCoords, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
   } else {
     if (sl.fixed_l == 96)
-      msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+      msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
     else
-      msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+      msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
   }
   return cudaGetLastError();
 }

@@ -84,7 +84,7 @@ __device__ __noinline__ void cluster_count(const UnitParams& P, const uint32_t* 
 
 template <int MODE, int CS, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
-    msc_sweep_cluster_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
+    msc_sweep_cluster_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeys keys) {
   extern __shared__ __align__(16) uint32_t lat[];  // stripe of A (LR*Wr words), then stripe of B
   __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMsb], s_cntM[kMsb];
@@ -97,7 +97,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
   const int prev = (rank + CS - 1) % CS, next = (rank + 1) % CS;
   const int tid = threadIdx.x;
   const int total = b->unit_prefix[b->npop];
-  const PhiloxKeys keys(stream_seed);
   int cur = -1;
   int tx = 0, rsub = 0, txl = 0, txr = 0;
   bool worker = false;
@@ -350,7 +349,7 @@ static cudaError_t cluster_launch(BatchDev* b, int energy_only, unsigned long lo
   }
   cfg.gridDim = dim3(sl->grid);
   cfg.dynamicSmemBytes = sl->smem;
-  return cudaLaunchKernelEx(&cfg, fn, b, energy_only, seed);
+  return cudaLaunchKernelEx(&cfg, fn, b, energy_only, PhiloxKeys(seed));
 }
 
 template <int CS, int THREADS>
