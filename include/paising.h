@@ -252,8 +252,9 @@ PA_API int pa_set_population(pa_handle* h, const void* host);
 
 /* Final population of population `pop` after the last pa_run, in the same
  * layout (MSC groups as stored: after resampling, replica s is at group
- * s % rg, bit s / rg, PAisingMSC.cu:413-414).  *R receives the population
- * size; bytes is the capacity of host. */
+ * s / 32, bit s % 32 with the native stream, and at group s % rg, bit s / rg
+ * with the reference stream, PAisingMSC.cu:413-414).  *R receives the
+ * population size; bytes is the capacity of host. */
 PA_API int pa_get_population(const pa_handle* h, int pop, void* host, size_t bytes, int* R);
 
 /* Per-kernel device time of one run executed launch by launch with CUDA
@@ -365,6 +366,15 @@ PA_API int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, 
  * src[k*rg_new + j], rg_new = ceil(R_new/32); new_active filled. */
 PA_API int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R_new, uint32_t* new_words,
                     uint8_t* new_active, void* stream);
+
+/* The native stream's MSC gather (no counterpart in the reference): the
+ * engine's own stream places offspring s at slot s (group s / 32, bit s % 32)
+ * instead of the reference's s % rg_new, s / rg_new, so that a new word is
+ * assembled from a few shifted old words.  new bit s <- old replica src[s],
+ * s < R_new (src nondecreasing, values < R_old); old_words holds
+ * ceil(R_old/32) groups; new_active filled. */
+PA_API int pa_msc_resample_native(const uint32_t* old_words, int L, int R_old, const uint32_t* src, int R_new,
+                                  uint32_t* new_words, uint8_t* new_active, void* stream);
 
 #ifdef __cplusplus
 }

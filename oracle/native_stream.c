@@ -419,3 +419,25 @@ void or_ssc_sweep_native(int8_t* spins, int L, int R, int sweeps, uint32_t T4, u
             }
     }
 }
+
+/* The engine's MSC gather with its own stream (no counterpart in the
+ * reference): offspring s -- in the scan order of old linear slots
+ * 32 * group + bit -- goes to new slot s, i.e. group s / 32, bit s % 32
+ * (the reference places it at group s % rg_new, bit s / rg_new,
+ * PAisingMSC.cu:413-414, which only its own random stream needs).  Same
+ * arguments as or_msc_resample; new_active[s] = s < R_new. */
+void or_msc_resample_linear(const uint32_t* old, const int32_t* E_old, int L, int rg_old, const uint32_t* roff,
+                            const uint32_t* offs, int rg_new, uint32_t* neu, uint8_t* new_active, int32_t* E_new) {
+    const int N = L * L;
+    for (int i = 0; i < rg_new * 32; ++i) new_active[i] = 0;
+    for (int g = 0; g < rg_old; ++g)
+        for (int k = 0; k < 32; ++k)
+            for (uint32_t p = 0; p < roff[g * 32 + k]; ++p) {
+                const uint32_t s = offs[g * 32 + k] + p, nj = s / 32, nk = s % 32;
+                new_active[s] = 1;
+                if (E_new) E_new[s] = E_old[g * 32 + k];
+                const uint32_t* src = old + (size_t)g * N;
+                uint32_t* dst = neu + (size_t)nj * N;
+                for (int i = 0; i < N; ++i) dst[i] |= ((src[i] >> k) & 1u) << nk;
+            }
+}

@@ -487,6 +487,10 @@ int or_anneal2(int msc, int L, int Rinit, int sweeps, double dBinit, double Bfin
                int max_steps, int adaptive, double minov, double maxov, double* rows, int max_rows,
                double* fam, double* attempts);
 
+/* The engine's native-stream MSC gather (native_stream.c). */
+void or_msc_resample_linear(const uint32_t* old, const int32_t* E_old, int L, int rg_old, const uint32_t* roff,
+                            const uint32_t* offs, int rg_new, uint32_t* neu, uint8_t* new_active, int32_t* E_new);
+
 /* The engine's native-stream MSC sweeps (native_stream.c). */
 void or_msc_sweep_native2(uint32_t* words, int L, int rg, int sweeps, uint32_t T4, uint32_t T8, uint64_t key,
                           uint32_t step, uint32_t tag, int threads, int G, int cs);
@@ -654,11 +658,16 @@ static int anneal_impl(int msc, int L, int Rinit, int sweeps, double dBinit, dou
                 if ((int)Rnew > Rcap) { ret = -1; break; }
                 int rgn = (int)((Rnew + MSB - 1) / MSB);
                 memset(wd2, 0, (size_t)rgn * N * 4);
-                or_msc_resample(wd, Ev, L, rg, roff, offs, rgn, wd2, act2, NULL);
+                /* the engine's own stream places offspring s at slot s, the
+                 * reference's at group s % rgn, bit s / rgn */
+                if (nat)
+                    or_msc_resample_linear(wd, Ev, L, rg, roff, offs, rgn, wd2, act2, NULL);
+                else
+                    or_msc_resample(wd, Ev, L, rg, roff, offs, rgn, wd2, act2, NULL);
                 for (int lin = 0; lin < rg * MSB; ++lin)
                     for (uint32_t p = 0; p < roff[lin]; ++p) {
                         const uint32_t s = offs[lin] + p;
-                        anc2[(s % rgn) * MSB + s / rgn] = anc[lin];
+                        anc2[nat ? s : (s % rgn) * MSB + s / rgn] = anc[lin];
                     }
                 int32_t* ta2 = anc; anc = anc2; anc2 = ta2;
                 uint32_t* t = wd; wd = wd2; wd2 = t;

@@ -40,6 +40,7 @@ _SIGS = {
     "or_msc_q": ([_vp, _vp, _i, _d, _d], _d),
     "or_msc_copy_numbers": ([_vp, _vp, _i, _i, _i, _d, _d, _u64, _u64, _vp], _u32),
     "or_msc_resample": ([_vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp, _vp], None),
+    "or_msc_resample_linear": ([_vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp, _vp], None),
     "or_anneal": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _vp, _i, _vp], _i),
     "or_anneal2": ([_i, _i, _i, _i, _d, _d, _i, _u64, _i, _i, _d, _d, _vp, _i, _vp, _vp], _i),
     "or_kaufman": ([_i, _d, _vp, _vp, _vp], None),
@@ -215,6 +216,19 @@ def msc_resample(old: np.ndarray, L: int, roff, offs, Rnew: int):
     E0 = np.zeros(old.shape[0] * 32, dtype=np.int32)
     lib().or_msc_resample(_p(old), _p(E0), L, old.shape[0], _p(np.ascontiguousarray(roff, np.uint32)),
                           _p(np.ascontiguousarray(offs, np.uint32)), rgn, _p(new), _p(act), None)
+    return new, act
+
+
+def msc_resample_linear(old: np.ndarray, L: int, roff, offs, Rnew: int):
+    """The native stream's MSC placement: offspring s at slot s (group s // 32,
+    bit s % 32); native_stream.c."""
+    old = np.ascontiguousarray(old, dtype=np.uint32)
+    rgn = (Rnew + 31) // 32
+    new = np.zeros((rgn, L * L), dtype=np.uint32)
+    act = np.zeros(rgn * 32, dtype=np.uint8)
+    E0 = np.zeros(old.shape[0] * 32, dtype=np.int32)
+    lib().or_msc_resample_linear(_p(old), _p(E0), L, old.shape[0], _p(np.ascontiguousarray(roff, np.uint32)),
+                                 _p(np.ascontiguousarray(offs, np.uint32)), rgn, _p(new), _p(act), None)
     return new, act
 
 

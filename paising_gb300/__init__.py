@@ -109,6 +109,7 @@ _SIGS = {
     "pa_resample_plan_noalloc": ([_vp, _vp, _i, _i, _i, _i, _d, _d, _d, _i, _u64, _u64, _vp, _vp, _vp, _vp, _vp], _i),
     "pa_ssc_resample": ([_vp, _i, _vp, _i, _vp, _vp], _i),
     "pa_msc_resample": ([_vp, _i, _vp, _i, _vp, _vp, _vp], _i),
+    "pa_msc_resample_native": ([_vp, _i, _i, _vp, _i, _vp, _vp, _vp], _i),
 }
 
 _lib: ctypes.CDLL | None = None

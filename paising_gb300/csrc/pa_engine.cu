@@ -316,7 +316,7 @@ struct pa_handle {
     if ((e = launch("copy_numbers", [&] { return launch_copy_numbers(d_pops, npop, rblocks, stream); })) != cudaSuccess)
       return e;
     if ((e = launch("scatter", [&] { return launch_scatter(d_pops, npop, rblocks, stream); })) != cudaSuccess) return e;
-    e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_batch, coding, stream); });
+    e = launch(msc ? "msc_resample" : "ssc_resample", [&] { return launch_resample(d_batch, coding, rng_mode, stream); });
     if (e != cudaSuccess) return e;
     if (family && (e = launch("family_resample", [&] { return launch_family_resample(d_pops, npop, rblocks, stream); })) !=
                       cudaSuccess)
@@ -830,6 +830,10 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       h.spins[1] = b2;
       chk(B.alloc(&h.active[0], units));
       chk(B.alloc(&h.active[1], units));
+      if (c.rng_mode == PA_RNG_NATIVE) {  // the native stream's word-level gather
+        chk(B.alloc(&h.res_pairs, units));
+        chk(B.alloc(&h.res_cnt, (size_t)rgcap));
+      }
     } else {
       int8_t *a = nullptr, *b2 = nullptr;
       chk(B.alloc(&a, (size_t)Rcap * N));

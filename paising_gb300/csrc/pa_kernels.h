@@ -73,7 +73,7 @@ cudaError_t launch_copy_numbers(PopDev* pops, int npop, int blocks, cudaStream_t
 cudaError_t launch_scatter(PopDev* pops, int npop, int blocks, cudaStream_t s);
 // Gather of the resampled populations of the batch (a plan launch and a
 // persistent gather launch taking units of every population from one queue).
-cudaError_t launch_resample(BatchDev* b, int coding, cudaStream_t s);
+cudaError_t launch_resample(BatchDev* b, int coding, int rng_mode, cudaStream_t s);
 
 // Coding-specific launchers behind the generic ones above.
 cudaError_t ssc_sweep_setup(int rng_mode, int smem, SweepLaunch* out);
@@ -85,7 +85,7 @@ cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigne
 cudaError_t launch_ssc_init(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s);
 cudaError_t launch_ssc_resample(BatchDev* b, cudaStream_t s);
-cudaError_t launch_msc_resample(BatchDev* b, cudaStream_t s);
+cudaError_t launch_msc_resample(BatchDev* b, int rng_mode, cudaStream_t s);
 
 // SSC populations swept on bit planes (native stream): tiles of G replicas
 // packed to one bit per site in shared memory, a sublattice row as Wr words

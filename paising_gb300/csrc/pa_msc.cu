@@ -169,7 +169,8 @@ static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the ti
 // while adding L = 96's form to it cost L = 64 1% (register allocation).
 template <int MODE, int FL>
 __global__ void __launch_bounds__(kSweepThreads, 4)
-    msc_sweep_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeys keys) {
+    msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
+  const PhiloxKeys keys(stream_seed);
   extern __shared__ __align__(16) uint32_t lat[];  // G*N words: G sublattices A, then G sublattices B
   __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMaxTile * kMsb], s_cntM[kMaxTile * kMsb];  // [group of the tile][bit]
@@ -454,9 +455,9 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 }
 
 // -------------------------------------------------------------- resample
-// resampleKer places offspring number s (in the scan order of
-// (old group, bit)) at new group s % rg_new, bit s / rg_new
-// (PAisingMSC.cu:413-414).  Here every new word gathers its 32 bits:
+// Reference stream: resampleKer places offspring number s (in the scan order
+// of (old group, bit)) at new group s % rg_new, bit s / rg_new
+// (PAisingMSC.cu:413-414), which the reference-stream parity needs.  Here every new word gathers its 32 bits:
 // bit k of new group j comes from old replica src[k*rg_new + j].
 //
 // Work unit of one warp: 32 consecutive new groups (lane g builds group
@@ -479,22 +480,39 @@ __device__ __forceinline__ int res_strip(int N, int rgn) {
   return (long long)tiles * (N / 32) >= 8192 ? 32 : kSub;
 }
 
-__global__ void __launch_bounds__(1024) msc_resample_plan_kernel(BatchDev* b) {
+// Native stream gather (msc_resample_native_kernel): units of kNatGroups new
+// groups x 32 sites.
+constexpr int kNatGroups = 16;      // new groups per unit of the native gather
+constexpr int kNatBatch = 4;        // of which staged and gathered together
+constexpr int kNatThreads = 256;
+constexpr int kNatBlocksPerSM = 4;
+
+__device__ __forceinline__ int nat_units(int N, int rgn) { return ((rgn + kNatGroups - 1) / kNatGroups) * ((N + 31) / 32); }
+
+__global__ void __launch_bounds__(1024) msc_resample_plan_kernel(BatchDev* b, int native) {
   __shared__ uint32_t s_u[33];
   const int p = threadIdx.x, np = b->npop;
-  uint32_t units = 0;
+  uint32_t units = 0, groups = 0;
   if (p < np) {
     const PopDev* st = b->pops + p;
     if (st->coding == kMSC && pop_stepping(st)) {
       const int rgn = (st->R_cur + kMsb - 1) / kMsb, S = res_strip(st->N, rgn);
-      units = (uint32_t)(((rgn + 31) / 32) * ((st->N + S - 1) / S));
+      units = native ? (uint32_t)nat_units(st->N, rgn)
+                                      : (uint32_t)(((rgn + 31) / 32) * ((st->N + S - 1) / S));
+      groups = (uint32_t)rgn;
     }
   }
-  uint32_t total;
+  uint32_t total, gtotal;
   const uint32_t ex = block_exscan(units, s_u, &total);
-  if (p < np) b->res_prefix[p] = (int)ex;
+  __syncthreads();  // s_u is reused
+  const uint32_t gex = block_exscan(groups, s_u, &gtotal);
+  if (p < np) {
+    b->res_prefix[p] = (int)ex;
+    b->grp_prefix[p] = (int)gex;
+  }
   if (p == 0) {
     b->res_prefix[np] = (int)total;
+    b->grp_prefix[np] = (int)gtotal;
     b->res_next = 0;
   }
 }
@@ -569,6 +587,171 @@ __global__ void __launch_bounds__(kResampleThreads, kResampleBlocksPerSM) msc_re
         uint4* d4 = reinterpret_cast<uint4*>(dst + tc);
         d4[0] = make_uint4(w[0], w[1], w[2], w[3]);
         if (nv > 4) d4[1] = make_uint4(w[4], w[5], w[6], w[7]);
+      }
+    }
+  }
+}
+
+// --------------------------------------------- resample, native stream
+// With the engine's own stream the placement of offspring is free (replicas
+// are exchangeable), so offspring s goes to slot s: group s / 32, bit s % 32.
+// The sources of a new group's 32 bits are then 32 consecutive entries of the
+// monotone gather map, i.e. a window of old replicas that are mostly
+// consecutive themselves: with offsets o_b = src[32j + b] - 32 (first - 1),
+// first = src[32j] / 32, bit b of the new word is bit o_b of the bit string
+// W = old words first-1, first, first+1, first+2 at that site (W's word 0 is
+// never selected: o_b >= 32).  Bits sharing the shift d = o_b - b form one
+// mask M_d, and the new word is OR_d ((W >> d) & M_d), one funnel shift and
+// one logic operation per distinct shift instead of per bit.  Copy numbers
+// of 1 keep the shift; a duplicate lowers it by one, a replica without
+// offspring raises it, so a word has a handful of distinct shifts.
+//
+// msc_pairs_kernel (one warp per new group of every population, lane b for
+// bit b) lists a group's distinct shifts as (M_d, d mod 32) pairs ordered by
+// the window word d / 32 they start in (counts n0, n1, n2): the lanes sharing
+// a shift find each other with one match, and the lowest of them writes the
+// pair.  A group whose sources span more than the four-word window (more
+// than 64 replicas without offspring among ~96 consecutive ones) is flagged
+// and gathered bit by bit.
+__global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
+  const int lane = threadIdx.x & 31, np = b->npop, total = b->grp_prefix[np];
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total; i += (gridDim.x * blockDim.x) >> 5) {
+    int lo = 0, hi = np;  // population of new group i (warp-uniform)
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (b->grp_prefix[mid] <= i) lo = mid;
+      else hi = mid;
+    }
+    PopDev* st = b->pops + lo;
+    const int j = i - b->grp_prefix[lo], nb = min(kMsb, st->R_cur - j * kMsb);
+    const uint32_t* src = st->src + (size_t)j * kMsb;
+    const bool v = lane < nb;
+    // shift of bit b: d = src[b] - 32 (first - 1) - b >= 1 (src nondecreasing, src[0] >= 32 first)
+    const uint32_t base = ((src[0] >> 5) - 1u) * 32u;  // may wrap; only differences matter
+    const uint32_t d = v ? src[lane] - base - (uint32_t)lane : 0xFFFFFFFFu;
+    const bool fallback = __any_sync(kFull, v && d >= 96u);
+    const uint32_t m = __match_any_sync(kFull, d);  // bits sharing this shift (the invalid ones share 0xFFFFFFFF)
+    const bool leader = v && (m & lt) == 0u;
+    const uint32_t word = d >> 5;
+    const uint32_t l0 = __ballot_sync(kFull, leader && word == 0u), l1 = __ballot_sync(kFull, leader && word == 1u),
+                   l2 = __ballot_sync(kFull, leader && word == 2u);
+    const uint32_t n0 = __popc(l0), n1 = __popc(l1), n2 = __popc(l2);
+    if (!fallback && leader && word < 3u) {
+      const uint32_t at = word == 0u ? __popc(l0 & lt) : word == 1u ? n0 + __popc(l1 & lt) : n0 + n1 + __popc(l2 & lt);
+      st->res_pairs[(size_t)j * kMsb + at] = make_uint2(m, d & 31u);
+    }
+    if (lane == 0) st->res_cnt[j] = fallback ? 1u << 31 : n0 | n1 << 8 | n2 << 16;
+  }
+}
+
+// The gather.  A warp takes a unit of kNatGroups consecutive new groups x 32
+// consecutive sites, lane = site: every load and store is one coalesced
+// 128-byte row segment, and a group's pair list is the same for all lanes
+// (staged in shared memory kNatBatch groups at a time, read as broadcasts),
+// so no lane waits for another's longer list.  Units are spread over the
+// persistent warps by a grid stride (the batch-wide unit prefix gives each
+// population its range).
+__device__ __forceinline__ void nat_apply(uint32_t& out, uint32_t lo, uint32_t hi, const uint2* pg, int i0, int i1) {
+  int i = i0;
+#pragma unroll 1
+  for (; i + 1 < i1; i += 2) {
+    const uint2 a = pg[i], c = pg[i + 1];
+    out |= (__funnelshift_r(lo, hi, a.y) & a.x) | (__funnelshift_r(lo, hi, c.y) & c.x);
+  }
+  if (i < i1) {
+    const uint2 a = pg[i];
+    out |= __funnelshift_r(lo, hi, a.y) & a.x;
+  }
+}
+
+__global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_native_kernel(BatchDev* b) {
+  __shared__ uint2 s_pairs[kNatThreads / 32][kNatBatch * kMsb];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint2* sp = s_pairs[wid];
+  const int total = b->res_prefix[b->npop];
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += nwarps) {
+    int lo = 0, hi = b->npop;  // population of unit u (warp-uniform)
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (b->res_prefix[mid] <= u) lo = mid;
+      else hi = mid;
+    }
+    const PopDev* st = b->pops + lo;
+    const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb, nstrip = (N + 31) / 32;
+    const int loc = u - b->res_prefix[lo], tile = loc / nstrip, strip = loc - tile * nstrip;
+    const int j0 = tile * kNatGroups, ng = min(kNatGroups, rgn - j0);
+    const int t = strip * 32 + lane;
+    const bool tv = t < N;
+    const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1] + t;  // this lane's site in old group 0
+    uint32_t* neu = (uint32_t*)st->spins[st->parity] + t;
+    const uint32_t* src = st->src;
+    const int gmax = st->rgcap - 1;
+    // lane g < ng: count word and window start of group j0 + g
+    uint32_t cnt_l = 0u;
+    int first_l = 0;
+    if (lane < ng) {
+      cnt_l = st->res_cnt[j0 + lane];
+      first_l = (int)(src[(size_t)(j0 + lane) * kMsb] >> 5);
+    }
+    if (strip == 0) {  // active flags: lane = bit
+      uint8_t* act = st->active[st->parity];
+      for (int g = 0; g < ng; ++g) act[(j0 + g) * kMsb + lane] = ((j0 + g) * kMsb + lane) < Rn ? 1 : 0;
+    }
+#pragma unroll 1
+    for (int g0 = 0; g0 < ng; g0 += kNatBatch) {
+      const int nbat = min(kNatBatch, ng - g0);
+      __syncwarp();  // the previous batch is done with the staged pairs
+      {  // pair lists of groups j0+g0 .. (contiguous, kMsb slots each) into shared memory
+        const uint4* gp = reinterpret_cast<const uint4*>(st->res_pairs + (size_t)(j0 + g0) * kMsb);
+        uint4* s4 = reinterpret_cast<uint4*>(sp);
+#pragma unroll
+        for (int k = lane; k < kNatBatch * kMsb / 2; k += 32)
+          if (k < nbat * kMsb / 2) s4[k] = __ldg(gp + k);
+      }
+      uint32_t W[kNatBatch][4];
+#pragma unroll
+      for (int g = 0; g < kNatBatch; ++g) {
+        const int first = __shfl_sync(kFull, first_l, g0 + g);
+        if (g < nbat && tv) {
+          if (first >= 1 && first + 2 <= gmax) {  // warp-uniform: the window lies inside the buffer
+            const uint32_t* r = old + (size_t)(first - 1) * N;
+            W[g][0] = __ldg(r);
+            W[g][1] = __ldg(r + N);
+            W[g][2] = __ldg(r + 2 * N);
+            W[g][3] = __ldg(r + 3 * N);
+          } else {  // clamped rows are never selected
+#pragma unroll
+            for (int q = 0; q < 4; ++q) W[g][q] = __ldg(old + (size_t)min(max(first - 1 + q, 0), gmax) * N);
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) W[g][q] = 0u;
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int g = 0; g < kNatBatch; ++g) {
+        if (g >= nbat) break;  // warp-uniform
+        const uint32_t cnt = __shfl_sync(kFull, cnt_l, g0 + g);
+        const int n0 = cnt & 0xff, n01 = n0 + ((cnt >> 8) & 0xff), n012 = n01 + ((cnt >> 16) & 0xff);
+        const uint2* pg = sp + g * kMsb;
+        uint32_t out = 0u;
+        nat_apply(out, W[g][0], W[g][1], pg, 0, n0);
+        nat_apply(out, W[g][1], W[g][2], pg, n0, n01);
+        nat_apply(out, W[g][2], W[g][3], pg, n01, n012);
+        const int j = j0 + g0 + g;
+        if (cnt >> 31) {  // sources beyond the window: bit by bit (warp-uniform)
+          const int nb = min(kMsb, Rn - j * kMsb);
+#pragma unroll 1
+          for (int bb = 0; bb < nb; ++bb) {
+            const uint32_t lin = src[(size_t)j * kMsb + bb];
+            const uint32_t v = tv ? __ldg(old + (size_t)(lin >> 5) * N) : 0u;
+            out |= ((v >> (lin & 31u)) & 1u) << bb;
+          }
+        }
+        if (tv) neu[(size_t)j * N] = out;
       }
     }
   }
@@ -654,12 +837,12 @@ cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out, int fixed_
 cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
                              const SweepLaunch& sl, cudaStream_t s) {
   if (rng_mode == kRefCoords) {
-    msc_sweep_kernel<kRefCoords, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
+    msc_sweep_kernel<kRefCoords, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   } else {
     if (sl.fixed_l == 96)
-      msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
+      msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
     else
-      msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
+      msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   }
   return cudaGetLastError();
 }
@@ -669,14 +852,20 @@ cudaError_t launch_msc_init(PopDev* pops, int npop, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_msc_resample(BatchDev* b, cudaStream_t s) {
+cudaError_t launch_msc_resample(BatchDev* b, int rng_mode, cudaStream_t s) {
   int dev, nsm;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  msc_resample_plan_kernel<<<1, 1024, 0, s>>>(b);
+  msc_resample_plan_kernel<<<1, 1024, 0, s>>>(b, rng_mode == kNative ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  msc_resample_kernel<<<nsm * kResampleBlocksPerSM, kResampleThreads, 0, s>>>(b);  // persistent warps
+  if (rng_mode == kRefCoords) {
+    msc_resample_kernel<<<nsm * kResampleBlocksPerSM, kResampleThreads, 0, s>>>(b);  // persistent warps
+    return cudaGetLastError();
+  }
+  msc_pairs_kernel<<<nsm * 8, 256, 0, s>>>(b);  // a warp per new group, grid-stride
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  msc_resample_native_kernel<<<nsm * kNatBlocksPerSM, kNatThreads, 0, s>>>(b);
   return cudaGetLastError();
 }
 

@@ -84,7 +84,8 @@ __device__ __noinline__ void cluster_count(const UnitParams& P, const uint32_t* 
 
 template <int MODE, int CS, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
-    msc_sweep_cluster_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeys keys) {
+    msc_sweep_cluster_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
+  const PhiloxKeys keys(stream_seed);
   extern __shared__ __align__(16) uint32_t lat[];  // stripe of A (LR*Wr words), then stripe of B
   __shared__ int s_unit, s_pop;
   __shared__ int s_cntE[kMsb], s_cntM[kMsb];
@@ -349,7 +350,7 @@ static cudaError_t cluster_launch(BatchDev* b, int energy_only, unsigned long lo
   }
   cfg.gridDim = dim3(sl->grid);
   cfg.dynamicSmemBytes = sl->smem;
-  return cudaLaunchKernelEx(&cfg, fn, b, energy_only, PhiloxKeys(seed));
+  return cudaLaunchKernelEx(&cfg, fn, b, energy_only, seed);
 }
 
 template <int CS, int THREADS>

@@ -299,8 +299,9 @@ __global__ void family_init_kernel(PopDev* pops) {
 }
 
 // After the spin gather of a temperature step: new replica slots take the
-// ancestor of their source (SSC: slot s <- src[s]; MSC: slot 32 g + b holds
-// offspring s = b rg_new + g, PAisingMSC.cu:413-414).
+// ancestor of their source (SSC, and MSC with the native stream: slot s <-
+// src[s]; MSC with the reference stream: slot 32 g + b holds offspring
+// s = b rg_new + g, PAisingMSC.cu:413-414).
 __global__ void family_resample_kernel(PopDev* pops) {
   PopDev* st = pops + blockIdx.y;
   if (!st->family || !pop_stepping(st)) return;
@@ -308,10 +309,10 @@ __global__ void family_resample_kernel(PopDev* pops) {
   const int32_t* old = st->anc[st->parity ^ 1];
   int32_t* neu = st->anc[st->parity];
   const uint32_t* src = st->src;
-  const bool msc = st->coding == kMSC;
+  const bool transposed = st->coding == kMSC && st->rng_mode == kRefCoords;
   const int rgn = (Rn + kMsb - 1) / kMsb;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const int s = msc ? (j & (kMsb - 1)) * rgn + (j >> 5) : j;
+    const int s = transposed ? (j & (kMsb - 1)) * rgn + (j >> 5) : j;
     neu[j] = s < Rn ? old[src[s]] : -1;
   }
 }
@@ -584,8 +585,8 @@ cudaError_t launch_init(PopDev* pops, int npop, int coding, cudaStream_t s) {
   return coding == kMSC ? launch_msc_init(pops, npop, s) : launch_ssc_init(pops, npop, s);
 }
 
-cudaError_t launch_resample(BatchDev* b, int coding, cudaStream_t s) {
-  return coding == kMSC ? launch_msc_resample(b, s) : launch_ssc_resample(b, s);
+cudaError_t launch_resample(BatchDev* b, int coding, int rng_mode, cudaStream_t s) {
+  return coding == kMSC ? launch_msc_resample(b, rng_mode, s) : launch_ssc_resample(b, s);
 }
 
 cudaError_t launch_q(PopDev* pops, int npop, int blocks, cudaStream_t s) {

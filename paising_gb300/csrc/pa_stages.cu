@@ -258,7 +258,7 @@ int pa_ssc_resample(const int8_t* old_spins, int L, const uint32_t* src, int R_n
   h.src = const_cast<uint32_t*>(src);
   int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  return finish(launch_resample(S.b, kSSC, s), s, "ssc_resample");
+  return finish(launch_resample(S.b, kSSC, kRefCoords, s), s, "ssc_resample");
 }
 
 int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R_new, uint32_t* new_words,
@@ -277,7 +277,37 @@ int pa_msc_resample(const uint32_t* old_words, int L, const uint32_t* src, int R
   h.src = const_cast<uint32_t*>(src);
   int rc = upload(S, h, nullptr, nullptr, s);
   if (rc) return rc;
-  return finish(launch_resample(S.b, kMSC, s), s, "msc_resample");
+  return finish(launch_resample(S.b, kMSC, kRefCoords, s), s, "msc_resample");
+}
+
+int pa_msc_resample_native(const uint32_t* old_words, int L, int R_old, const uint32_t* src, int R_new,
+                           uint32_t* new_words, uint8_t* new_active, void* stream) {
+  SweepGeom g;
+  (void)g;
+  if (!old_words || !src || !new_words || !new_active || R_old < 1 || R_new < 1 || L < 4 || L % 2 || L > 256)
+    return PA_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  Scratch S;
+  cudaError_t e = S.alloc();
+  if (e != cudaSuccess) return stage_fail(e, "scratch");
+  const int rg_new = (R_new + kMsb - 1) / kMsb;
+  void* pairs = nullptr;  // pair lists and counts of the new groups
+  e = cudaMalloc(&pairs, (size_t)rg_new * (kMsb * sizeof(uint2) + sizeof(uint32_t)));
+  if (e != cudaSuccess) return stage_fail(e, "pair scratch");
+  PopDev h = base_state(kMSC, L);
+  h.rng_mode = kNative;
+  h.spins[0] = new_words;
+  h.spins[1] = const_cast<uint32_t*>(old_words);
+  h.active[0] = new_active;
+  h.rgcap = (R_old + kMsb - 1) / kMsb;  // groups the old buffer holds
+  h.R_cur = R_new;
+  h.src = const_cast<uint32_t*>(src);
+  h.res_pairs = static_cast<uint2*>(pairs);
+  h.res_cnt = reinterpret_cast<uint32_t*>(static_cast<uint2*>(pairs) + (size_t)rg_new * kMsb);
+  int rc = upload(S, h, nullptr, nullptr, s);
+  if (rc == PA_OK) rc = finish(launch_resample(S.b, kMSC, kNative, s), s, "msc_resample_native");
+  cudaFree(pairs);
+  return rc;
 }
 
 }  // extern "C"

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector_types.h>
 
 namespace pa {
 
@@ -92,6 +93,12 @@ struct PopDev {
   uint32_t* fam_cnt;   // [Rinit] replicas per family; zero between temperatures
   double* fam_rows;    // [rows][3] families, rho_t, S_f per temperature
   double* fam_part;    // [kResBlocksMax][3] per-block partial sums
+  // ------------------------------------------------ MSC gather, native stream
+  // (offspring s at slot s = 32 * group + bit): per new group the distinct
+  // source shifts of its bits as (bit mask, shift) pairs, grouped by which
+  // pair of window words they read, and their counts (msc_pairs_kernel)
+  uint2* res_pairs;    // [rgcap][32]
+  uint32_t* res_cnt;   // [rgcap]: n0 | n1 << 8 | n2 << 16 | per-bit fallback << 31
 };
 
 constexpr int kRecMhr = 1, kRecEnergies = 2;
@@ -112,6 +119,7 @@ struct BatchDev {
   // the MSC resampling gather's work list: units of 32 new groups x 32 sites
   unsigned int res_next;
   int res_prefix[kMaxPop + 1];
+  int grp_prefix[kMaxPop + 1];  // new groups of the populations before p (native-stream pair pass)
 };
 
 // A population takes part in the current temperature step.

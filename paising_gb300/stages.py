@@ -12,7 +12,8 @@ import torch
 
 from . import SSC, MSC, PaisingError, lib
 
-__all__ = ["ssc_init", "ssc_sweep", "ssc_sweep_bits", "msc_init", "msc_sweep", "resample_plan", "ssc_resample", "msc_resample"]
+__all__ = ["ssc_init", "ssc_sweep", "ssc_sweep_bits", "msc_init", "msc_sweep", "resample_plan", "ssc_resample", "msc_resample",
+           "msc_resample_native"]
 
 
 def _ptr(t: torch.Tensor | None):
@@ -102,4 +103,13 @@ def msc_resample(old: torch.Tensor, L: int, src: torch.Tensor, R_new: int):
     new = torch.empty((rgn, L * L), dtype=torch.int32, device=old.device)
     act = torch.empty(rgn * 32, dtype=torch.uint8, device=old.device)
     _check(lib().pa_msc_resample(_ptr(old), L, _ptr(src), R_new, _ptr(new), _ptr(act), _stream()))
+    return new, act
+
+
+def msc_resample_native(old: torch.Tensor, L: int, R_old: int, src: torch.Tensor, R_new: int):
+    """The native stream's gather: offspring s at slot s (group s // 32, bit s % 32)."""
+    rgn = (R_new + 31) // 32
+    new = torch.empty((rgn, L * L), dtype=torch.int32, device=old.device)
+    act = torch.empty(rgn * 32, dtype=torch.uint8, device=old.device)
+    _check(lib().pa_msc_resample_native(_ptr(old), L, R_old, _ptr(src), R_new, _ptr(new), _ptr(act), _stream()))
     return new, act

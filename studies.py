@@ -88,8 +88,11 @@ def batch(seed: int = 2026, coding: str = "msc") -> dict:
             wall = time.perf_counter() - t0
             ms, att = e.timing()
             spw = e.sweep_form(0)["spins_per_word"]
+            prof = e.profile()
+        tot = sum(v[1] for v in prof.values())
         res[form] = {"device_s": ms / 1e3, "wall_s": wall, "attempts_per_ns": att / (ms * 1e6),
-                     "spins_per_word": spw}
+                     "spins_per_word": spw,
+                     "kernel_share": {k: round(v[1] / tot, 4) for k, v in prof.items()}}
         if tune:
             res[form]["autotune_s"] = tune_s
             res[form]["tiles_by_L"] = {str(p["L"]): t for p, t in zip(pops, tiles)}

@@ -59,15 +59,15 @@ def _family_stats_of(sizes: np.ndarray):
 
 def _replica_lattices(coding: str, pop: np.ndarray, R: int, L: int) -> np.ndarray:
     """Active replicas of a population read back with pa_get_population, one
-    row of bytes per replica.  MSC slot (g, b) holds offspring s = b * rg + g
-    (PAisingMSC.cu:413-414) and is active when s < R."""
+    row of bytes per replica.  With the engine's own stream MSC slot (g, b)
+    holds offspring s = 32 g + b and is active when s < R."""
     if coding == "ssc":
         return pop[:R].astype(np.int8)
     rg = pop.shape[0]
     out = []
     for g in range(rg):
         for b in range(32):
-            if b * rg + g < R:
+            if 32 * g + b < R:
                 out.append(((pop[g] >> np.uint32(b)) & np.uint32(1)).astype(np.int8))
     return np.array(out)
 

@@ -156,6 +156,45 @@ def test_msc_resample_gather(cuda, st, oracle, L, R):
     assert np.array_equal(nact.cpu().numpy(), oact)
 
 
+@pytest.mark.parametrize("L,R,kind", [(16, 200, "mixed"), (12, 70, "mixed"), (64, 3000, "mixed"),
+                                      (64, 5000, "identity"), (32, 4000, "sparse"), (128, 700, "bursty"),
+                                      (10, 33, "mixed"), (256, 100, "mixed"), (16, 900, "gap")])
+def test_msc_resample_gather_native(cuda, st, oracle, L, R, kind):
+    """The native stream's gather (offspring s at slot s) equals the oracle's
+    restatement bit for bit, active flags included: copy numbers of 0..3
+    (mixed), all 1 (every word one shift), mostly 0 with some 4s (sparse:
+    sources far apart, many per-bit fallbacks), and runs of 0 and of 3
+    (bursty: long duplicate runs), and one run of 150 replicas without
+    offspring (gap: sources beyond the four-word window, gathered bit by
+    bit)."""
+    torch = cuda
+    old, act = oracle.msc_init(L, R, 4, 0)
+    rng = np.random.default_rng(R + L)
+    n = len(act)
+    if kind == "mixed":
+        roff = rng.integers(0, 4, n)
+    elif kind == "identity":
+        roff = np.ones(n, dtype=np.int64)
+    elif kind == "sparse":
+        roff = np.where(rng.random(n) < 0.2, 4, 0)
+    elif kind == "bursty":
+        roff = np.repeat(rng.choice([0, 1, 3], size=n // 40 + 1, p=[0.4, 0.3, 0.3]), 40)[:n]
+    else:  # one copy each, but 150 replicas in a row without offspring
+        roff = np.ones(n, dtype=np.int64)
+        roff[300:450] = 0
+    roff = (roff * act).astype(np.uint32)
+    offs, tot = oracle.scan(roff)
+    assert tot > 0
+    src = np.repeat(np.arange(n), roff).astype(np.int32)
+    new, nact = st.msc_resample_native(torch.from_numpy(old.view(np.int32)).cuda(), L, R,
+                                       torch.from_numpy(src).cuda(), tot)
+    onew, oact = oracle.msc_resample_linear(old, L, roff, offs, tot)
+    assert np.array_equal(nact.cpu().numpy(), oact)
+    got = msc_words_np(new)
+    bad = np.nonzero((got != onew).any(axis=1))[0]
+    assert bad.size == 0, f"{bad.size} of {len(onew)} groups differ, first {bad[:5]}"
+
+
 @pytest.mark.parametrize("coding", ["ssc", "msc"])
 @pytest.mark.parametrize("beta", [0.25, 0.6])
 def test_native_acceptance_probability(cuda, st, oracle, coding, beta):
