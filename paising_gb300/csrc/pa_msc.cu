@@ -481,13 +481,17 @@ __device__ __forceinline__ int res_strip(int N, int rgn) {
 }
 
 // Native stream gather (msc_resample_native_kernel): units of kNatGroups new
-// groups x 32 sites.
+// groups x kNatSites sites.
 constexpr int kNatGroups = 16;      // new groups per unit of the native gather
-constexpr int kNatBatch = 4;        // of which staged and gathered together
+constexpr int kNatBatch = 2;        // of which staged and gathered together
 constexpr int kNatThreads = 256;
 constexpr int kNatBlocksPerSM = 4;
 
-__device__ __forceinline__ int nat_units(int N, int rgn) { return ((rgn + kNatGroups - 1) / kNatGroups) * ((N + 31) / 32); }
+constexpr int kNatSites = 64;       // sites per unit (two per lane)
+
+__device__ __forceinline__ int nat_units(int N, int rgn) {
+  return ((rgn + kNatGroups - 1) / kNatGroups) * ((N + kNatSites - 1) / kNatSites);
+}
 
 __global__ void __launch_bounds__(1024) msc_resample_plan_kernel(BatchDev* b, int native) {
   __shared__ uint32_t s_u[33];
@@ -645,23 +649,20 @@ __global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
   }
 }
 
-// The gather.  A warp takes a unit of kNatGroups consecutive new groups x 32
-// consecutive sites, lane = site: every load and store is one coalesced
-// 128-byte row segment, and a group's pair list is the same for all lanes
-// (staged in shared memory kNatBatch groups at a time, read as broadcasts),
-// so no lane waits for another's longer list.  Units are spread over the
-// persistent warps by a grid stride (the batch-wide unit prefix gives each
-// population its range).
-__device__ __forceinline__ void nat_apply(uint32_t& out, uint32_t lo, uint32_t hi, const uint2* pg, int i0, int i1) {
-  int i = i0;
+// The gather.  A warp takes a unit of kNatGroups consecutive new groups x 64
+// consecutive sites, lane = sites t and t + 32: every load and store is a
+// coalesced 128-byte row segment, and a group's pair list is the same for
+// all lanes (staged in shared memory kNatBatch groups at a time, read as
+// broadcasts), so no lane waits for another's longer list.  Units are spread
+// over the persistent warps by a grid stride (the batch-wide unit prefix
+// gives each population its range).
+__device__ __forceinline__ void nat_apply(uint32_t (&out)[2], const uint32_t (&lo)[2], const uint32_t (&hi)[2],
+                                          const uint2* pg, int i0, int i1) {
 #pragma unroll 1
-  for (; i + 1 < i1; i += 2) {
-    const uint2 a = pg[i], c = pg[i + 1];
-    out |= (__funnelshift_r(lo, hi, a.y) & a.x) | (__funnelshift_r(lo, hi, c.y) & c.x);
-  }
-  if (i < i1) {
+  for (int i = i0; i < i1; ++i) {
     const uint2 a = pg[i];
-    out |= __funnelshift_r(lo, hi, a.y) & a.x;
+    out[0] |= __funnelshift_r(lo[0], hi[0], a.y) & a.x;
+    out[1] |= __funnelshift_r(lo[1], hi[1], a.y) & a.x;
   }
 }
 
@@ -679,12 +680,12 @@ __global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_nat
       else hi = mid;
     }
     const PopDev* st = b->pops + lo;
-    const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb, nstrip = (N + 31) / 32;
+    const int N = st->N, Rn = st->R_cur, rgn = (Rn + kMsb - 1) / kMsb, nstrip = (N + kNatSites - 1) / kNatSites;
     const int loc = u - b->res_prefix[lo], tile = loc / nstrip, strip = loc - tile * nstrip;
     const int j0 = tile * kNatGroups, ng = min(kNatGroups, rgn - j0);
-    const int t = strip * 32 + lane;
-    const bool tv = t < N;
-    const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1] + t;  // this lane's site in old group 0
+    const int t = strip * kNatSites + lane;
+    const bool tv0 = t < N, tv1 = t + 32 < N;
+    const uint32_t* old = (const uint32_t*)st->spins[st->parity ^ 1] + t;  // this lane's first site in old group 0
     uint32_t* neu = (uint32_t*)st->spins[st->parity] + t;
     const uint32_t* src = st->src;
     const int gmax = st->rgcap - 1;
@@ -710,24 +711,20 @@ __global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_nat
         for (int k = lane; k < kNatBatch * kMsb / 2; k += 32)
           if (k < nbat * kMsb / 2) s4[k] = __ldg(gp + k);
       }
-      uint32_t W[kNatBatch][4];
+      uint32_t W[kNatBatch][4][2];
 #pragma unroll
       for (int g = 0; g < kNatBatch; ++g) {
         const int first = __shfl_sync(kFull, first_l, g0 + g);
-        if (g < nbat && tv) {
-          if (first >= 1 && first + 2 <= gmax) {  // warp-uniform: the window lies inside the buffer
-            const uint32_t* r = old + (size_t)(first - 1) * N;
-            W[g][0] = __ldg(r);
-            W[g][1] = __ldg(r + N);
-            W[g][2] = __ldg(r + 2 * N);
-            W[g][3] = __ldg(r + 3 * N);
-          } else {  // clamped rows are never selected
+        if (g < nbat) {
+          // the window's rows (clamped rows are never selected by a mask)
+          const bool inside = first >= 1 && first + 2 <= gmax;  // warp-uniform
+          const uint32_t* r = old + (size_t)(inside ? first - 1 : 0) * N;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) W[g][q] = __ldg(old + (size_t)min(max(first - 1 + q, 0), gmax) * N);
+          for (int q = 0; q < 4; ++q) {
+            const uint32_t* rq = inside ? r + (size_t)q * N : old + (size_t)min(max(first - 1 + q, 0), gmax) * N;
+            W[g][q][0] = tv0 ? __ldg(rq) : 0u;
+            W[g][q][1] = tv1 ? __ldg(rq + 32) : 0u;
           }
-        } else {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) W[g][q] = 0u;
         }
       }
       __syncwarp();
@@ -737,7 +734,7 @@ __global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_nat
         const uint32_t cnt = __shfl_sync(kFull, cnt_l, g0 + g);
         const int n0 = cnt & 0xff, n01 = n0 + ((cnt >> 8) & 0xff), n012 = n01 + ((cnt >> 16) & 0xff);
         const uint2* pg = sp + g * kMsb;
-        uint32_t out = 0u;
+        uint32_t out[2] = {0u, 0u};
         nat_apply(out, W[g][0], W[g][1], pg, 0, n0);
         nat_apply(out, W[g][1], W[g][2], pg, n0, n01);
         nat_apply(out, W[g][2], W[g][3], pg, n01, n012);
@@ -747,11 +744,15 @@ __global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_nat
 #pragma unroll 1
           for (int bb = 0; bb < nb; ++bb) {
             const uint32_t lin = src[(size_t)j * kMsb + bb];
-            const uint32_t v = tv ? __ldg(old + (size_t)(lin >> 5) * N) : 0u;
-            out |= ((v >> (lin & 31u)) & 1u) << bb;
+            const uint32_t* rl = old + (size_t)(lin >> 5) * N;
+            const uint32_t v0 = tv0 ? __ldg(rl) : 0u, v1 = tv1 ? __ldg(rl + 32) : 0u;
+            out[0] |= ((v0 >> (lin & 31u)) & 1u) << bb;
+            out[1] |= ((v1 >> (lin & 31u)) & 1u) << bb;
           }
         }
-        if (tv) neu[(size_t)j * N] = out;
+        uint32_t* d = neu + (size_t)j * N;
+        if (tv0) d[0] = out[0];
+        if (tv1) d[32] = out[1];
       }
     }
   }
