@@ -199,8 +199,8 @@ def run_ours(a):
     nsteps = eng.num_rows() - 1
     # one launch sequence serves all P populations: 5 kernels to initialise,
     # 8 per temperature (q, copy numbers, scatter, gather plan, gather, sweep
-    # plan, sweep, finish)
-    launches_per_run = 5 + 8 * nsteps
+    # plan, sweep, finish), 9 for MSC (the gather's pair-list pass)
+    launches_per_run = 5 + (9 if a.coding == "msc" else 8) * nsteps
 
     def barrier():
         if dist:

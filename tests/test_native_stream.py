@@ -240,16 +240,22 @@ def test_ssc_anneal_native_stream_int8(cuda, oracle, L, R, variant):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("coding", ["msc", "ssc"])
-def test_native_batch_each_population_equals_oracle(cuda, oracle, coding):
+@pytest.mark.parametrize("coding,L,R,P,sweeps,dbeta", [
+    ("msc", 64, 2000, 4, 2, 0.05), ("ssc", 64, 2000, 4, 2, 0.05),
+    ("msc", 16, 700, 3, 3, 0.1), ("msc", 96, 300, 2, 2, 0.1), ("msc", 128, 200, 2, 2, 0.2),
+    ("msc", 256, 64, 2, 1, 0.25), ("ssc", 32, 500, 3, 3, 0.1), ("ssc", 128, 150, 2, 2, 0.2)])
+def test_native_batch_each_population_equals_oracle(cuda, oracle, coding, L, R, P, sweeps, dbeta):
     """The batched form the benchmark times (runs=P concurrent populations of
     one configuration in one launch sequence, native stream, graph), here
     with FP64 weights so that every R_i must agree exactly: population k
     equals the oracle's anneal started at subsequence k << 40 with sweep tag
-    | k, row for row.  The reference's -M runs (PAisingMSC.cu:583,784) are
+    | k, row for row -- at the headline's L=64 in both codings and in the
+    other sweep forms a batch can take (stacked MSC tiles at L=16, the L=96
+    kernel, L=128, clusters at L=256, SSC segments at L=32, two-word SSC rows
+    at L=128).  The reference's -M runs (PAisingMSC.cu:583,784) are
     the sequential form this batching generalises."""
     from conftest import compare_rows
-    L, R, P, seed, sweeps, dbeta = 64, 2000, 4, 4242, 2, 0.05
+    seed = 4242 + L
     with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=1.0, runs=P, seed=seed, coding=coding,
                    rng="native", weights="fp64", graph=True, device=0) as e:
         e.run()
