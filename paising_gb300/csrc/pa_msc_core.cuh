@@ -94,8 +94,9 @@ constexpr uint32_t kFinishTagFlip = 0x20u << 24;
 // are finished one at a time by finish_bit, four per Philox block (counter
 // (c0, c1 | (fsub + k), step, tag ^ kFinishTagFlip), k = 0..7, enough for all
 // 32 bits).  Returns the bits decided "less".
+template <class Keys>
 __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uint32_t c0, uint32_t c1, uint32_t sub,
-                                                  uint32_t fsub, uint32_t step, uint32_t tag, const PhiloxKeys& K,
+                                                  uint32_t fsub, uint32_t step, uint32_t tag, const Keys& K,
                                                   const uint2* dig, uint32_t T4, uint32_t T8) {
   // no vote first: some lane of the warp nearly always has undecided bits
   // here (and the overflow path only calls when one has); a lane without
@@ -135,9 +136,11 @@ __device__ __forceinline__ uint32_t finish_digits(uint32_t und, uint32_t am, uin
 //   acc[k] : accepted bits (in: outright accepts; out: all accepts)
 //   nvalid : block-uniform count of the leading slots that hold sites; the
 //            other slots have und = 0 and draw nothing
+//   K      : PhiloxKeys or PhiloxKeysWide (the same stream, two code forms)
+template <class Keys>
 __device__ __forceinline__ void accept_native(const uint32_t (&a)[kKB], uint32_t (&und)[kKB], uint32_t (&acc)[kKB],
                                               const uint32_t (&site)[kKB], uint32_t chain_c0, uint32_t c1,
-                                              uint32_t step, uint32_t tag, const PhiloxKeys& K, const uint2* dig,
+                                              uint32_t step, uint32_t tag, const Keys& K, const uint2* dig,
                                               int nvalid, uint32_t T4, uint32_t T8) {
   // independent Philox chains of the kKB sites, interleaved by the compiler
   const uint2 d0 = dig[0], d1 = dig[1], d2 = dig[2], d3 = dig[3];

@@ -241,7 +241,7 @@ double ssc_bits_fill(int L) {
 }
 
 __global__ void __launch_bounds__(kSweepThreads, 4)
-    ssc_sweep_bits_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeys keys) {
+    ssc_sweep_bits_kernel(BatchDev* b, int energy_only, const __grid_constant__ PhiloxKeysWide keys) {
   extern __shared__ __align__(16) uint32_t pl[];  // [X][word group][y][c]: plane X, row y, word c
   __shared__ int s_unit, s_pop;
   __shared__ uint2 s_dig[kMsb];
@@ -438,7 +438,7 @@ cudaError_t ssc_bits_setup(int smem, SweepLaunch* out) {
 
 cudaError_t launch_ssc_bits_sweep(BatchDev* b, int energy_only, unsigned long long seed, const SweepLaunch& sl,
                                   cudaStream_t s) {
-  ssc_sweep_bits_kernel<<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeys(seed));
+  ssc_sweep_bits_kernel<<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, PhiloxKeysWide(seed));
   return cudaGetLastError();
 }
 
