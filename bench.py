@@ -158,6 +158,31 @@ def reduce_over_ranks(dist, device, elapsed: float, attempts: float):
     return mx[0].item(), t[1].item()
 
 
+# ------------------------------------------------------------- the workload
+def schedule_steps(dbeta: float, beta_final: float) -> int:
+    """Temperatures after beta = 0 of the reference's schedule: beta
+    accumulated as B[i] = B[i-1] + dbeta while B[i] <= beta_final
+    (PAisingSSC.cu:508-510)."""
+    b, n = 0.0, 0
+    while b + dbeta <= beta_final and n < 10000:
+        b += dbeta
+        n += 1
+    return n
+
+
+def workload_config(a, ws: int) -> dict:
+    """The workload both arms run, described identically: P independent
+    populations of the anneal per step (how an arm schedules them is
+    reported outside this dict)."""
+    P = a.populations
+    nsteps = schedule_steps(a.dbeta, a.beta_final)
+    return {"workload": f"PA anneal {a.coding.upper()} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} beta 0->"
+                        f"{a.beta_final} ({nsteps} temperatures), {P} independent population(s) per step",
+            "L": a.L, "R": a.R, "sweeps": a.sweeps, "dbeta": a.dbeta, "beta_final": a.beta_final,
+            "coding": a.coding, "populations": P, "parallelism": f"replicas x{ws}",
+            "l2": "flushed between timed steps (256 MB write)"}
+
+
 # ------------------------------------------------------------- our engine
 def engine_kwargs(a, seed: int, device: int) -> dict:
     """The timed engine: P populations of the workload in one launch
@@ -251,18 +276,16 @@ def run_ours(a):
 
     out = None
     if rank == 0:
-        workload = f"PA anneal {a.coding.upper()} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} beta 0->" \
-                   f"{a.beta_final} ({nsteps} temperatures), {P} population(s) per launch"
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": tot_ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u32 bit-planes (int32 energies, fp32-compensated weights, fp64 lnQ)" if a.coding == "msc"
             else "i8 spins (int32 energies, fp32-compensated weights, fp64 lnQ)",
             "data": "synthetic (random initial spins from the seed, native Philox stream)",
-            "config": {"workload": workload, "L": a.L, "R": a.R, "sweeps": a.sweeps, "dbeta": a.dbeta,
-                       "beta_final": a.beta_final, "coding": a.coding, "populations_per_launch": P,
-                       "graph": bool(a.graph), "parallelism": f"replicas x{ws}",
-                       "l2": "flushed between timed steps (256 MB write)"},
+            "config": workload_config(a, ws),
+            "schedule": {"populations_per_launch": P, "graph": bool(a.graph),
+                         "how": "all populations of a step in the same launches (persistent kernels), the whole "
+                                "schedule one CUDA graph"},
             "full_anneal_s": tot_ms_max / a.steps / 1e3,
             "full_anneal_s_per_population": tot_ms_max / a.steps / 1e3 / P,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": pop_bytes,
@@ -418,11 +441,21 @@ def run_reference(a):
     if binp is None:
         return {"impl": "reference", "unavailable": why}
     P = a.populations
+    flush = None
+    try:  # the same L2 flush between steps as our arm (L2 is the GPU's, whichever process writes it)
+        import torch
+        if torch.cuda.is_available():
+            flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    except ImportError:
+        pass
     for w in range(a.warmup):
         _reference_once(binp, a, 1 + w, 1)
     els, atts = [], []
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for k in range(a.steps):
+            if flush is not None:
+                flush.zero_()
+                torch.cuda.synchronize()
             el, att = _reference_once(binp, a, 100 + k, P)
             els.append(el)
             atts.append(att)
@@ -434,11 +467,9 @@ def run_reference(a):
         "warmup": a.warmup, "ms_per_step": 1e3 * sum(els) / len(els), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 bit-planes" if a.coding == "msc" else "i8 spins",
         "data": "synthetic (random initial spins from the seed, cuRAND Philox)",
-        "config": {"workload": f"PA anneal {prog} L={a.L} R={a.R} sweeps={a.sweeps} dbeta={a.dbeta} beta 0->"
-                               f"{a.beta_final}, {P} population(s) per step (reference -M {P}: one after the "
-                               "other)", "L": a.L, "R": a.R, "sweeps": a.sweeps, "dbeta": a.dbeta,
-                   "beta_final": a.beta_final, "coding": a.coding, "populations_per_launch": P,
-                   "parallelism": "single GPU"},
+        "config": workload_config(a, 1),
+        "schedule": {"how": f"one invocation of the program per step with -M {P}: the populations one after the "
+                            "other, each with the reference's own launches and host synchronisation"},
         "full_anneal_s": sum(els) / len(els),
         "full_anneal_s_per_population": sum(els) / len(els) / P,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
