@@ -1205,6 +1205,10 @@ std::string read_checkpoint(const char* path, CkptFile* out) {
     FILE* f;
     ~Closer() { std::fclose(f); }
   } closer{f};
+  // the file's length bounds every buffer before anything is allocated for it
+  if (std::fseek(f, 0, SEEK_END) != 0) return "cannot read the file";
+  const long fsize = std::ftell(f);
+  if (fsize < 0 || std::fseek(f, 0, SEEK_SET) != 0) return "cannot read the file";
   char magic[8];
   if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kCkptMagic, 8) != 0) return "not a checkpoint";
   int32_t* head = out->head;
@@ -1235,7 +1239,13 @@ std::string read_checkpoint(const char* path, CkptFile* out) {
       uint64_t n = 0;
       if (std::fread(&n, sizeof(n), 1, f) != 1) return "truncated";
       if (n != want) return "buffer size does not match the population";
-      p.bufs.emplace_back(n);
+      const long at = std::ftell(f);
+      if (at < 0 || n > (uint64_t)(fsize - at)) return "truncated";
+      try {
+        p.bufs.emplace_back(n);
+      } catch (const std::bad_alloc&) {
+        return "buffer too large for host memory";
+      }
       if (std::fread(p.bufs.back().data(), 1, n, f) != n) return "truncated";
     }
   }

@@ -74,6 +74,17 @@ def test_inconsistent_file_is_refused(tmp_path, coding, field, kw, words):
     assert words in msg, (field, msg)
 
 
+def test_huge_claimed_shape_is_refused_without_allocating(tmp_path):
+    """A shape claiming a population far larger than the file (here ~2^31
+    replicas at L=4096, terabytes of buffers) is refused as truncated before
+    any buffer is allocated."""
+    big = ckpt_bytes(coding=0, L=8)
+    head, rest = big[:28], big[28:]
+    shape = struct.pack("<9i", 4096, 2 ** 30, 2 ** 31 - 1, (2 ** 31 - 1 + 31) // 32, 6, 1, 0, 0, 0)
+    st, msg = verify(tmp_path, head + shape + rest[36:])
+    assert st == 1 and ("truncated" in msg or "size" in msg), msg
+
+
 def test_not_a_checkpoint(tmp_path):
     st, msg = verify(tmp_path, b"PAGB300X" + bytes(64))
     assert st == 1 and "not a checkpoint" in msg
