@@ -5,6 +5,7 @@ repository root):
     python studies.py batch       [--coding msc|ssc] [--out FILE]
     python studies.py large       [--out FILE]
     python studies.py reference_large [--out FILE]
+    python studies.py populations [--coding msc|ssc] [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
@@ -169,14 +170,40 @@ def reference_large(seed: int = 256, sweeps: int = 50) -> dict:
     return res
 
 
+def populations(counts=(1, 2, 4, 8, 16, 32), coding: str = "msc") -> dict:
+    """The headline anneal (L=64, R=20000, 100 sweeps, dbeta=0.005) with P
+    independent populations per launch sequence: attempts/ns as P grows (the
+    batched form's gain over the plain one-population form)."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    res = {"workload": f"{coding.upper()} L=64 R=20000 100 sweeps dbeta=0.005 beta 0->1, native stream, FP32 "
+                       "weights, graph", "by_populations": {}}
+    for P in counts:
+        with pa.Engine(L=64, R=20000, sweeps=100, dbeta=0.005, runs=P, seed=500 + P, coding=coding) as e:
+            e.run()
+            ms = att = 0.0
+            for _ in range(2):
+                flush.zero_()
+                torch.cuda.synchronize()
+                e.run()
+                m, a = e.timing()
+                ms += m
+                att += a
+        r = {"attempts_per_ns": att / (ms * 1e6), "s_per_population_anneal": ms / 2 / 1e3 / P}
+        res["by_populations"][str(P)] = r
+        print(json.dumps({"P": P, **r}), flush=True)
+    return res
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large"])
+    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations"])
     ap.add_argument("--out", default=None)
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
     r = batch(coding=a.coding) if a.study == "batch" else \
-        {"precision": precision, "large": large, "reference_large": reference_large}[a.study]()
+        {"precision": precision, "large": large, "reference_large": reference_large,
+         "populations": lambda: populations(coding=a.coding)}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0
