@@ -71,7 +71,9 @@ typedef struct pa_config {
   int device;        /* CUDA device ordinal */
   double capacity;   /* replica buffer = ceil(capacity * R) + 256; 0 selects 1.25 */
   int sweep_variant; /* MSC sweep kernel: 0 automatic, 1 one CTA per group, 2 or 4: a thread-block
-                        cluster of that many CTAs per group (needed for L > 128).  SSC: 0 automatic
+                        cluster of that many CTAs per group (needed for L > 128; chosen automatically
+                        for batches of 48 <= L <= 128, L % 8 == 0, with too few groups to fill the
+                        GPU).  SSC: 0 automatic
                         (native stream: bit planes, 32 sites per word, where L packs into words at
                         least 3/4 full -- L = 8, 16, 24, 32, 48, 56, 64, 96, 112, 128, 144, 168, 192,
                         224, 240, 256 -- else int8), 1 int8 */

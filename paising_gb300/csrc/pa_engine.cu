@@ -209,6 +209,7 @@ struct pa_handle {
   int max_steps = 0;
   int rblocks = 1;
   int cs = 1;  // CTAs per MSC group in the sweep (1, or a cluster of 2 / 4)
+  int cthreads = 256;  // threads per CTA of a cluster (msc_cluster_threads)
   bool ssc_bits = false;  // SSC swept on bit planes (pa_ssc_bits.cu)
   bool adaptive = false;  // some population chooses its temperatures as it goes
   static constexpr int kChunk = 16;  // adaptive runs: steps per graph launch between host checks
@@ -277,7 +278,7 @@ struct pa_handle {
 
   cudaError_t sweep_launch(int energy_only) {
     if (ssc_bits) return launch_ssc_bits_sweep(d_batch, energy_only, stream_seed, sweep, stream);
-    return cs > 1 ? launch_msc_cluster_sweep(cs, d_batch, rng_mode, energy_only, stream_seed, sweep, stream)
+    return cs > 1 ? launch_msc_cluster_sweep(cs, cthreads, d_batch, rng_mode, energy_only, stream_seed, sweep, stream)
                   : launch_sweep(d_batch, coding, rng_mode, energy_only, stream_seed, sweep, stream);
   }
 
@@ -561,7 +562,7 @@ struct pa_handle {
       geo.push_back(P.geom);
     }
     cudaError_t e = ssc_bits ? ssc_bits_setup(max_smem, &sweep)
-                    : cs > 1 ? msc_cluster_setup(cs, rng_mode, max_smem, &sweep)
+                    : cs > 1 ? msc_cluster_setup(cs, cthreads, rng_mode, max_smem, &sweep)
                              : sweep_setup(coding, rng_mode, max_smem, &sweep, fixed_l(geo));
     if (e != cudaSuccess || !graph) return e;
     if (exec) cudaGraphExecDestroy(exec);
@@ -650,6 +651,27 @@ namespace {
 // the group (4 N bytes) fits its shared memory and a cluster of 2 otherwise.
 int msc_variant(int requested, int L) { return requested ? requested : (L > 128 ? 2 : 1); }
 
+// Automatic sweep form of an MSC batch whose populations all leave the form
+// to the engine (sweep_variant 0, tile_groups 0) and have 48 <= L <= 128,
+// L % 8 == 0: a batch with too few groups to fill the resident one-CTA sweep
+// slots (groups = work units) runs each group on a cluster of 4 or 2 CTAs of
+// 256 threads instead, so that more SMs take part.  Measured at 100 sweeps
+// (L=64: one CTA per group / clusters of 2 / of 4, attempts/ns): 79 groups
+// 817 / 988 / 1220, 157 groups 1393 / 1971 / 2076, 313 groups 2525 / 3343 /
+// 2390, 391 groups 3151 / 3576 / 2362, 469 groups 3765 / 3546 / -; L=128,
+// 157 groups 1662 / 2143 / 3268.  Smaller lattices keep stacked tiles,
+// which serve them better.
+int msc_auto_clusters(const std::vector<pa_config>& cfgs, int cs, long long groups, int slots) {
+  if (cs != 1) return cs;
+  for (const auto& c : cfgs)
+    if (c.coding != PA_CODING_MSC || c.sweep_variant != 0 || c.tile_groups != 0 || c.L < 48 || c.L > 128 ||
+        c.L % 8 != 0)
+      return cs;
+  if (4 * groups * 10 <= 11LL * slots) return 4;  // 4 G <= 1.1 S
+  if (2 * groups * 20 <= 27LL * slots) return 2;  // 2 G <= 1.35 S
+  return 1;
+}
+
 int validate(const pa_config& c) {
   auto bad = [](const char* m) {
     pa::g_last_error = m;
@@ -683,7 +705,7 @@ int validate(const pa_config& c) {
     const int cs = msc_variant(c.sweep_variant, c.L);
     if (cs == 1 && c.tile_groups > 1 && !msc_geom(c.L, &g, c.tile_groups))
       return bad("tile_groups > 1 needs L % 4 == 0 and at most 44 KB of spins per tile");
-    const bool ok = cs == 1 ? msc_geom(c.L, &g) : msc_cluster_geom(c.L, cs, msc_cluster_threads(cs), &g);
+    const bool ok = cs == 1 ? msc_geom(c.L, &g) : msc_cluster_geom(c.L, cs, msc_cluster_threads(cs, c.L), &g);
     if (!ok) return bad("MSC needs even L in [8, 128] (one CTA per group) or L % 4 == 0 up to 256 (clusters)");
   } else if (!ssc_geom(c.L, &g)) {
     return bad("SSC needs L % 8 == 0, 8 <= L <= 256");
@@ -730,11 +752,15 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
   const int slots = 4 * nsm;  // resident one-CTA sweep CTAs (four per SM, register-bound)
   H->cs = 1;
   long long batch_groups = 0;  // work available to the one-CTA sweep: bounds automatic tile sizes
+  int maxL = 0;
   if (H->coding == PA_CODING_MSC)
     for (const auto& c : cfgs) {
       H->cs = std::max(H->cs, msc_variant(c.sweep_variant, c.L));
       batch_groups += (c.R + kMsb - 1) / kMsb;
+      maxL = std::max(maxL, c.L);
     }
+  H->cs = msc_auto_clusters(cfgs, H->cs, batch_groups, slots);
+  H->cthreads = msc_cluster_threads(H->cs, maxL);
   // SSC with the native stream: bit-plane sweep when every lattice packs
   // into words at least 3/4 full (sweep_variant 1 keeps the int8 sweep;
   // pa_autotune may also choose a sparser bit-plane layout by timing)
@@ -765,7 +791,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       okg = H->ssc_bits ? ssc_bits_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_replicas, slots)
                         : ssc_geom(P.cfg.L, &P.geom);
     else if (H->cs == 1) okg = msc_geom(P.cfg.L, &P.geom, P.cfg.tile_groups, batch_groups, slots);
-    else okg = msc_cluster_geom(P.cfg.L, H->cs, msc_cluster_threads(H->cs), &P.geom);
+    else okg = msc_cluster_geom(P.cfg.L, H->cs, H->cthreads, &P.geom);
     if (!okg) return fail(PA_ERR_ARG, "L=" + std::to_string(P.cfg.L) + " cannot join a batch swept by clusters of " +
                                           std::to_string(H->cs) + " CTAs");
     if (P.cfg.adaptive) {

@@ -106,9 +106,9 @@ cudaError_t launch_ssc_bits_sweep(BatchDev* b, int energy_only, unsigned long lo
 // MSC sweep by thread-block clusters of cs = 2 or 4 CTAs (one horizontal
 // stripe of the group per CTA), for lattices too large for one CTA.
 bool msc_cluster_geom(int L, int cs, int threads, SweepGeom* g);
-int msc_cluster_threads(int cs);
-cudaError_t msc_cluster_setup(int cs, int rng_mode, int smem, SweepLaunch* out);
-cudaError_t launch_msc_cluster_sweep(int cs, BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
+int msc_cluster_threads(int cs, int maxL);
+cudaError_t msc_cluster_setup(int cs, int threads, int rng_mode, int smem, SweepLaunch* out);
+cudaError_t launch_msc_cluster_sweep(int cs, int threads, BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
                                      const SweepLaunch& sl, cudaStream_t s);
 
 // Per-run / per-step bookkeeping.

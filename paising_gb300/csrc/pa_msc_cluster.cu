@@ -203,10 +203,11 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
             const uint32_t acc = hi | (~hi & ((s0 & c4) | (~s0 & c8)));
             if (valid) self[row + tx] = s ^ acc;
           }
-        } else if (P.L == 256) {
+        } else if (THREADS > 256 && P.L == 256) {
           // L = 256 with every size fixed at compile time: rows of 128 words,
           // THREADS/128 thread rows of kRows consecutive stripe rows each,
-          // every offset an immediate (same batches as the general form below)
+          // every offset an immediate (same batches as the general form below);
+          // the 256-thread clusters serve L <= 128 only
           constexpr int kW = 128, kLR = 256 / CS, kRpp = THREADS / kW, kRows = kLR / kRpp;
           static_assert(kLR % kRpp == 0 && kRows % kKB == 0, "whole batches");
           const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
@@ -360,19 +361,26 @@ static cudaError_t cluster_dispatch(int rng_mode, BatchDev* b, int energy_only, 
                                 : cluster_launch<kNative, CS, THREADS>(b, energy_only, seed, sl, setup, s);
 }
 
-int msc_cluster_threads(int cs) { return cs == 2 ? 1024 : 512; }
+// Threads per CTA of a cluster: lattices up to L = 128 take 256 (a stripe of
+// L/cs rows of L/2 words then gives every thread whole batches of kKB rows,
+// as the one-CTA sweep does), larger ones 1024 (clusters of 2) or 512 (4).
+int msc_cluster_threads(int cs, int maxL) { return maxL <= 128 ? 256 : cs == 2 ? 1024 : 512; }
 
-cudaError_t msc_cluster_setup(int cs, int rng_mode, int smem, SweepLaunch* out) {
+cudaError_t msc_cluster_setup(int cs, int threads, int rng_mode, int smem, SweepLaunch* out) {
   out->smem = smem;
-  if (cs == 2) return cluster_dispatch<2, 1024>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
-  if (cs == 4) return cluster_dispatch<4, 512>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  if (cs == 2 && threads == 256) return cluster_dispatch<2, 256>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  if (cs == 4 && threads == 256) return cluster_dispatch<4, 256>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  if (cs == 2 && threads == 1024) return cluster_dispatch<2, 1024>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
+  if (cs == 4 && threads == 512) return cluster_dispatch<4, 512>(rng_mode, nullptr, 0, 0, nullptr, out, nullptr);
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_msc_cluster_sweep(int cs, BatchDev* b, int rng_mode, int energy_only, unsigned long long seed,
-                                     const SweepLaunch& sl, cudaStream_t s) {
-  if (cs == 2) return cluster_dispatch<2, 1024>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
-  if (cs == 4) return cluster_dispatch<4, 512>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+cudaError_t launch_msc_cluster_sweep(int cs, int threads, BatchDev* b, int rng_mode, int energy_only,
+                                     unsigned long long seed, const SweepLaunch& sl, cudaStream_t s) {
+  if (cs == 2 && threads == 256) return cluster_dispatch<2, 256>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+  if (cs == 4 && threads == 256) return cluster_dispatch<4, 256>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+  if (cs == 2 && threads == 1024) return cluster_dispatch<2, 1024>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
+  if (cs == 4 && threads == 512) return cluster_dispatch<4, 512>(rng_mode, b, energy_only, seed, &sl, nullptr, s);
   return cudaErrorInvalidValue;
 }
 

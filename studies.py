@@ -6,6 +6,7 @@ repository root):
     python studies.py large       [--out FILE]
     python studies.py reference_large [--out FILE]
     python studies.py populations [--coding msc|ssc] [--out FILE]
+    python studies.py small       [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
@@ -195,15 +196,48 @@ def populations(counts=(1, 2, 4, 8, 16, 32), coding: str = "msc") -> dict:
     return res
 
 
+def small(cases=((64, (2500, 5000, 7500, 10000, 12500, 15000, 20000)), (96, (2000, 5000, 10000)),
+                  (128, (1000, 2000, 5000, 10000)), (48, (5000, 20000)))) -> dict:
+    """Single populations too small to fill the GPU with one CTA per group:
+    the one-CTA sweep (sweep_variant=1) against the engine's automatic form
+    (clusters of 2 or 4 CTAs per group where the groups are too few) and
+    against each cluster size forced; MSC, native stream, 100 sweeps up to
+    L=64, 50 above, dbeta=0.005."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    res = {"cases": []}
+    for L, Rs in cases:
+        for R in Rs:
+            row = {"L": L, "R": R, "groups": (R + 31) // 32}
+            for name, v in (("one_cta", 1), ("automatic", 0), ("clusters2", 2), ("clusters4", 4)):
+                with pa.Engine(L=L, R=R, sweeps=100 if L <= 64 else 50, dbeta=0.005, seed=7, coding="msc",
+                               sweep_variant=v) as e:
+                    e.run()
+                    ms = att = 0.0
+                    for _ in range(2):
+                        flush.zero_()
+                        torch.cuda.synchronize()
+                        e.run()
+                        m, a = e.timing()
+                        ms += m
+                        att += a
+                    row[name] = round(att / (ms * 1e6), 1)
+                    if v == 0:
+                        row["automatic_cluster_ctas"] = e.sweep_form(0)["cluster_ctas"]
+            res["cases"].append(row)
+            print(json.dumps(row), flush=True)
+    return res
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations"])
+    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations", "small"])
     ap.add_argument("--out", default=None)
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
     r = batch(coding=a.coding) if a.study == "batch" else \
         {"precision": precision, "large": large, "reference_large": reference_large,
-         "populations": lambda: populations(coding=a.coding)}[a.study]()
+         "populations": lambda: populations(coding=a.coding), "small": small}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0

@@ -142,13 +142,16 @@ def test_msc_anneal_native_stream_stacked_tiles(cuda, oracle, L, R, tile):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,R,cs", [(16, 200, 2), (16, 200, 4), (64, 100, 4), (256, 40, 2)])
+@pytest.mark.parametrize("L,R,cs", [(16, 200, 2), (16, 200, 4), (64, 100, 4), (64, 300, 2), (128, 90, 2),
+                                     (256, 40, 2)])
 def test_msc_anneal_native_stream_clusters(cuda, oracle, L, R, cs):
-    """Thread-block clusters (cs CTAs per group, 1024 or 512 threads each,
-    halo rows over distributed shared memory) under the native stream equal
-    the oracle's restatement of the same thread layout row for row."""
+    """Thread-block clusters (cs CTAs per group, 256 threads each up to
+    L = 128, else 1024 or 512, halo rows over distributed shared memory)
+    under the native stream equal the oracle's restatement of the same thread
+    layout row for row."""
     from conftest import compare_rows
-    seed, threads = 57 + cs, {2: 1024, 4: 512}[cs]
+    # threads per CTA: 256 up to L = 128, else 1024 (clusters of 2) or 512 (4)
+    seed, threads = 57 + cs, 256 if L <= 128 else {2: 1024, 4: 512}[cs]
     sweeps, dbeta = (2, 0.25) if L == 256 else (3, 0.1)
     with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=1.0, seed=seed, coding="msc", rng="native",
                    weights="fp64", graph=True, sweep_variant=cs, device=0) as e:
@@ -266,7 +269,7 @@ def test_native_batch_each_population_equals_oracle(cuda, oracle, coding, L, R, 
     for k in range(P):
         f = forms[k]
         if coding == "msc":
-            threads = {2: 1024, 4: 512}.get(f["cluster_ctas"], 256)
+            threads = 256 if L <= 128 else {2: 1024, 4: 512}.get(f["cluster_ctas"], 256)
             ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_MSC | k,
                                            threads, f["tile"], max(1, f["cluster_ctas"]), iseq0=k << 40)
         else:
@@ -274,3 +277,23 @@ def test_native_batch_each_population_equals_oracle(cuda, oracle, coding, L, R, 
             ref = oracle.anneal_ssc_bits_native(L, R, sweeps, dbeta, 1.0, 1, seed, seed, oracle.NATIVE_TAG_SSC | k,
                                                 f["tile"], iseq0=k << 40)
         compare_rows(got[k], ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R,cs", [(64, 2000, 4), (64, 9000, 2), (96, 600, 4), (64, 20000, 1)])
+def test_automatic_clusters_for_small_populations(cuda, oracle, L, R, cs):
+    """A population with too few groups to fill the resident one-CTA sweep
+    slots is swept by clusters of 4 or 2 CTAs per group (256 threads each)
+    without being asked; the anneal equals the oracle's restatement of that
+    form.  20000 replicas at L=64 fill the GPU and keep one CTA per group."""
+    from conftest import compare_rows
+    seed, sweeps, dbeta = 300 + L, 2, 0.1
+    with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=0.5, seed=seed, coding="msc", rng="native",
+                   weights="fp64", graph=True, device=0) as e:
+        f = e.sweep_form(0)
+        assert f["cluster_ctas"] == cs, f
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 0.5, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256,
+                                   f["tile"], max(1, f["cluster_ctas"]))
+    compare_rows(got, ref[0], rtol=2e-10)
