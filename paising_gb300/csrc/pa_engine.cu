@@ -653,22 +653,32 @@ int msc_variant(int requested, int L) { return requested ? requested : (L > 128 
 
 // Automatic sweep form of an MSC batch whose populations all leave the form
 // to the engine (sweep_variant 0, tile_groups 0) and have 48 <= L <= 128,
-// L % 8 == 0: a batch with too few groups to fill the resident one-CTA sweep
-// slots (groups = work units) runs each group on a cluster of 4 or 2 CTAs of
-// 256 threads instead, so that more SMs take part.  Measured at 100 sweeps
-// (L=64: one CTA per group / clusters of 2 / of 4, attempts/ns): 79 groups
-// 817 / 988 / 1220, 157 groups 1393 / 1971 / 2076, 313 groups 2525 / 3343 /
-// 2390, 391 groups 3151 / 3576 / 2362, 469 groups 3765 / 3546 / -; L=128,
-// 157 groups 1662 / 2143 / 3268.  Smaller lattices keep stacked tiles,
-// which serve them better.
+// L % 8 == 0: a batch with too few groups to keep the resident one-CTA sweep
+// slots busy runs each group on a cluster of 4 or 2 CTAs of 256 threads,
+// so that more SMs take part and the last wave is finer.  The thresholds
+// (groups as fractions of the slots, 608 on a GB300) come from the measured
+// crossovers (profiles/study_small_populations_msc.md): L=64 (compile-time
+// cluster form for clusters of 2) clusters of 4 up to ~110 groups, of 2 up
+// to ~700; L=128 (compile-time forms for both; its one-CTA form fits three
+// CTAs per SM) 4 up to ~550, 2 up to ~2000; other sizes 4 up to ~200, 2 up to
+// ~400.  Smaller lattices keep stacked tiles, which serve them better.
 int msc_auto_clusters(const std::vector<pa_config>& cfgs, int cs, long long groups, int slots) {
   if (cs != 1) return cs;
-  for (const auto& c : cfgs)
+  int L0 = 0;
+  bool same_L = true;
+  for (const auto& c : cfgs) {
     if (c.coding != PA_CODING_MSC || c.sweep_variant != 0 || c.tile_groups != 0 || c.L < 48 || c.L > 128 ||
         c.L % 8 != 0)
       return cs;
-  if (4 * groups * 10 <= 11LL * slots) return 4;  // 4 G <= 1.1 S
-  if (2 * groups * 20 <= 27LL * slots) return 2;  // 2 G <= 1.35 S
+    if (L0 && c.L != L0) same_L = false;
+    L0 = c.L;
+  }
+  // per mille of the slots: clusters of 4 up to t4, of 2 up to t2
+  long long t4 = 330, t2 = 660;
+  if (same_L && L0 == 64) t4 = 180, t2 = 1150;
+  if (same_L && L0 == 128) t4 = 900, t2 = 3300;
+  if (groups * 1000 <= t4 * slots) return 4;
+  if (groups * 1000 <= t2 * slots) return 2;
   return 1;
 }
 

@@ -15,6 +15,7 @@
 #include <cooperative_groups.h>
 
 #include <climits>
+#include <type_traits>
 
 #include "pa_kernels.h"
 #include "pa_msc_core.cuh"
@@ -236,6 +237,46 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
 #pragma unroll
             for (int k = 0; k < kKB; ++k) ps[k * kW] ^= ac[k];
           }
+        } else if (THREADS == 256 && ((CS == 2 && P.L == 64) || P.L == 128)) {
+          // L = 64 (clusters of 2) and 128 on 256-thread CTAs with every size
+          // fixed at compile time: rows of kW = L/2 words, THREADS/kW thread
+          // rows of kRows consecutive stripe rows (whole batches), rows -1 and
+          // LR are the halo rows; same batches, numbering and draws as the
+          // general form below, so the same results
+          auto fixed = [&](auto l_c) {
+            constexpr int kL = decltype(l_c)::value, kW = kL / 2, kLR = kL / CS, kR = THREADS / kW;
+            constexpr int kRows = kLR / kR;
+            if constexpr (kRows % kKB == 0 && kR * kW == THREADS && kLR % kR == 0) {
+              const uint32_t c1 = (uint32_t)((sw * 2 + hf) << 4);
+              const int vb0 = rsub * kRows;
+              // stripes and batches start on even rows: the side neighbour of
+              // even rows is x-1 for A, x+1 for B (PAisingMSC.cu:203, 238)
+              const uint32_t* txs = oth + (hf == 0 ? txl : txr);
+              const uint32_t* txo = oth + (hf == 0 ? txr : txl);
+#pragma unroll 1
+              for (int p0 = 0; p0 < kRows; p0 += kKB) {
+                const int vb = vb0 + p0;
+                const uint32_t* po = oth + (vb - 1) * kW + tx;  // stripe rows vb-1 .. vb+4 (halos included)
+                uint32_t* ps = self + vb * kW + tx;
+                uint32_t av[kKB], un[kKB], ac[kKB], site[kKB];
+#pragma unroll
+                for (int k = 0; k < kKB; ++k) {
+                  const uint32_t s = ps[k * kW];
+                  const uint32_t side = ((k & 1) ? txo : txs)[(vb + k) * kW];
+                  count_masks(s, side, po[(k + 1) * kW], po[k * kW], po[(k + 2) * kW], av[k], ac[k]);
+                  un[k] = 0xFFFFFFFFu - ac[k];  // = ~ac, on the FMA pipe
+                  site[k] = (uint32_t)gi * (uint32_t)h + (uint32_t)((row0 + vb + k) * kW + tx);
+                }
+                const uint32_t chain = (((uint32_t)gi * CS + (uint32_t)rank) * blockDim.x + (uint32_t)tid) *
+                                           (uint32_t)(kRows / kKB) + (uint32_t)(p0 / kKB);
+                accept_native(av, un, ac, site, chain, c1, (uint32_t)P.step, P.tag, keys, s_dig, kKB, P.T4, P.T8);
+#pragma unroll
+                for (int k = 0; k < kKB; ++k) ps[k * kW] ^= ac[k];
+              }
+            }
+          };
+          if (P.L == 64) fixed(std::integral_constant<int, 64>());
+          else fixed(std::integral_constant<int, 128>());
         } else {
           // thread rsub owns the consecutive stripe rows rsub*npass ..
           // rsub*npass + npass - 1 of column tx: a batch of kKB rows shares

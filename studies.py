@@ -196,8 +196,10 @@ def populations(counts=(1, 2, 4, 8, 16, 32), coding: str = "msc") -> dict:
     return res
 
 
-def small(cases=((64, (2500, 5000, 7500, 10000, 12500, 15000, 20000)), (96, (2000, 5000, 10000)),
-                  (128, (1000, 2000, 5000, 10000)), (48, (5000, 20000)))) -> dict:
+def small(cases=((64, (2500, 5000, 7500, 10000, 12500, 15000, 20000, 25000, 30000, 40000, 100000)),
+                  (96, (2000, 5000, 10000, 20000)),
+                  (128, (1000, 2000, 5000, 10000, 15000, 20000, 30000, 40000, 100000)),
+                  (48, (5000, 20000)))) -> dict:
     """Single populations too small to fill the GPU with one CTA per group:
     the one-CTA sweep (sweep_variant=1) against the engine's automatic form
     (clusters of 2 or 4 CTAs per group where the groups are too few) and

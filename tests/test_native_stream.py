@@ -280,12 +280,13 @@ def test_native_batch_each_population_equals_oracle(cuda, oracle, coding, L, R, 
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,R,cs", [(64, 2000, 4), (64, 9000, 2), (96, 600, 4), (64, 20000, 1)])
+@pytest.mark.parametrize("L,R,cs", [(64, 2000, 4), (64, 20000, 2), (96, 600, 4), (128, 9000, 4), (128, 30000, 2),
+                                     (64, 40000, 1)])
 def test_automatic_clusters_for_small_populations(cuda, oracle, L, R, cs):
-    """A population with too few groups to fill the resident one-CTA sweep
-    slots is swept by clusters of 4 or 2 CTAs per group (256 threads each)
-    without being asked; the anneal equals the oracle's restatement of that
-    form.  20000 replicas at L=64 fill the GPU and keep one CTA per group."""
+    """A population with too few groups to keep the resident one-CTA sweep
+    slots busy is swept by clusters of 4 or 2 CTAs per group (256 threads
+    each) without being asked; the anneal equals the oracle's restatement of
+    that form.  40000 replicas at L=64 keep one CTA per group."""
     from conftest import compare_rows
     seed, sweeps, dbeta = 300 + L, 2, 0.1
     with pa.Engine(L=L, R=R, sweeps=sweeps, dbeta=dbeta, beta_final=0.5, seed=seed, coding="msc", rng="native",
