@@ -111,3 +111,16 @@ def test_restore_refuses_tampered_files_and_keeps_the_handle(cuda, tmp_path, cod
             pass
         b.run_end()
         assert np.array_equal(b.rows(0), ref)
+
+
+def test_checkpoint_of_a_cluster_swept_population(cuda, tmp_path):
+    """A small L=64 population, swept by clusters of CTAs by default, stepped,
+    checkpointed and finished in a second handle gives pa_run's rows."""
+    kw = dict(L=64, R=3000, sweeps=4, dbeta=0.05, seed=17, coding="msc")
+    with pa.Engine(**kw) as e:
+        assert e.sweep_form(0)["cluster_ctas"] > 1
+        e.run()
+        ref = e.rows(0)
+    b = stepped(kw, 7, tmp_path / "c.bin")
+    assert np.array_equal(b.rows(0), ref)
+    b.close()
