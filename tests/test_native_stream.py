@@ -298,3 +298,23 @@ def test_automatic_clusters_for_small_populations(cuda, oracle, L, R, cs):
     ref = oracle.anneal_msc_native(L, R, sweeps, dbeta, 0.5, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256,
                                    f["tile"], max(1, f["cluster_ctas"]))
     compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+def test_automatic_clusters_in_a_mixed_batch(cuda, oracle):
+    """Populations of L = 64, 96 and 128 in one small batch share one
+    automatically chosen cluster form (compile-time paths for 64 and 128, the
+    general one for 96 in the same launch); each equals the oracle's run of
+    that population alone with its subsequence base and sweep tag."""
+    from conftest import compare_rows
+    pops = [dict(L=64, R=1000, seed=41), dict(L=96, R=500, seed=42), dict(L=128, R=300, seed=43)]
+    common = dict(sweeps=2, dbeta=0.1, beta_final=0.5, coding="msc", rng="native", weights="fp64", graph=True)
+    with pa.Engine.batch(pops, **common) as e:
+        forms = [e.sweep_form(k) for k in range(3)]
+        assert all(f["cluster_ctas"] == forms[0]["cluster_ctas"] > 1 for f in forms), forms
+        e.run()
+        got = [e.rows(k) for k in range(3)]
+    for k, p in enumerate(pops):
+        ref = oracle.anneal_msc_native(p["L"], p["R"], 2, 0.1, 0.5, 1, p["seed"], pops[0]["seed"],
+                                       oracle.NATIVE_TAG_MSC | k, 256, 1, forms[k]["cluster_ctas"], iseq0=k << 40)
+        compare_rows(got[k], ref[0], rtol=2e-10)
