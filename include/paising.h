@@ -172,8 +172,12 @@ PA_API int pa_checkpoint_verify(const char* path);
  * temperature) per candidate, keeps the fastest per spin-flip attempt and
  * rebuilds the launch plan (and graph):
  *   MSC, one CTA per work unit: for every lattice size, 1, 2, 4 or 8 groups
- *     of 32 replicas stacked per work unit, where valid.  Results are
- *     unchanged by the choice (draws are keyed by group and site).
+ *     of 32 replicas stacked per work unit, where valid; then, when every
+ *     population has 48 <= L <= 128, L % 8 == 0 and leaves the form to the
+ *     engine, that tuned form against clusters of 2 and of 4 CTAs per group
+ *     for the whole batch.  Under the reference stream results are unchanged
+ *     by the choice (draws are keyed by group and site); the native stream's
+ *     draws follow the form, as for SSC below.
  *   SSC, native stream, every L with a bit-plane layout and sweep_variant 0:
  *     for every lattice size the bit-plane tile (replicas per work unit), then
  *     for the whole batch the int8 sweep (4 sites of a replica per 32-bit

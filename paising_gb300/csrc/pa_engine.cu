@@ -598,8 +598,10 @@ struct pa_handle {
   // geometry geo[k] for population k (SSC: `bits` selects the bit-plane
   // sweep); the population state is the one left on the device by the caller
   // (an initialised population at step 1).
+  // cs > 1: the MSC cluster sweep with clusters of cs CTAs of cluster_threads
   cudaError_t time_sweep(const std::vector<PopDev>& state, const std::vector<char>& part,
-                         const std::vector<SweepGeom>& geo, bool bits, double* ns_per_attempt) {
+                         const std::vector<SweepGeom>& geo, bool bits, double* ns_per_attempt, int tcs = 1,
+                         int cluster_threads = 256) {
     std::vector<PopDev> hp = state;
     double attempts = 0;
     int smem = 0;
@@ -614,14 +616,19 @@ struct pa_handle {
     }
     cudaError_t e = upload_pops(hp);
     SweepLaunch sl{};
-    if (e == cudaSuccess) e = bits ? ssc_bits_setup(smem, &sl) : sweep_setup(coding, rng_mode, smem, &sl, fixed_l(geo));
+    if (e == cudaSuccess)
+      e = bits ? ssc_bits_setup(smem, &sl)
+               : tcs > 1 ? msc_cluster_setup(tcs, cluster_threads, rng_mode, smem, &sl)
+                         : sweep_setup(coding, rng_mode, smem, &sl, fixed_l(geo));
     float best = 0.f;
     for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {  // the first launch warms up
       e = launch_plan(d_batch, npop, 0, stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
       if (e == cudaSuccess)
         e = bits ? launch_ssc_bits_sweep(d_batch, 0, stream_seed, sl, stream)
-                 : launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sl, stream);
+                 : tcs > 1 ? launch_msc_cluster_sweep(tcs, cluster_threads, d_batch, rng_mode, 0, stream_seed, sl,
+                                                      stream)
+                           : launch_sweep(d_batch, coding, rng_mode, 0, stream_seed, sl, stream);
       if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
       if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
       float ms = 0.f;
@@ -1404,7 +1411,16 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
     H->err = "pa_autotune must precede the first pa_run";
     return PA_ERR_STATE;
   }
-  const bool msc_tiles = H->coding == PA_CODING_MSC && H->cs == 1;
+  // MSC: groups per tile of the one-CTA sweep for every lattice size and,
+  // where every population allows it (48 <= L <= 128, L % 8 == 0, form left
+  // to the engine), clusters of 2 or 4 CTAs per group: the fastest form of
+  // the batch is kept
+  bool msc_tiles = H->coding == PA_CODING_MSC, msc_clusters = H->coding == PA_CODING_MSC;
+  for (const auto& P : H->pops) {
+    if (P.cfg.L > 128 || P.cfg.sweep_variant > 1) msc_tiles = false;
+    if (P.cfg.sweep_variant != 0 || P.cfg.tile_groups != 0 || P.cfg.L < 48 || P.cfg.L > 128 || P.cfg.L % 8 != 0)
+      msc_clusters = false;
+  }
   // SSC, native stream: int8 (4 sites per word) or bit planes (32 sites per
   // word) for the whole batch, when every population allows both and asks
   // for neither
@@ -1445,6 +1461,31 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
             msc_geom(L, &P.geom, best_G);
             geom_to_pop(P.geom, &P.h);
           }
+      }
+      H->cs = 1;
+      if (msc_clusters && e == cudaSuccess) {  // the tuned one-CTA form against clusters of 2 and 4
+        std::vector<char> all(H->npop, 1);
+        std::vector<SweepGeom> g1(H->npop);
+        for (int k = 0; k < H->npop; ++k) g1[k] = H->pops[k].geom;
+        double best = 0;
+        e = H->time_sweep(state, all, g1, false, &best);
+        for (int tcs = 2; tcs <= 4 && e == cudaSuccess; tcs *= 2) {
+          std::vector<SweepGeom> gc(H->npop);
+          bool ok = true;
+          for (int k = 0; k < H->npop; ++k) ok = ok && msc_cluster_geom(H->pops[k].cfg.L, tcs, 256, &gc[k]);
+          if (!ok) continue;
+          double t = 0;
+          e = H->time_sweep(state, all, gc, false, &t, tcs, 256);
+          if (e == cudaSuccess && t > 0 && (best == 0 || t < best)) {
+            best = t;
+            H->cs = tcs;
+            for (int k = 0; k < H->npop; ++k) {
+              H->pops[k].geom = gc[k];
+              geom_to_pop(gc[k], &H->pops[k].h);
+            }
+          }
+        }
+        H->cthreads = 256;
       }
     } else {  // SSC: bit-plane replicas per tile for every lattice size, then the form of the batch
       std::vector<char> all(H->npop, 1);
