@@ -73,7 +73,8 @@ typedef struct pa_config {
   int sweep_variant; /* MSC sweep kernel: 0 automatic, 1 one CTA per group, 2 or 4: a thread-block
                         cluster of that many CTAs per group (needed for L > 128; chosen automatically
                         for batches of 48 <= L <= 128, L % 8 == 0, with too few groups to fill the
-                        GPU).  SSC: 0 automatic
+                        GPU; above L = 128 automatically 4 when the groups need more than one and at
+                        most eight waves of resident clusters of 2, else 2).  SSC: 0 automatic
                         (native stream: bit planes, 32 sites per word, where L packs into words at
                         least 3/4 full -- L = 8, 16, 24, 32, 48, 56, 64, 96, 112, 128, 144, 168, 192,
                         224, 240, 256 -- else int8), 1 int8 */
@@ -175,9 +176,13 @@ PA_API int pa_checkpoint_verify(const char* path);
  *     of 32 replicas stacked per work unit, where valid; then, when every
  *     population has 48 <= L <= 128, L % 8 == 0 and leaves the form to the
  *     engine, that tuned form against clusters of 2 and of 4 CTAs per group
- *     for the whole batch.  Under the reference stream results are unchanged
- *     by the choice (draws are keyed by group and site); the native stream's
- *     draws follow the form, as for SSC below.
+ *     for the whole batch.
+ *   MSC, a lattice above L = 128 (clusters needed), every population leaving
+ *     the form to the engine and able to take both: clusters of 2 CTAs of
+ *     1024 threads against clusters of 4 of 512 for the whole batch.
+ *   For MSC, results under the reference stream are unchanged by the choice
+ *   (draws are keyed by group and site); the native stream's draws follow the
+ *   form, as for SSC below.
  *   SSC, native stream, every L with a bit-plane layout and sweep_variant 0:
  *     for every lattice size the bit-plane tile (replicas per work unit), then
  *     for the whole batch the int8 sweep (4 sites of a replica per 32-bit

@@ -689,6 +689,37 @@ int msc_auto_clusters(const std::vector<pa_config>& cfgs, int cs, long long grou
   return 1;
 }
 
+// Automatic cluster size of an MSC batch that holds a lattice above L = 128
+// (which needs a cluster) and leaves the form to the engine: clusters of 4
+// CTAs of 512 threads from just over one resident wave of clusters of 2 (1024
+// threads, one CTA per SM) up to eight such waves, clusters of 2 otherwise.
+// Measured on L = 144..256 (profiles/study_large_lattice_clusters_msc.md):
+// with at most one wave the larger halo share and cluster barriers of
+// clusters of 4 cost more than they spread; just past one wave clusters of 2
+// run a nearly empty second wave (L=256: 63 groups 3795 vs 3162 attempts/ns,
+// 82 groups 2553 vs 3377); from about eight waves on both fill the GPU and
+// clusters of 2 do slightly less work per site.
+int msc_auto_large_clusters(const std::vector<pa_config>& cfgs, int cs, long long groups, int rng_mode) {
+  if (cs != 2) return cs;
+  int maxL = 0, smem = 0;
+  for (const auto& c : cfgs) {
+    SweepGeom g2, g4;
+    if (c.coding != PA_CODING_MSC || c.sweep_variant != 0 || c.tile_groups != 0 ||
+        !msc_cluster_geom(c.L, 2, 1024, &g2) || !msc_cluster_geom(c.L, 4, 512, &g4))
+      return cs;
+    maxL = std::max(maxL, c.L);
+    smem = std::max(smem, g2.smem);
+  }
+  if (maxL <= 128) return cs;
+  SweepLaunch sl{};
+  if (msc_cluster_setup(2, 1024, rng_mode, smem, &sl) != cudaSuccess) {
+    cudaGetLastError();
+    return cs;
+  }
+  const long long wave2 = sl.grid / 2;  // resident clusters of 2
+  return groups > wave2 && groups <= 8 * wave2 ? 4 : 2;
+}
+
 int validate(const pa_config& c) {
   auto bad = [](const char* m) {
     pa::g_last_error = m;
@@ -777,6 +808,7 @@ int build_handle(const std::vector<pa_config>& cfgs, int seq_runs, pa_handle** o
       maxL = std::max(maxL, c.L);
     }
   H->cs = msc_auto_clusters(cfgs, H->cs, batch_groups, slots);
+  H->cs = msc_auto_large_clusters(cfgs, H->cs, batch_groups, H->rng_mode);
   H->cthreads = msc_cluster_threads(H->cs, maxL);
   // SSC with the native stream: bit-plane sweep when every lattice packs
   // into words at least 3/4 full (sweep_variant 1 keeps the int8 sweep;
@@ -1415,12 +1447,22 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
   // where every population allows it (48 <= L <= 128, L % 8 == 0, form left
   // to the engine), clusters of 2 or 4 CTAs per group: the fastest form of
   // the batch is kept
+  // Above L = 128 (clusters needed, form left to the engine): clusters of 2
+  // CTAs of 1024 threads against clusters of 4 of 512.
   bool msc_tiles = H->coding == PA_CODING_MSC, msc_clusters = H->coding == PA_CODING_MSC;
+  bool msc_large = H->coding == PA_CODING_MSC;
+  int maxL = 0;
   for (const auto& P : H->pops) {
+    SweepGeom g2, g4;
+    maxL = std::max(maxL, P.cfg.L);
     if (P.cfg.L > 128 || P.cfg.sweep_variant > 1) msc_tiles = false;
     if (P.cfg.sweep_variant != 0 || P.cfg.tile_groups != 0 || P.cfg.L < 48 || P.cfg.L > 128 || P.cfg.L % 8 != 0)
       msc_clusters = false;
+    if (P.cfg.sweep_variant != 0 || P.cfg.tile_groups != 0 || !msc_cluster_geom(P.cfg.L, 2, 1024, &g2) ||
+        !msc_cluster_geom(P.cfg.L, 4, 512, &g4))
+      msc_large = false;
   }
+  msc_large = msc_large && maxL > 128;
   // SSC, native stream: int8 (4 sites per word) or bit planes (32 sites per
   // word) for the whole batch, when every population allows both and asks
   // for neither
@@ -1429,7 +1471,7 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
     SweepGeom gb;
     if (P.cfg.sweep_variant != 0 || !ssc_bits_geom(P.cfg.L, &gb)) ssc_forms = false;
   }
-  if (msc_tiles || ssc_forms) {
+  if (msc_tiles || ssc_forms || msc_large) {
     // an initialised population (step 1, random spins) to sweep
     cudaError_t e = H->enqueue_init();
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
@@ -1486,6 +1528,25 @@ int pa_autotune(pa_handle* H, int* tiles, int n) {
           }
         }
         H->cthreads = 256;
+      }
+    } else if (msc_large) {  // clusters of 2 against clusters of 4
+      std::vector<char> all(H->npop, 1);
+      double best = 0;
+      for (int tcs = 2; tcs <= 4 && e == cudaSuccess; tcs *= 2) {
+        const int th = msc_cluster_threads(tcs, maxL);
+        std::vector<SweepGeom> gc(H->npop);
+        for (int k = 0; k < H->npop; ++k) msc_cluster_geom(H->pops[k].cfg.L, tcs, th, &gc[k]);
+        double t = 0;
+        e = H->time_sweep(state, all, gc, false, &t, tcs, th);
+        if (e == cudaSuccess && t > 0 && (best == 0 || t < best)) {
+          best = t;
+          H->cs = tcs;
+          H->cthreads = th;
+          for (int k = 0; k < H->npop; ++k) {
+            H->pops[k].geom = gc[k];
+            geom_to_pop(gc[k], &H->pops[k].h);
+          }
+        }
       }
     } else {  // SSC: bit-plane replicas per tile for every lattice size, then the form of the batch
       std::vector<char> all(H->npop, 1);

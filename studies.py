@@ -7,6 +7,7 @@ repository root):
     python studies.py reference_large [--out FILE]
     python studies.py populations [--coding msc|ssc] [--out FILE]
     python studies.py small       [--out FILE]
+    python studies.py large_clusters [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
@@ -231,15 +232,50 @@ def small(cases=((64, (2500, 5000, 7500, 10000, 12500, 15000, 20000, 25000, 3000
     return res
 
 
+def large_clusters(cases=((256, (1000, 2000, 2600, 3000, 8000, 20000, 65536)), (224, (3000, 20000)),
+                           (192, (1000, 3000, 8000, 30000)), (160, (1000, 5000, 20000)), (144, (3000,)))) -> dict:
+    """Lattices above L = 128 (a group needs a cluster) with few groups:
+    clusters of 2 CTAs (1024 threads) against clusters of 4 (512 threads),
+    the engine's automatic choice and pa_autotune's; MSC, native stream, 50
+    sweeps, dbeta=0.05 up to beta = 1 (20 temperatures, whole anneals)."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    res = {"cases": []}
+    for L, Rs in cases:
+        for R in Rs:
+            row = {"L": L, "R": R, "groups": (R + 31) // 32}
+            for name, v in (("automatic", 0), ("clusters2", 2), ("clusters4", 4), ("autotuned", 0)):
+                with pa.Engine(L=L, R=R, sweeps=50, dbeta=0.05, seed=7, coding="msc", sweep_variant=v) as e:
+                    if name == "autotuned":
+                        e.autotune()
+                    e.run()
+                    ms = att = 0.0
+                    for _ in range(2):
+                        flush.zero_()
+                        torch.cuda.synchronize()
+                        e.run()
+                        m, a = e.timing()
+                        ms += m
+                        att += a
+                    row[name] = round(att / (ms * 1e6), 1)
+                    if v == 0:
+                        row[name + "_cluster_ctas"] = e.sweep_form(0)["cluster_ctas"]
+            res["cases"].append(row)
+            print(json.dumps(row), flush=True)
+    return res
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations", "small"])
+    ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations", "small",
+                                          "large_clusters"])
     ap.add_argument("--out", default=None)
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
     r = batch(coding=a.coding) if a.study == "batch" else \
         {"precision": precision, "large": large, "reference_large": reference_large,
-         "populations": lambda: populations(coding=a.coding), "small": small}[a.study]()
+         "populations": lambda: populations(coding=a.coding), "small": small,
+         "large_clusters": large_clusters}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0

@@ -177,3 +177,22 @@ def test_autotune_chooses_between_one_cta_and_clusters(cuda, oracle, L, R):
     ref = oracle.anneal_msc_native(L, R, 2, 0.1, 0.4, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256, f["tile"],
                                    max(1, f["cluster_ctas"]))
     compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,R", [(192, 3000), (256, 1000)])
+def test_autotune_large_lattice_cluster_size(cuda, oracle, L, R):
+    """Above L = 128 pa_autotune times clusters of 2 CTAs (1024 threads)
+    against clusters of 4 (512 threads) and keeps the faster; the anneal
+    equals the oracle's restatement of the kept form."""
+    seed = 650 + L
+    with pa.Engine(L=L, R=R, sweeps=2, dbeta=0.25, beta_final=0.5, seed=seed, coding="msc", rng="native",
+                   weights="fp64") as e:
+        e.autotune()
+        f = e.sweep_form(0)
+        assert f["cluster_ctas"] in (2, 4), f
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_msc_native(L, R, 2, 0.25, 0.5, 1, seed, seed, oracle.NATIVE_TAG_MSC,
+                                   {2: 1024, 4: 512}[f["cluster_ctas"]], 1, f["cluster_ctas"])
+    compare_rows(got, ref[0], rtol=2e-10)

@@ -301,6 +301,38 @@ def test_automatic_clusters_for_small_populations(cuda, oracle, L, R, cs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("L,R,cs", [(256, 1000, 2), (256, 5000, 4), (144, 3000, 4), (192, 3000, 4)])
+def test_automatic_clusters_for_large_lattices(cuda, oracle, L, R, cs):
+    """Above L = 128 a population left to the engine is swept by clusters of
+    4 CTAs of 512 threads when its groups exceed one resident wave of
+    clusters of 2 (1024 threads, one CTA per SM: about 72-76 clusters on a
+    GB300) and stay within eight such waves, else by clusters of 2; the
+    anneal equals the oracle's restatement of that form."""
+    from conftest import compare_rows
+    seed = 700 + L
+    with pa.Engine(L=L, R=R, sweeps=2, dbeta=0.25, beta_final=0.5, seed=seed, coding="msc", rng="native",
+                   weights="fp64", graph=True, device=0) as e:
+        f = e.sweep_form(0)
+        assert f["cluster_ctas"] == cs, f
+        e.run()
+        got = e.rows(0)
+    ref = oracle.anneal_msc_native(L, R, 2, 0.25, 0.5, 1, seed, seed, oracle.NATIVE_TAG_MSC, {2: 1024, 4: 512}[cs],
+                                   1, cs)
+    compare_rows(got, ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
+def test_automatic_clusters_for_many_large_groups(cuda):
+    """2048 groups at L = 256 (far beyond eight waves of clusters of 2) keep
+    clusters of 2, as does a population that asks for them."""
+    with pa.Engine(L=256, R=65536, sweeps=1, dbeta=0.5, beta_final=0.5, coding="msc", device=0) as e:
+        assert e.sweep_form(0)["cluster_ctas"] == 2
+    with pa.Engine(L=256, R=5000, sweeps=1, dbeta=0.5, beta_final=0.5, coding="msc", sweep_variant=2,
+                   device=0) as e:
+        assert e.sweep_form(0)["cluster_ctas"] == 2
+
+
+@pytest.mark.gpu
 def test_automatic_clusters_in_a_mixed_batch(cuda, oracle):
     """Populations of L = 64, 96 and 128 in one small batch share one
     automatically chosen cluster form (compile-time paths for 64 and 128, the
