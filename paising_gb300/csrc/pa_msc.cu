@@ -5,7 +5,7 @@
 //   checkKerALL  (PAisingMSC.cu:191-266)  -> msc_sweep_kernel (group resident in
 //   energyKer    (PAisingMSC.cu:268-317)     shared memory for all sweeps; per
 //                                            replica energy and magnetisation by
-//                                            warp ballots in the epilogue)
+//                                            bitsliced counters in the epilogue)
 //   resampleKer  (PAisingMSC.cu:397-435)  -> msc_resample_kernel (gather: each new
 //                                            word assembles its 32 source bits,
 //                                            no atomics, no memset)
@@ -124,16 +124,18 @@ __device__ __noinline__ void msc_move_tile(const UnitParams& P, uint32_t* lat, i
 }
 
 // Energy and magnetisation per replica bit of the tile: the left and up
-// bond of every A and B site (PAisingMSC.cu:272-294), counted per bit with
-// warp ballots into cntE / cntM [group of the tile][bit].  Each warp works
-// inside one group (kSweepThreads/32/G warps per group), so a ballot never
-// mixes groups.
+// bond of every A and B site (PAisingMSC.cu:272-294), counted per bit in
+// bitsliced counters (BitCounters) and added into cntE / cntM [group of the
+// tile][bit].  Each warp works inside one group (kSweepThreads/32/G warps per
+// group, at most h / (32 wpg) <= 32 words per lane), so its counts never mix
+// groups.
 __device__ __noinline__ void msc_count(const UnitParams& P, const uint32_t* lat, int gc, int* cntE, int* cntM) {
   const int tid = threadIdx.x, lane = tid & 31;
   const int L = P.L, Wr = P.Wr, h = P.h, G = P.G, wpg = (kSweepThreads / 32) / G;
   const int w = tid >> 5, g = w / wpg, ws = w - g * wpg;
-  int cE = 0, cM = 0;  // lane k accumulates bit k
   if (g >= gc) return;  // warp-uniform
+  BitCounters bc;
+  bc.reset();
   const uint32_t* A = G == 1 ? lat + Wr : lat + g * h;
   const uint32_t* B = G == 1 ? lat + P.sb + Wr : lat + G * h + g * h;
   for (int j0 = ws * 32; j0 < h; j0 += wpg * 32) {
@@ -149,14 +151,10 @@ __device__ __noinline__ void msc_count(const UnitParams& P, const uint32_t* lat,
       else { Ai2 = B[iL]; Bi2 = sA; }
       adder4(sA ^ Ai2, sA ^ B[iU], sB ^ Bi2, sB ^ A[iU], s0, s1, s2);
     }
-#pragma unroll 4
-    for (int k = 0; k < kMsb; ++k) {
-      const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
-                    4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
-      const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
-      if (lane == k) { cE += e; cM += m; }
-    }
+    bc.add(s0, s1, s2, sA, sB);
   }
+  int cE, cM;  // lane k: bit k
+  bc.totals(lane, cE, cM);
   atomicAdd(&cntE[g * kMsb + lane], cE);
   atomicAdd(&cntM[g * kMsb + lane], cM);
 }
@@ -610,13 +608,22 @@ __global__ void __launch_bounds__(kResampleThreads, kResampleBlocksPerSM) msc_re
 // of 1 keep the shift; a duplicate lowers it by one, a replica without
 // offspring raises it, so a word has a handful of distinct shifts.
 //
+// Copies of one parent are the exception: a run of k new bits with the same
+// source has k distinct shifts, so a parent with many copies (a large dbeta
+// against the energy spread) would turn a word into 32 single-bit pairs.
+// Such a run is one broadcast pair instead: the run's mask M and the
+// source's position p in the window, new |= M & -(bit p of W).
+//
 // msc_pairs_kernel (one warp per new group of every population, lane b for
-// bit b) lists a group's distinct shifts as (M_d, d mod 32) pairs ordered by
-// the window word d / 32 they start in (counts n0, n1, n2): the lanes sharing
-// a shift find each other with one match, and the lowest of them writes the
-// pair.  A group whose sources span more than the four-word window (more
-// than 64 replicas without offspring among ~96 consecutive ones) is flagged
-// and gathered bit by bit.
+// bit b) lists a group's distinct shifts of single-copy bits as (M_d, d mod
+// 32) pairs ordered by the window word d / 32 they start in (counts n0, n1,
+// n2), then its runs of one source as (M, 31 - p mod 32) pairs ordered by the
+// window word p / 32 holding the source (counts k1, k2, k3): the lanes
+// sharing a shift or a source find each other with one match each, and the
+// lowest of them writes the pair.  A group whose sources span more than the
+// four-word window (more than 64 replicas without offspring among ~96
+// consecutive ones), or whose counts do not fit the 5-bit fields of its count
+// word, is flagged and gathered bit by bit.
 __global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
   const int lane = threadIdx.x & 31, np = b->npop, total = b->grp_prefix[np];
   const uint32_t lt = (1u << lane) - 1u;
@@ -631,21 +638,35 @@ __global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
     const int j = i - b->grp_prefix[lo], nb = min(kMsb, st->R_cur - j * kMsb);
     const uint32_t* src = st->src + (size_t)j * kMsb;
     const bool v = lane < nb;
-    // shift of bit b: d = src[b] - 32 (first - 1) - b >= 1 (src nondecreasing, src[0] >= 32 first)
+    // source of bit b relative to the window, o = src[b] - 32 (first - 1) >= 32
+    // (src nondecreasing, src[0] >= 32 first), and its shift d = o - b >= 1
     const uint32_t base = ((src[0] >> 5) - 1u) * 32u;  // may wrap; only differences matter
-    const uint32_t d = v ? src[lane] - base - (uint32_t)lane : 0xFFFFFFFFu;
-    const bool fallback = __any_sync(kFull, v && d >= 96u);
-    const uint32_t m = __match_any_sync(kFull, d);  // bits sharing this shift (the invalid ones share 0xFFFFFFFF)
-    const bool leader = v && (m & lt) == 0u;
-    const uint32_t word = d >> 5;
-    const uint32_t l0 = __ballot_sync(kFull, leader && word == 0u), l1 = __ballot_sync(kFull, leader && word == 1u),
-                   l2 = __ballot_sync(kFull, leader && word == 2u);
-    const uint32_t n0 = __popc(l0), n1 = __popc(l1), n2 = __popc(l2);
-    if (!fallback && leader && word < 3u) {
-      const uint32_t at = word == 0u ? __popc(l0 & lt) : word == 1u ? n0 + __popc(l1 & lt) : n0 + n1 + __popc(l2 & lt);
+    const uint32_t s = v ? src[lane] : 0xFFFFFFFFu;    // the invalid bits share 0xFFFFFFFF
+    const uint32_t o = s - base, d = o - (uint32_t)lane;
+    bool fallback = __any_sync(kFull, v && d >= 96u);  // then o < 128 for every bit
+    const uint32_t ms = __match_any_sync(kFull, s);    // bits with this bit's source
+    const bool run = v && __popc(ms) > 1;
+    const uint32_t m = __match_any_sync(kFull, v && !run ? d : 0xFFFFFFFFu);  // single-copy bits with this shift
+    const bool lead_d = v && !run && (m & lt) == 0u, lead_r = run && (ms & lt) == 0u;
+    const uint32_t wd = d >> 5, wr = o >> 5;
+    const uint32_t l0 = __ballot_sync(kFull, lead_d && wd == 0u), l1 = __ballot_sync(kFull, lead_d && wd == 1u),
+                   l2 = __ballot_sync(kFull, lead_d && wd == 2u), r1 = __ballot_sync(kFull, lead_r && wr == 1u),
+                   r2 = __ballot_sync(kFull, lead_r && wr == 2u), r3 = __ballot_sync(kFull, lead_r && wr == 3u);
+    const uint32_t n0 = __popc(l0), n1 = __popc(l1), n2 = __popc(l2), k1 = __popc(r1), k2 = __popc(r2),
+                   k3 = __popc(r3);
+    fallback = fallback || n0 > 31u || n1 > 31u || n2 > 31u;  // a run has two bits: k <= 16
+    if (!fallback && lead_d && wd < 3u) {
+      const uint32_t at = wd == 0u ? __popc(l0 & lt) : wd == 1u ? n0 + __popc(l1 & lt) : n0 + n1 + __popc(l2 & lt);
       st->res_pairs[(size_t)j * kMsb + at] = make_uint2(m, d & 31u);
     }
-    if (lane == 0) st->res_cnt[j] = fallback ? 1u << 31 : n0 | n1 << 8 | n2 << 16;
+    if (!fallback && lead_r) {
+      const uint32_t c = n0 + n1 + n2;
+      const uint32_t at = wr == 1u ? c + __popc(r1 & lt) : wr == 2u ? c + k1 + __popc(r2 & lt)
+                                                                  : c + k1 + k2 + __popc(r3 & lt);
+      st->res_pairs[(size_t)j * kMsb + at] = make_uint2(ms, 31u - (o & 31u));
+    }
+    if (lane == 0)
+      st->res_cnt[j] = fallback ? 1u << 31 : n0 | n1 << 5 | n2 << 10 | k1 << 15 | k2 << 20 | k3 << 25;
   }
 }
 
@@ -663,6 +684,18 @@ __device__ __forceinline__ void nat_apply(uint32_t (&out)[2], const uint32_t (&l
     const uint2 a = pg[i];
     out[0] |= __funnelshift_r(lo[0], hi[0], a.y) & a.x;
     out[1] |= __funnelshift_r(lo[1], hi[1], a.y) & a.x;
+  }
+}
+
+// broadcast pairs (M, 31 - p): bit p of the window word w, copied to every
+// bit of M (the shift left puts bit p on top, the arithmetic shift spreads it)
+__device__ __forceinline__ void nat_bcast(uint32_t (&out)[2], const uint32_t (&w)[2], const uint2* pg, int i0,
+                                          int i1) {
+#pragma unroll 1
+  for (int i = i0; i < i1; ++i) {
+    const uint2 a = pg[i];
+    out[0] |= (uint32_t)((int32_t)(w[0] << a.y) >> 31) & a.x;
+    out[1] |= (uint32_t)((int32_t)(w[1] << a.y) >> 31) & a.x;
   }
 }
 
@@ -732,12 +765,16 @@ __global__ void __launch_bounds__(kNatThreads, kNatBlocksPerSM) msc_resample_nat
       for (int g = 0; g < kNatBatch; ++g) {
         if (g >= nbat) break;  // warp-uniform
         const uint32_t cnt = __shfl_sync(kFull, cnt_l, g0 + g);
-        const int n0 = cnt & 0xff, n01 = n0 + ((cnt >> 8) & 0xff), n012 = n01 + ((cnt >> 16) & 0xff);
+        const int c1 = cnt & 31u, c2 = c1 + ((cnt >> 5) & 31u), c3 = c2 + ((cnt >> 10) & 31u);
+        const int c4 = c3 + ((cnt >> 15) & 31u), c5 = c4 + ((cnt >> 20) & 31u), c6 = c5 + ((cnt >> 25) & 31u);
         const uint2* pg = sp + g * kMsb;
         uint32_t out[2] = {0u, 0u};
-        nat_apply(out, W[g][0], W[g][1], pg, 0, n0);
-        nat_apply(out, W[g][1], W[g][2], pg, n0, n01);
-        nat_apply(out, W[g][2], W[g][3], pg, n01, n012);
+        nat_apply(out, W[g][0], W[g][1], pg, 0, c1);
+        nat_apply(out, W[g][1], W[g][2], pg, c1, c2);
+        nat_apply(out, W[g][2], W[g][3], pg, c2, c3);
+        nat_bcast(out, W[g][1], pg, c3, c4);
+        nat_bcast(out, W[g][2], pg, c4, c5);
+        nat_bcast(out, W[g][3], pg, c5, c6);
         const int j = j0 + g0 + g;
         if (cnt >> 31) {  // sources beyond the window: bit by bit (warp-uniform)
           const int nb = min(kMsb, Rn - j * kMsb);

@@ -56,7 +56,8 @@ __device__ __noinline__ void cluster_count(const UnitParams& P, const uint32_t* 
   const int Wr = P.Wr, rpp = P.rpp, npass = P.npass, lane = threadIdx.x & 31;
   const uint32_t* A = lat + Wr;
   const uint32_t* Bs = lat + SH + Wr;
-  int cE = 0, cM = 0;
+  BitCounters bc;  // npass <= 32 words per lane
+  bc.reset();
   for (int pass = 0; pass < npass; ++pass) {
     const int lr = rsub + pass * rpp;
     const bool valid = worker && lr < LR;
@@ -71,14 +72,10 @@ __device__ __noinline__ void cluster_count(const UnitParams& P, const uint32_t* 
       const uint32_t Ai4 = Bs[row + Wr + tx], Bi4 = A[row + Wr + tx];
       adder4(sA ^ Ai2, sA ^ Ai4, sB ^ Bi2, sB ^ Bi4, s0, s1, s2);
     }
-#pragma unroll 4
-    for (int k = 0; k < kMsb; ++k) {
-      const int e = __popc(__ballot_sync(kFull, (s0 >> k) & 1u)) + 2 * __popc(__ballot_sync(kFull, (s1 >> k) & 1u)) +
-                    4 * __popc(__ballot_sync(kFull, (s2 >> k) & 1u));
-      const int m = __popc(__ballot_sync(kFull, (sA >> k) & 1u)) + __popc(__ballot_sync(kFull, (sB >> k) & 1u));
-      if (lane == k) { cE += e; cM += m; }
-    }
+    bc.add(s0, s1, s2, sA, sB);
   }
+  int cE, cM;  // lane k: bit k
+  bc.totals(lane, cE, cM);
   atomicAdd(&cntE[lane], cE);
   atomicAdd(&cntM[lane], cM);
 }

@@ -28,6 +28,61 @@ __device__ __forceinline__ void adder4(uint32_t I1, uint32_t I2, uint32_t I3, ui
   s2 = a12 & a34;
 }
 
+// Per-replica-bit sums over the words of a warp, for the energy epilogue.
+// Each lane adds its words' bond counts (0..4 per word, as adder4's planes
+// s0 + 2 s1 + 4 s2) and spin bits into bitsliced counters -- bit k of plane
+// l holds bit l of the lane's running count for replica bit k -- at a few
+// logic operations per word instead of a warp vote per replica bit.  At the
+// end each plane is transposed across the warp (bit i of lane k <- bit k of
+// lane i) and counted, so lane k receives bit k's sums over the warp.  Eight
+// and seven planes hold the counts of up to 63 words per lane.
+struct BitCounters {
+  uint32_t e[8], m[7];
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) e[l] = 0u;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) m[l] = 0u;
+  }
+  // c += x << at, bit by bit (ripple of half adders)
+  template <int NL>
+  __device__ __forceinline__ static void ripple(uint32_t (&c)[NL], int at, uint32_t x) {
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+      if (l >= at) {
+        const uint32_t t = c[l] & x;
+        c[l] ^= x;
+        x = t;
+      }
+  }
+  __device__ __forceinline__ void add(uint32_t s0, uint32_t s1, uint32_t s2, uint32_t sA, uint32_t sB) {
+    ripple(e, 0, s0);
+    ripple(e, 1, s1);
+    ripple(e, 2, s2);
+    ripple(m, 0, sA ^ sB);
+    ripple(m, 1, sA & sB);
+  }
+  __device__ __forceinline__ static uint32_t transpose(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j >= 1; j >>= 1) {
+      const uint32_t lo = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu
+                                                 : j == 2 ? 0x33333333u : 0x55555555u;  // bit positions b & j == 0
+      const uint32_t y = __shfl_xor_sync(kFull, x, j);
+      x = (lane & j) ? (x & ~lo) | ((y >> j) & lo) : (x & lo) | ((y & lo) << j);
+    }
+    return x;
+  }
+  // whole warp: lane k gets the sums of replica bit k
+  __device__ __forceinline__ void totals(int lane, int& cE, int& cM) const {
+    cE = 0;
+    cM = 0;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) cE += __popc(transpose(e[l], lane)) << l;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) cM += __popc(transpose(m[l], lane)) << l;
+  }
+};
+
 // The two masks the acceptance needs from a word's four neighbour words:
 // odd = an odd number of anti-parallel neighbours (among undecided bits: one,
 // threshold T4), ge2 = two or more (dE <= 0: flipped outright) -- adder4's s0

@@ -210,23 +210,43 @@ __global__ void __launch_bounds__(kResThreads) copy_numbers_kernel(PopDev* pops)
 
 // ------------------------------------------------------------------ scatter
 // offs_j = exclusive prefix of roff; src[offs_j + p] = j for p < roff_j.
+// The new replicas of a tile of 256 old ones are filled by the whole block,
+// new index i taking the last old replica of the tile whose offset is <= i
+// (a binary search over the tile's offsets in shared memory): one old
+// replica with thousands of copies -- a large dbeta against the energy
+// spread makes them -- costs the block a few passes instead of leaving one
+// thread to write them all.
 __global__ void __launch_bounds__(kResThreads) scatter_kernel(PopDev* pops) {
   __shared__ uint32_t s_u[33];
+  __shared__ uint32_t s_off[kResThreads + 1];
   PopDev* st = pops + blockIdx.y;
   if (!pop_stepping(st)) return;
   const int n = pop_units(st, st->R_prev);
   int lo, hi;
   block_chunk(n, lo, hi);
   uint32_t run = st->blk_off[blockIdx.x];
-  for (int base = lo; base < hi; base += blockDim.x) {
+  const int nt = blockDim.x;
+  for (int base = lo; base < hi; base += nt) {
     const int j = base + threadIdx.x;
     const uint32_t r = j < hi ? st->roff[j] : 0u;
     uint32_t total;
     const uint32_t off = run + block_exscan(r, s_u, &total);
-    if (j < hi) {
-      st->offs[j] = off;
-      for (uint32_t p = 0; p < r; ++p) st->src[off + p] = (uint32_t)j;
+    if (j < hi) st->offs[j] = off;
+    s_off[threadIdx.x] = off;  // non-decreasing; equal to run + total past hi
+    if (threadIdx.x == 0) s_off[nt] = run + total;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < total; t += nt) {
+      const uint32_t i = run + t;
+      // last k with s_off[k] <= i: s_off[0] = run <= i < s_off[nt]
+      int a = 0, b = nt;
+      while (b - a > 1) {
+        const int m = (a + b) >> 1;
+        if (s_off[m] <= i) a = m;
+        else b = m;
+      }
+      st->src[i] = (uint32_t)(base + a);
     }
+    __syncthreads();
     run += total;
   }
 }

@@ -98,7 +98,8 @@ struct PopDev {
   // source shifts of its bits as (bit mask, shift) pairs, grouped by which
   // pair of window words they read, and their counts (msc_pairs_kernel)
   uint2* res_pairs;    // [rgcap][32]
-  uint32_t* res_cnt;   // [rgcap]: n0 | n1 << 8 | n2 << 16 | per-bit fallback << 31
+  uint32_t* res_cnt;   // [rgcap]: pair counts n0 | n1 << 5 | n2 << 10 | k1 << 15 | k2 << 20 | k3 << 25,
+                       // per-bit fallback << 31
 };
 
 constexpr int kRecMhr = 1, kRecEnergies = 2;

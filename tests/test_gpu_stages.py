@@ -107,6 +107,45 @@ def test_resample_plan_fp64(cuda, st, oracle, coding, L, R):
 
 
 @pytest.mark.parametrize("coding", ["ssc", "msc"])
+def test_resample_plan_concentrated_copies(cuda, st, oracle, coding):
+    """A few replicas far below the others in energy take nearly all the
+    copies (thousands each: one alone in its tile of 256, two in the same
+    tile, one in the last tile), as a large dbeta against the energy spread
+    makes them; the map of new to old replicas is still CalcParSum's."""
+    torch = cuda
+    L, R = 16, 6000
+    _, E, act = _energies(oracle, coding, L, R, 33, 0.3)
+    E = E.copy()
+    heavy = [300, 1024, 1030, len(E) - 40]
+    if act is not None:
+        heavy = [int(np.flatnonzero(act[h:])[0]) + h for h in heavy]
+    for k, h in enumerate(heavy):
+        E[h] -= 900 + 40 * k
+    b0, b1, seed, iseq = 0.3, 0.31, 5, 77
+    dB = b1 - b0
+    valid = E if act is None else E[act.astype(bool)]
+    Emean = float(valid.mean())
+    if coding == "ssc":
+        q = oracle.ssc_q(E, dB, Emean)
+        lnQ = -dB * Emean + np.log(q) - np.log(R)
+        roff, Rn = oracle.ssc_copy_numbers(E, R, lnQ, dB, seed, iseq)
+    else:
+        q = oracle.msc_q(E, act, dB, Emean)
+        lnQ = -dB * Emean + np.log(q) - np.log(R)
+        roff, Rn = oracle.msc_copy_numbers(E, act, R, R, lnQ, dB, seed, iseq)
+    assert roff[heavy].min() > 400 and roff[heavy].sum() > 0.9 * R, roff[heavy]
+    offs, tot = oracle.scan(roff)
+    Et = torch.from_numpy(E).cuda()
+    actt = None if act is None else torch.from_numpy(act).cuda()
+    groff, goffs, gsrc, glnQ, gq, gRn = st.resample_plan(Et, actt, pa.SSC if coding == "ssc" else pa.MSC, R, R,
+                                                         2 * R, b0, b1, Emean, pa.WEIGHTS_FP64, seed, iseq)
+    assert gRn == Rn == tot
+    assert np.array_equal(groff.cpu().numpy().view(np.uint32), roff)
+    assert np.array_equal(goffs.cpu().numpy().view(np.uint32), offs)
+    assert np.array_equal(gsrc[:Rn].cpu().numpy(), np.repeat(np.arange(len(roff)), roff))
+
+
+@pytest.mark.parametrize("coding", ["ssc", "msc"])
 def test_resample_plan_fp32_close_to_fp64(cuda, st, oracle, coding):
     """FP32 compensated weights: lnQ within 1e-6 of the FP64 value, copy
     numbers identical except where U falls within FP32 round-off of the
@@ -158,7 +197,8 @@ def test_msc_resample_gather(cuda, st, oracle, L, R):
 
 @pytest.mark.parametrize("L,R,kind", [(16, 200, "mixed"), (12, 70, "mixed"), (64, 3000, "mixed"),
                                       (64, 5000, "identity"), (32, 4000, "sparse"), (128, 700, "bursty"),
-                                      (10, 33, "mixed"), (256, 100, "mixed"), (16, 900, "gap")])
+                                      (10, 33, "mixed"), (256, 100, "mixed"), (16, 900, "gap"),
+                                      (16, 3000, "copies"), (64, 2000, "concentrated"), (24, 1500, "alternating")])
 def test_msc_resample_gather_native(cuda, st, oracle, L, R, kind):
     """The native stream's gather (offspring s at slot s) equals the oracle's
     restatement bit for bit, active flags included: copy numbers of 0..3
@@ -166,7 +206,10 @@ def test_msc_resample_gather_native(cuda, st, oracle, L, R, kind):
     sources far apart, many per-bit fallbacks), and runs of 0 and of 3
     (bursty: long duplicate runs), and one run of 150 replicas without
     offspring (gap: sources beyond the four-word window, gathered bit by
-    bit)."""
+    bit); 0..9 copies each (copies: runs of one source as broadcast pairs
+    beside shifted single copies), a few parents with hundreds of copies
+    among single ones (concentrated: whole words of one source), and 2 and 0
+    copies in turn (alternating: runs of two beside every gap)."""
     torch = cuda
     old, act = oracle.msc_init(L, R, 4, 0)
     rng = np.random.default_rng(R + L)
@@ -179,6 +222,13 @@ def test_msc_resample_gather_native(cuda, st, oracle, L, R, kind):
         roff = np.where(rng.random(n) < 0.2, 4, 0)
     elif kind == "bursty":
         roff = np.repeat(rng.choice([0, 1, 3], size=n // 40 + 1, p=[0.4, 0.3, 0.3]), 40)[:n]
+    elif kind == "copies":
+        roff = rng.integers(0, 10, n)
+    elif kind == "concentrated":
+        roff = np.where(rng.random(n) < 0.5, 1, 0)
+        roff[rng.choice(n, 6, replace=False)] = [300, 150, 97, 64, 33, 500]
+    elif kind == "alternating":
+        roff = np.tile([2, 0], n // 2 + 1)[:n]
     else:  # one copy each, but 150 replicas in a row without offspring
         roff = np.ones(n, dtype=np.int64)
         roff[300:450] = 0

@@ -164,9 +164,11 @@ def test_autotune_chooses_between_one_cta_and_clusters(cuda, oracle, L, R):
     """pa_autotune also times clusters of 2 and 4 CTAs per group against the
     tuned one-CTA sweep for a population at 48 <= L <= 128; whichever form
     it keeps, the native-stream anneal equals the oracle's restatement of
-    that form (small populations are expected to land on clusters)."""
+    that form (small populations are expected to land on clusters: at 20
+    sweeps per temperature the sweeps, not the per-unit loading and energy
+    epilogue, decide)."""
     seed = 600 + L
-    with pa.Engine(L=L, R=R, sweeps=2, dbeta=0.1, beta_final=0.4, seed=seed, coding="msc", rng="native",
+    with pa.Engine(L=L, R=R, sweeps=20, dbeta=0.1, beta_final=0.4, seed=seed, coding="msc", rng="native",
                    weights="fp64") as e:
         e.autotune()
         f = e.sweep_form(0)
@@ -174,7 +176,7 @@ def test_autotune_chooses_between_one_cta_and_clusters(cuda, oracle, L, R):
             assert f["cluster_ctas"] > 1, f
         e.run()
         got = e.rows(0)
-    ref = oracle.anneal_msc_native(L, R, 2, 0.1, 0.4, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256, f["tile"],
+    ref = oracle.anneal_msc_native(L, R, 20, 0.1, 0.4, 1, seed, seed, oracle.NATIVE_TAG_MSC, 256, f["tile"],
                                    max(1, f["cluster_ctas"]))
     compare_rows(got, ref[0], rtol=2e-10)
 
