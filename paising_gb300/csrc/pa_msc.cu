@@ -611,16 +611,16 @@ __global__ void __launch_bounds__(kResampleThreads, kResampleBlocksPerSM) msc_re
 // Copies of one parent are the exception: a run of k new bits with the same
 // source has k distinct shifts, so a parent with many copies (a large dbeta
 // against the energy spread) would turn a word into 32 single-bit pairs.
-// Such a run is one broadcast pair instead: the run's mask M and the
-// source's position p in the window, new |= M & -(bit p of W).
+// A run of four or more is one broadcast pair instead: the run's mask M and
+// the source's position p in the window, new |= M & -(bit p of W).
 //
 // msc_pairs_kernel (one warp per new group of every population, lane b for
-// bit b) lists a group's distinct shifts of single-copy bits as (M_d, d mod
-// 32) pairs ordered by the window word d / 32 they start in (counts n0, n1,
-// n2), then its runs of one source as (M, 31 - p mod 32) pairs ordered by the
-// window word p / 32 holding the source (counts k1, k2, k3): the lanes
-// sharing a shift or a source find each other with one match each, and the
-// lowest of them writes the pair.  A group whose sources span more than the
+// bit b) lists a group's distinct shifts of the other bits as (M_d, d mod 32)
+// pairs ordered by the window word d / 32 they start in (counts n0, n1, n2),
+// then its runs of four or more bits of one source as (M, 31 - p mod 32)
+// pairs ordered by the window word p / 32 holding the source (counts k1, k2,
+// k3): the lanes sharing a shift or a source find each other with one match
+// each, and the lowest of them writes the pair.  A group whose sources span more than the
 // four-word window (more than 64 replicas without offspring among ~96
 // consecutive ones), or whose counts do not fit the 5-bit fields of its count
 // word, is flagged and gathered bit by bit.
@@ -644,9 +644,12 @@ __global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
     const uint32_t s = v ? src[lane] : 0xFFFFFFFFu;    // the invalid bits share 0xFFFFFFFF
     const uint32_t o = s - base, d = o - (uint32_t)lane;
     bool fallback = __any_sync(kFull, v && d >= 96u);  // then o < 128 for every bit
-    const uint32_t ms = __match_any_sync(kFull, s);    // bits with this bit's source
-    const bool run = v && __popc(ms) > 1;
-    const uint32_t m = __match_any_sync(kFull, v && !run ? d : 0xFFFFFFFFu);  // single-copy bits with this shift
+    // bits with this bit's source; a run of k >= 4 of them is one broadcast
+    // pair (as shifts its first and last bits join their neighbours' pairs,
+    // the k - 2 between take a pair each)
+    const uint32_t ms = __match_any_sync(kFull, s);
+    const bool run = v && __popc(ms) >= 4;
+    const uint32_t m = __match_any_sync(kFull, v && !run ? d : 0xFFFFFFFFu);  // bits outside runs with this shift
     const bool lead_d = v && !run && (m & lt) == 0u, lead_r = run && (ms & lt) == 0u;
     const uint32_t wd = d >> 5, wr = o >> 5;
     const uint32_t l0 = __ballot_sync(kFull, lead_d && wd == 0u), l1 = __ballot_sync(kFull, lead_d && wd == 1u),
@@ -654,7 +657,7 @@ __global__ void __launch_bounds__(256) msc_pairs_kernel(BatchDev* b) {
                    r2 = __ballot_sync(kFull, lead_r && wr == 2u), r3 = __ballot_sync(kFull, lead_r && wr == 3u);
     const uint32_t n0 = __popc(l0), n1 = __popc(l1), n2 = __popc(l2), k1 = __popc(r1), k2 = __popc(r2),
                    k3 = __popc(r3);
-    fallback = fallback || n0 > 31u || n1 > 31u || n2 > 31u;  // a run has two bits: k <= 16
+    fallback = fallback || n0 > 31u || n1 > 31u || n2 > 31u;  // a run has four bits: k <= 8
     if (!fallback && lead_d && wd < 3u) {
       const uint32_t at = wd == 0u ? __popc(l0 & lt) : wd == 1u ? n0 + __popc(l1 & lt) : n0 + n1 + __popc(l2 & lt);
       st->res_pairs[(size_t)j * kMsb + at] = make_uint2(m, d & 31u);
