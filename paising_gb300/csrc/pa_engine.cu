@@ -696,9 +696,9 @@ int msc_auto_clusters(const std::vector<pa_config>& cfgs, int cs, long long grou
 // Measured on L = 144..256 (profiles/study_large_lattice_clusters_msc.md):
 // with at most one wave the larger halo share and cluster barriers of
 // clusters of 4 cost more than they spread; just past one wave clusters of 2
-// run a nearly empty second wave (L=256: 63 groups 3795 vs 3162 attempts/ns,
-// 82 groups 2553 vs 3377); from about eight waves on both fill the GPU and
-// clusters of 2 do slightly less work per site.
+// run a nearly empty second wave (L=256, clusters of 2 vs 4: 63 groups 4095
+// vs 3897 attempts/ns, 82 groups 2723 vs 3599); from about eight waves on
+// both fill the GPU and clusters of 2 do slightly less work per site.
 int msc_auto_large_clusters(const std::vector<pa_config>& cfgs, int cs, long long groups, int rng_mode) {
   if (cs != 2) return cs;
   int maxL = 0, smem = 0;
