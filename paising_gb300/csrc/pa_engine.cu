@@ -664,7 +664,7 @@ int msc_variant(int requested, int L) { return requested ? requested : (L > 128 
 // slots busy runs each group on a cluster of 4 or 2 CTAs of 256 threads,
 // so that more SMs take part and the last wave is finer.  The thresholds
 // (groups as fractions of the slots, 608 on a GB300) come from the measured
-// crossovers (profiles/study_small_populations_msc.md): L=64 (compile-time
+// crossovers of whole single-population anneals on a GB300: L=64 (compile-time
 // cluster form for clusters of 2) clusters of 4 up to ~110 groups, of 2 up
 // to ~700; L=128 (compile-time forms for both; its one-CTA form fits three
 // CTAs per SM) 4 up to ~550, 2 up to ~2000; other sizes 4 up to ~200, 2 up to
@@ -693,7 +693,7 @@ int msc_auto_clusters(const std::vector<pa_config>& cfgs, int cs, long long grou
 // (which needs a cluster) and leaves the form to the engine: clusters of 4
 // CTAs of 512 threads from just over one resident wave of clusters of 2 (1024
 // threads, one CTA per SM) up to eight such waves, clusters of 2 otherwise.
-// Measured on L = 144..256 (profiles/study_large_lattice_clusters_msc.md):
+// Measured on whole anneals at L = 144..256 on a GB300:
 // with at most one wave the larger halo share and cluster barriers of
 // clusters of 4 cost more than they spread; just past one wave clusters of 2
 // run a nearly empty second wave (L=256, clusters of 2 vs 4: 63 groups 4095
