@@ -545,13 +545,13 @@ struct pa_handle {
   // Persistent sweep grid for the populations' current geometry and, in
   // graph mode, the run captured as one graph (again, after a re-tune).
   // The lattice size of a sweep kernel built for one size, when every
-  // population of the handle can use it (MSC, one group per work unit, one L).
+  // population of the handle can use it (MSC, one group per work unit, one
+  // L); kWith96 when only some can (the general kernel with that size's form).
   int fixed_l(const std::vector<SweepGeom>& geo) const {
     if (coding != PA_CODING_MSC || cs != 1 || rng_mode != PA_RNG_NATIVE || geo.empty()) return 0;
-    const int l = msc_fixed_l(geo[0].L, geo[0].G);
-    for (const auto& g : geo)
-      if (msc_fixed_l(g.L, g.G) != l) return 0;
-    return l;
+    int n = 0;
+    for (const auto& g : geo) n += msc_fixed_l(g.L, g.G) == 96;
+    return n == (int)geo.size() ? 96 : n > 0 ? kWith96 : 0;
   }
 
   cudaError_t setup_launches() {

@@ -44,13 +44,18 @@ bool ssc_geom(int L, SweepGeom* g);
 bool msc_geom(int L, SweepGeom* g, int tile = 0, long long groups = 0, int slots = 0);
 void geom_to_pop(const SweepGeom& g, PopDev* h);
 
+// fixed_l of a launch whose populations include L = 96 with one group per
+// work unit beside other sizes: the general MSC kernel with L = 96's
+// compile-time form as well
+constexpr int kWith96 = 1;
 struct SweepLaunch {
   int grid, block, smem;
-  int fixed_l;  // MSC, native stream: L of a kernel built for that one size (96), else 0
+  int fixed_l;  // MSC, native stream: 96, kWith96 or 0 (see sweep_setup)
 };
 // Persistent grid for a sweep kernel with `smem` bytes of dynamic shared memory.
-// fixed_l (MSC, native stream): every population of the launch has this L and
-// one group per work unit, and a kernel built for that size alone is used.
+// fixed_l (MSC, native stream): 96 -- every population of the launch has
+// L = 96 and one group per work unit, and a kernel built for that size alone
+// is used; kWith96 -- some do, beside other sizes; 0 -- none.
 cudaError_t sweep_setup(int coding, int rng_mode, int smem, SweepLaunch* out, int fixed_l = 0);
 // The fixed_l for MSC populations of lattice size L and G groups per work unit
 // (0 where no kernel is built for it).

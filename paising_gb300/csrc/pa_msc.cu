@@ -164,7 +164,10 @@ static_assert(kMaxTile * kMsb == kSweepThreads, "one thread per (group of the ti
 // with one group per work unit, holding that size's compile-time sweep alone.
 // Built for L = 96 only: the general kernel (FL = 0) carries the compile-time
 // forms of L = 64 and 128, measured as fast there as kernels of their own,
-// while adding L = 96's form to it cost L = 64 1% (register allocation).
+// while adding L = 96's form to it cost L = 64 2.4% (register allocation).
+// FL = kWith96 is the general kernel with L = 96's form as well, for batches
+// that mix L = 96 with other sizes (64 uneven populations: 2% faster than the
+// general kernel; L = 96 beside L = 64: 7%).
 template <int MODE, int FL>
 __global__ void __launch_bounds__(kSweepThreads, 4)
     msc_sweep_kernel(BatchDev* b, int energy_only, unsigned long long stream_seed) {
@@ -345,7 +348,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
               }
             }
           };
-          if constexpr (FL != 0) {
+          if constexpr (FL > kWith96) {
             if (G == 1 && P.L == FL) {  // block-uniform; anything else is a host error, recorded below
               native_fixed(std::integral_constant<int, FL>());
             } else if (tid == 0 && sw == 0 && hf == 0) {
@@ -355,6 +358,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
             native_fixed(std::integral_constant<int, 64>());
           } else if (G == 1 && P.L == 128) {
             native_fixed(std::integral_constant<int, 128>());
+          } else if (FL == kWith96 && G == 1 && P.L == 96) {
+            native_fixed(std::integral_constant<int, 96>());
           } else if (G == 1) {
             // one group, any other L: thread rsub owns the
             // consecutive rows rsub*npass .. rsub*npass + npass - 1 of column
@@ -865,11 +870,13 @@ int msc_fixed_l(int L, int G) { return G == 1 && L == 96 ? L : 0; }
 
 static const void* msc_sweep_fn(int rng_mode, int fixed_l) {
   if (rng_mode == kRefCoords) return (const void*)msc_sweep_kernel<kRefCoords, 0>;
-  return fixed_l == 96 ? (const void*)msc_sweep_kernel<kNative, 96> : (const void*)msc_sweep_kernel<kNative, 0>;
+  return fixed_l == 96         ? (const void*)msc_sweep_kernel<kNative, 96>
+         : fixed_l == kWith96 ? (const void*)msc_sweep_kernel<kNative, kWith96>
+                              : (const void*)msc_sweep_kernel<kNative, 0>;
 }
 
 cudaError_t msc_sweep_setup(int rng_mode, int smem, SweepLaunch* out, int fixed_l) {
-  if (rng_mode == kRefCoords || msc_fixed_l(fixed_l, 1) != fixed_l) fixed_l = 0;
+  if (rng_mode == kRefCoords || (fixed_l != 96 && fixed_l != kWith96)) fixed_l = 0;
   cudaError_t e = persistent_launch(msc_sweep_fn(rng_mode, fixed_l), kSweepThreads, smem, out);
   out->fixed_l = fixed_l;
   return e;
@@ -882,6 +889,8 @@ cudaError_t launch_msc_sweep(BatchDev* b, int rng_mode, int energy_only, unsigne
   } else {
     if (sl.fixed_l == 96)
       msc_sweep_kernel<kNative, 96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
+    else if (sl.fixed_l == kWith96)
+      msc_sweep_kernel<kNative, kWith96><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
     else
       msc_sweep_kernel<kNative, 0><<<sl.grid, sl.block, sl.smem, s>>>(b, energy_only, seed);
   }

@@ -301,6 +301,30 @@ def test_automatic_clusters_for_small_populations(cuda, oracle, L, R, cs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("sizes", [(96, 64, 32, 96), (96, 96, 96), (96, 128, 48)])
+def test_one_cta_batches_with_l96(cuda, oracle, sizes):
+    """One CTA per group (sweep_variant=1) for batches holding L = 96: all
+    of them L = 96 (the kernel built for that size alone) or mixed with
+    other sizes (the general kernel that also carries L = 96's compile-time
+    form, beside L = 64's and 128's and the general paths of L = 32 and 48);
+    each population equals the oracle's anneal of that population alone,
+    with its subsequence base and sweep tag."""
+    from conftest import compare_rows
+    pops = [dict(L=L, R=700 + 150 * k, seed=90 + k) for k, L in enumerate(sizes)]
+    common = dict(sweeps=2, dbeta=0.1, beta_final=0.5, coding="msc", rng="native", weights="fp64", graph=True,
+                  sweep_variant=1)
+    with pa.Engine.batch(pops, **common) as e:
+        forms = [e.sweep_form(k) for k in range(len(pops))]
+        assert all(f["cluster_ctas"] == 1 for f in forms), forms
+        e.run()
+        got = [e.rows(k) for k in range(len(pops))]
+    for k, p in enumerate(pops):
+        ref = oracle.anneal_msc_native(p["L"], p["R"], 2, 0.1, 0.5, 1, p["seed"], pops[0]["seed"],
+                                       oracle.NATIVE_TAG_MSC | k, 256, forms[k]["tile"], 1, iseq0=k << 40)
+        compare_rows(got[k], ref[0], rtol=2e-10)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("L,R,cs", [(256, 1000, 2), (256, 5000, 4), (144, 3000, 4), (192, 3000, 4)])
 def test_automatic_clusters_for_large_lattices(cuda, oracle, L, R, cs):
     """Above L = 128 a population left to the engine is swept by clusters of
