@@ -124,15 +124,30 @@ __global__ void __launch_bounds__(kResThreads) q_kernel(PopDev* pops) {
       st->qpart_f[2 * blockIdx.x] = bsum.s;
       st->qpart_f[2 * blockIdx.x + 1] = __fadd_rn(bsum.c, c);
     }
-    if (last_block(&st->ticket) && tid == 0) {
+    if (last_block(&st->ticket)) {
+      // thread t sums the partials of blocks t, t + 256, ... (all loads in
+      // flight at once), thread 0 then the 256 thread sums in thread order:
+      // a fixed order, so the result does not depend on block scheduling
       Comp32 t;
       float c = 0.f;
       const volatile float* qp = st->qpart_f;
-      for (int bb = 0; bb < (int)gridDim.x; ++bb) { t.add(qp[2 * bb]); c = __fadd_rn(c, qp[2 * bb + 1]); }
-      const float q = __fadd_rn(t.s, __fadd_rn(t.c, c));
-      st->q = (double)q;
-      st->lnQ = -dB * (double)Emin + log((double)q) - log((double)Rp);
-      st->ticket = 0;
+      for (int bb = tid; bb < (int)gridDim.x; bb += blockDim.x) {
+        t.add(qp[2 * bb]);
+        c = __fadd_rn(c, qp[2 * bb + 1]);
+      }
+      __syncthreads();  // the block sums above are done with s_f
+      s_f[0][tid] = t.s;
+      s_f[1][tid] = __fadd_rn(t.c, c);
+      __syncthreads();
+      if (tid == 0) {
+        Comp32 u;
+        float cc = 0.f;
+        for (int i = 0; i < (int)blockDim.x; ++i) { u.add(s_f[0][i]); cc = __fadd_rn(cc, s_f[1][i]); }
+        const float q = __fadd_rn(u.s, __fadd_rn(u.c, cc));
+        st->q = (double)q;
+        st->lnQ = -dB * (double)Emin + log((double)q) - log((double)Rp);
+        st->ticket = 0;
+      }
     }
   }
 }

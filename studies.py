@@ -8,6 +8,7 @@ repository root):
     python studies.py populations [--coding msc|ssc] [--out FILE]
     python studies.py small       [--out FILE]
     python studies.py large_clusters [--out FILE]
+    python studies.py sweeps      [--out FILE]
 
 precision: L in {32, 64, 128} (R = 1e6 at L=32, 1e5 at L=64 and 128), 100
     sweeps, dbeta=0.005, beta 0 -> 1, MSC, native stream; FP32 compensated
@@ -265,17 +266,47 @@ def large_clusters(cases=((256, (1000, 2000, 2600, 3000, 8000, 20000, 65536)), (
     return res
 
 
+def sweeps(cases=((64, 524288), (128, 131072), (256, 32768), (16, 524288)), counts=(5, 20, 100)) -> dict:
+    """Whole anneals with few and many sweeps per temperature: MSC, native
+    stream, FP32 weights, dbeta=0.05 up to beta = 1 (20 temperatures: strong
+    reweighting, so a few replicas take many copies), one population of each
+    size; attempts/ns (best of three runs after a warm-up, L2 flushed before
+    each) and the per-kernel device time of one further run."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    res = {"cases": []}
+    for L, R in cases:
+        for sw in counts:
+            with pa.Engine(L=L, R=R, sweeps=sw, dbeta=0.05, beta_final=1.0, seed=7, coding="msc") as e:
+                e.run()
+                best = None
+                for _ in range(3):
+                    flush.zero_()
+                    torch.cuda.synchronize()
+                    e.run()
+                    m, a = e.timing()
+                    if best is None or m < best[0]:
+                        best = (m, a)
+                prof = e.profile()
+            row = {"L": L, "R": R, "sweeps": sw, "attempts_per_ns": round(best[1] / (best[0] * 1e6), 1),
+                   "anneal_ms": round(best[0], 2),
+                   "kernels_ms": {k: round(v[1], 3) for k, v in prof.items()}}
+            res["cases"].append(row)
+            print(json.dumps(row), flush=True)
+    return res
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("study", choices=["precision", "batch", "large", "reference_large", "populations", "small",
-                                          "large_clusters"])
+                                          "large_clusters", "sweeps"])
     ap.add_argument("--out", default=None)
     ap.add_argument("--coding", choices=["msc", "ssc"], default="msc", help="batch study: spin coding")
     a = ap.parse_args(argv)
     r = batch(coding=a.coding) if a.study == "batch" else \
         {"precision": precision, "large": large, "reference_large": reference_large,
          "populations": lambda: populations(coding=a.coding), "small": small,
-         "large_clusters": large_clusters}[a.study]()
+         "large_clusters": large_clusters, "sweeps": sweeps}[a.study]()
     if a.out:
         json.dump(r, open(a.out, "w"), indent=1)
     return 0
